@@ -1,0 +1,340 @@
+"""ctypes binding of libaderdg_gpu.so (include/aderdg_gpu.h).
+
+The Solver class mirrors the reference driver (Euler/main.f90:24-100): one
+method per phase of the loop body, plus the fused step and the fused run.
+Arrays use the reference's Fortran layouts, flattened in Fortran order.
+There is no CPU fallback: every call goes to the CUDA library, and a missing
+library or a failing CUDA call raises.
+"""
+import ctypes
+import dataclasses
+import os
+
+import numpy as np
+
+from . import builder as _build
+
+SYS_ADVDIFF, SYS_EULER, SYS_BN = 0, 1, 2
+NVAR = {SYS_ADVDIFF: 1, SYS_EULER: 4, SYS_BN: 9}
+FP64, FP32_MIXED = 0, 1
+
+(A_UH, A_DUH, A_QHI, A_FHI, A_SHI, A_QBND, A_FBND, A_GRADQBND, A_FU, A_GU, A_FP, A_GP, A_LH, A_LMIN,
+ A_LMAX, A_RECOMPUTE, A_STATUS) = range(17)
+INT_ARRAYS = (A_RECOMPUTE, A_STATUS)
+
+IC_AD_ZERO, IC_AD_SINE = 0, 1
+IC_EULER_DMR, IC_EULER_VORTEX, IC_EULER_RP2D = 10, 11, 12
+IC_BN_RP1D, IC_BN_CYLINDER = 20, 21
+
+ERRORS = {0: "OK", -1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "ETIMEOUT", -5: "ENONFINITE", -6: "ESTATE",
+          -7: "EUNSUPPORTED", -8: "ENOSPACE"}
+
+
+class AderdgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "?"), code, msg))
+        self.code = code
+
+
+class _Config(ctypes.Structure):
+    _fields_ = [
+        ("system", ctypes.c_int), ("N", ctypes.c_int), ("imax", ctypes.c_int), ("jmax", ctypes.c_int),
+        ("xl", ctypes.c_double * 2), ("xr", ctypes.c_double * 2), ("bc", ctypes.c_int * 4),
+        ("bc_mode", ctypes.c_int), ("cfl", ctypes.c_double), ("gamma", ctypes.c_double),
+        ("gamma_s", ctypes.c_double), ("gamma_g", ctypes.c_double), ("pi_s", ctypes.c_double),
+        ("pi_g", ctypes.c_double), ("cx", ctypes.c_double), ("cy", ctypes.c_double), ("a", ctypes.c_double),
+        ("ad_flux_mode", ctypes.c_int), ("limiter", ctypes.c_int), ("precision", ctypes.c_int),
+    ]
+
+
+class _Info(ctypes.Structure):
+    _fields_ = [("cells", ctypes.c_long), ("dofs", ctypes.c_long), ("device_bytes", ctypes.c_long),
+                ("steps", ctypes.c_long), ("time", ctypes.c_double), ("dt", ctypes.c_double),
+                ("n_recompute", ctypes.c_int), ("n_limited", ctypes.c_int)]
+
+
+@dataclasses.dataclass
+class Config:
+    """What the reference reads from params.ini plus its compile-time N and CFL."""
+    system: int = SYS_EULER
+    N: int = 3
+    imax: int = 16
+    jmax: int = 16
+    xl: tuple = (0.0, 0.0)
+    xr: tuple = (1.0, 1.0)
+    bc: tuple = (1, 1, 1, 1)
+    bc_mode: int = 0
+    cfl: float = 0.9
+    gamma: float = 1.4
+    gamma_s: float = 1.4
+    gamma_g: float = 1.4
+    pi_s: float = 0.0
+    pi_g: float = 0.0
+    cx: float = 1.0
+    cy: float = 1.0
+    a: float = 1e-3
+    ad_flux_mode: int = 0
+    limiter: int = 1
+    precision: int = FP64
+
+    @property
+    def nvar(self):
+        return NVAR[self.system]
+
+    @property
+    def P(self):
+        return self.N + 1
+
+    @property
+    def S(self):
+        return 2 * self.N + 1
+
+    @property
+    def cells(self):
+        return self.imax * self.jmax
+
+    @property
+    def dofs(self):
+        """DOF-updates per step: nVar (N+1)^2 per cell."""
+        return self.nvar * self.P * self.P * self.cells
+
+    def to_c(self):
+        c = _Config()
+        c.system, c.N, c.imax, c.jmax = self.system, self.N, self.imax, self.jmax
+        c.xl[0], c.xl[1] = self.xl
+        c.xr[0], c.xr[1] = self.xr
+        for k in range(4):
+            c.bc[k] = self.bc[k]
+        c.bc_mode, c.cfl, c.gamma = self.bc_mode, self.cfl, self.gamma
+        c.gamma_s, c.gamma_g, c.pi_s, c.pi_g = self.gamma_s, self.gamma_g, self.pi_s, self.pi_g
+        c.cx, c.cy, c.a = self.cx, self.cy, self.a
+        c.ad_flux_mode, c.limiter, c.precision = self.ad_flux_mode, self.limiter, self.precision
+        return c
+
+
+_lib = None
+
+
+def library_path():
+    return _build.LIB_PATH
+
+
+def load(build_if_missing=False):
+    """Load libaderdg_gpu.so; raises when it is not built (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError("libaderdg_gpu.so is not built (%s); run aderdg.build.build()" % path)
+        _build.build()
+    L = ctypes.CDLL(path)
+    vp, dp, ip, i, d = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_double
+    cfgp = ctypes.POINTER(_Config)
+    sig = {
+        "aderdg_create": (i, [cfgp, ctypes.POINTER(vp)]), "aderdg_destroy": (i, [vp]),
+        "aderdg_upload": (i, [vp, dp]), "aderdg_init_limiter": (i, [vp, dp, ip]),
+        "aderdg_upload_limiter": (i, [vp, ip, dp]), "aderdg_download_limiter": (i, [vp, ip, dp]),
+        "aderdg_download": (i, [vp, dp, ip]),
+        "aderdg_calc_time_step": (i, [vp, d, d, dp]), "aderdg_set_time_step": (i, [vp, d, d]),
+        "aderdg_limiter_prepare": (i, [vp]), "aderdg_space_time_predictor": (i, [vp]),
+        "aderdg_volume_integral": (i, [vp]), "aderdg_riemann_problem": (i, [vp]),
+        "aderdg_surface_integral": (i, [vp]), "aderdg_element_update": (i, [vp, ip]),
+        "aderdg_limiter": (i, [vp]), "aderdg_step": (i, [vp, dp, d, dp, ip]),
+        "aderdg_run": (i, [vp, dp, d, i, i, ip]), "aderdg_array_size": (ctypes.c_long, [vp, i]),
+        "aderdg_get_array": (i, [vp, i, vp]), "aderdg_get_info": (i, [vp, ctypes.POINTER(_Info)]),
+        "aderdg_last_error": (ctypes.c_char_p, [vp]),
+        "aderdg_project_initial_condition": (i, [cfgp, i, dp, dp, dp]),
+        "aderdg_probe_peaks": (i, [dp, dp]), "aderdg_set_array": (i, [vp, i, vp]),
+        "aderdg_operator": (i, [i, i, dp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+EXPORTED = ("aderdg_create", "aderdg_destroy", "aderdg_upload", "aderdg_init_limiter", "aderdg_upload_limiter",
+            "aderdg_download_limiter", "aderdg_download", "aderdg_calc_time_step", "aderdg_set_time_step",
+            "aderdg_limiter_prepare", "aderdg_space_time_predictor", "aderdg_volume_integral",
+            "aderdg_riemann_problem", "aderdg_surface_integral", "aderdg_element_update", "aderdg_limiter",
+            "aderdg_step", "aderdg_run", "aderdg_array_size", "aderdg_get_array", "aderdg_get_info",
+            "aderdg_last_error", "aderdg_project_initial_condition", "aderdg_probe_peaks", "aderdg_set_array",
+            "aderdg_operator")
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+def project_initial_condition(cfg, ic, params=()):
+    """Initial field at the Gauss-Legendre nodes (uh) and subcell barycentres (lh_ic)."""
+    L = load()
+    p = np.zeros(32, dtype=np.float64)
+    p[: len(params)] = params
+    uh = np.empty(cfg.dofs, dtype=np.float64)
+    lh = np.empty(cfg.nvar * cfg.S * cfg.S * cfg.cells, dtype=np.float64)
+    c = cfg.to_c()
+    r = L.aderdg_project_initial_condition(ctypes.byref(c), ic, _dp(p), _dp(uh), _dp(lh))
+    if r:
+        raise AderdgError(r, L.aderdg_last_error(None).decode())
+    return uh, lh
+
+
+(OP_XI, OP_W, OP_KXI, OP_DUDX, OP_IK1, OP_F0, OP_FL, OP_FR, OP_UH2LIM, OP_LIM2UH, OP_UH2LOB,
+ OP_XILIMBARY) = range(12)
+
+
+def operator(N, which):
+    """Host-built 1D operator of degree N (column-major, flattened)."""
+    L = load()
+    out = np.zeros(256, dtype=np.float64)
+    n = L.aderdg_operator(N, which, _dp(out))
+    if n < 0:
+        raise AderdgError(n, "bad operator request")
+    return out[:n].copy()
+
+
+def probe_peaks():
+    """(FP64, FP32) FMA throughput of the current device in GFLOP/s."""
+    L = load()
+    a, b = ctypes.c_double(0), ctypes.c_double(0)
+    r = L.aderdg_probe_peaks(ctypes.byref(a), ctypes.byref(b))
+    if r:
+        raise AderdgError(r, "probe failed")
+    return a.value, b.value
+
+
+class Solver:
+    """One simulation on the GPU: the reference's module state plus its phases."""
+
+    def __init__(self, cfg):
+        self.cfg = cfg
+        self.L = load()
+        self._c = cfg.to_c()
+        h = ctypes.c_void_p()
+        r = self.L.aderdg_create(ctypes.byref(self._c), ctypes.byref(h))
+        if r:
+            raise AderdgError(r, self.L.aderdg_last_error(None).decode())
+        self.h = h
+
+    def _ck(self, r):
+        if r:
+            raise AderdgError(r, self.L.aderdg_last_error(self.h).decode())
+        return r
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.aderdg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # state transfer
+    def upload(self, uh):
+        uh = np.ascontiguousarray(uh, dtype=np.float64).ravel()
+        assert uh.size == self.cfg.dofs
+        self._ck(self.L.aderdg_upload(self.h, _dp(uh)))
+
+    def init_limiter(self, lh_ic):
+        n = ctypes.c_int(0)
+        lh = None if lh_ic is None else np.ascontiguousarray(lh_ic, dtype=np.float64).ravel()
+        self._ck(self.L.aderdg_init_limiter(self.h, None if lh is None else _dp(lh), ctypes.byref(n)))
+        return n.value
+
+    def upload_limiter(self, status, lh):
+        st = np.ascontiguousarray(status, dtype=np.int32).ravel()
+        lh = np.ascontiguousarray(lh, dtype=np.float64).ravel()
+        self._ck(self.L.aderdg_upload_limiter(self.h, _ip(st), _dp(lh)))
+
+    def download(self):
+        uh = np.empty(self.cfg.dofs, dtype=np.float64)
+        st = np.empty(self.cfg.cells, dtype=np.int32)
+        self._ck(self.L.aderdg_download(self.h, _dp(uh), _ip(st)))
+        return uh, st
+
+    def download_into(self, uh):
+        self._ck(self.L.aderdg_download(self.h, _dp(uh), None))
+
+    # phases of main.f90's loop body
+    def calc_time_step(self, time, tend):
+        dt = ctypes.c_double(0)
+        self._ck(self.L.aderdg_calc_time_step(self.h, time, tend, ctypes.byref(dt)))
+        return dt.value
+
+    def set_time_step(self, time, dt):
+        self._ck(self.L.aderdg_set_time_step(self.h, time, dt))
+
+    def limiter_prepare(self):
+        self._ck(self.L.aderdg_limiter_prepare(self.h))
+
+    def space_time_predictor(self):
+        self._ck(self.L.aderdg_space_time_predictor(self.h))
+
+    def volume_integral(self):
+        self._ck(self.L.aderdg_volume_integral(self.h))
+
+    def riemann_problem(self):
+        self._ck(self.L.aderdg_riemann_problem(self.h))
+
+    def surface_integral(self):
+        self._ck(self.L.aderdg_surface_integral(self.h))
+
+    def element_update(self):
+        n = ctypes.c_int(0)
+        self._ck(self.L.aderdg_element_update(self.h, ctypes.byref(n)))
+        return n.value
+
+    def limiter(self):
+        self._ck(self.L.aderdg_limiter(self.h))
+
+    # fused
+    def step(self, time, tend):
+        t = ctypes.c_double(time)
+        dt = ctypes.c_double(0)
+        n = ctypes.c_int(0)
+        self._ck(self.L.aderdg_step(self.h, ctypes.byref(t), tend, ctypes.byref(dt), ctypes.byref(n)))
+        return t.value, dt.value, n.value
+
+    def run(self, time, tend, max_steps, sync_every=0):
+        t = ctypes.c_double(time)
+        n = ctypes.c_int(0)
+        self._ck(self.L.aderdg_run(self.h, ctypes.byref(t), tend, max_steps, sync_every, ctypes.byref(n)))
+        return t.value, n.value
+
+    # introspection
+    def get(self, which):
+        n = self.L.aderdg_array_size(self.h, which)
+        if n < 0:
+            raise AderdgError(int(n), "array not available")
+        out = np.empty(n, dtype=np.int32 if which in INT_ARRAYS else np.float64)
+        self._ck(self.L.aderdg_get_array(self.h, which, out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    def set(self, which, arr):
+        arr = np.ascontiguousarray(arr, dtype=np.int32 if which in INT_ARRAYS else np.float64).ravel()
+        n = self.L.aderdg_array_size(self.h, which)
+        assert arr.size == n, (arr.size, n)
+        self._ck(self.L.aderdg_set_array(self.h, which, arr.ctypes.data_as(ctypes.c_void_p)))
+
+    def info(self):
+        i = _Info()
+        self._ck(self.L.aderdg_get_info(self.h, ctypes.byref(i)))
+        return {k: getattr(i, k) for k, _ in _Info._fields_}

@@ -1,0 +1,363 @@
+// cells.cuh -- K3: surface integral + element update + DMP / positivity
+// detection + CFL partials, one thread per spatial node, CPB cells per CTA.
+//
+// Reference: surface_integral.f90:8-39, element_update.f90:8-30, the DMP of
+// Euler/limiter.f90:179-245 (called from Euler/main.f90:74-88), the per-cell
+// part of get_min_max (Euler/limiter.f90:115-143) for the next step, and the
+// node loop of calc_time_step.f90.  Compiled with --fmad=false: all values
+// follow the reference's FP64 operation order.
+//
+// Modes (BatchArgs::mode):
+//   kCellFused   surface + update + [DMP, next min/max] + CFL partials
+//   kCellSurface surface integral only (phase API)
+//   kCellUpdate  update + [DMP, next min/max] + CFL partials (phase API)
+//   kCellPrime   min/max of the current state for the DMP neighbourhood
+//                (get_min_max step 1) + CFL denominators; no update
+//   kCellInitDmp initial limiter: DMP with argmax 0.1 against the cell's own
+//                nodal min/max; failing cells take the initial subcell data
+//   kCellCfl     CFL denominators of the current state only
+#pragma once
+
+#include "common.cuh"
+#include "physics.cuh"
+
+namespace aderdg {
+
+#define kInf __longlong_as_double(0x7ff0000000000000LL)
+
+// Subcell / Gauss-Lobatto projections of one cell (get_subcell_data and
+// get_lobatto_data, Euler/limiter.f90:12-68), sum-factorised y then x with
+// the reference's summation order.  A "team" of nr threads with rank r works
+// on one cell; the caller synchronises between the two passes.
+template <int N, int V>
+struct Proj {
+  static constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1;
+  // y pass: LY[v][s][i] = sum_k U[v][i + P k] uh2lim(s,k); LB[v][s][i] likewise with uh2lob
+  __device__ static void ypass(const double* U, double* LY, double* LB, const DevOps<N, double>& op, int r, int nr) {
+    for (int idx = r; idx < P * S; idx += nr) {
+      const int ii = idx % P, s = idx / P;
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        double acc = 0.0;
+#pragma unroll
+        for (int k = 0; k < P; ++k) acc = acc + U[v * P2 + ii + P * k] * op.uh2lim[s + S * k];
+        LY[(v * S + s) * P + ii] = acc;
+      }
+    }
+    for (int idx = r; idx < P * P; idx += nr) {
+      const int ii = idx % P, s = idx / P;
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        double acc = 0.0;
+#pragma unroll
+        for (int k = 0; k < P; ++k) acc = acc + U[v * P2 + ii + P * k] * op.uh2lob[s + P * k];
+        LB[(v * P + s) * P + ii] = acc;
+      }
+    }
+  }
+  // subcell value (s1, s2) from the y pass
+  __device__ static void subcell(const double* LY, const DevOps<N, double>& op, int s1, int s2, double* out) {
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      double acc = 0.0;
+#pragma unroll
+      for (int k = 0; k < P; ++k) acc = acc + LY[(v * S + s2) * P + k] * op.uh2lim[s1 + S * k];
+      out[v] = acc;
+    }
+  }
+  __device__ static void lobatto(const double* LB, const DevOps<N, double>& op, int s1, int s2, double* out) {
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      double acc = 0.0;
+#pragma unroll
+      for (int k = 0; k < P; ++k) acc = acc + LB[(v * P + s2) * P + k] * op.uh2lob[s1 + P * k];
+      out[v] = acc;
+    }
+  }
+  // x pass fused with min/max and the positivity test of every subcell
+  template <class Sys>
+  __device__ static void xpass_minmax(const double* U, const double* LY, const double* LB, const DevOps<N, double>& op,
+                                      const Phys& ph, int r, int nr, double* mn, double* mx, bool& posfail) {
+    double val[V];
+    for (int idx = r; idx < S * S; idx += nr) {
+      subcell(LY, op, idx % S, idx / S, val);
+#pragma unroll
+      for (int v = 0; v < V; ++v) { mn[v] = fmin(mn[v], val[v]); mx[v] = fmax(mx[v], val[v]); }
+      if constexpr (Sys::ID != kSysAD) {
+        if (!Sys::positive(ph, val)) posfail = true;
+      }
+    }
+    for (int idx = r; idx < P * P; idx += nr) {
+      lobatto(LB, op, idx % P, idx / P, val);
+#pragma unroll
+      for (int v = 0; v < V; ++v) { mn[v] = fmin(mn[v], val[v]); mx[v] = fmax(mx[v], val[v]); }
+    }
+    for (int idx = r; idx < P2; idx += nr) {
+#pragma unroll
+      for (int v = 0; v < V; ++v) { mn[v] = fmin(mn[v], U[v * P2 + idx]); mx[v] = fmax(mx[v], U[v * P2 + idx]); }
+    }
+  }
+};
+
+// Voronoi neighbour index along one axis (Euler/initialize.f90:219-258):
+// periodic sides wrap, all others clamp.
+__device__ __forceinline__ int nb_index(int x, int d, int n, int bc_lo, int bc_hi) {
+  int y = x + d;
+  if (y < 0) y = (bc_lo == 3) ? n - 1 : 0;
+  if (y > n - 1) y = (bc_hi == 3) ? 0 : n - 1;
+  return y;
+}
+
+// CFL denominator at one node (calc_time_step.f90: Euler/BN :31-45, AD :37-50)
+template <class Sys, int N>
+__device__ __forceinline__ double cfl_denom(const InstDesc& in, const double* Q) {
+  if constexpr (Sys::ID == kSysAD) {
+    const double factor = (double)(2 * N + 1);
+    double denom = 0.0;
+    const double smax_v = fabs(in.ph.a);
+    denom = denom + (ADSys::max_eig_c(in.ph, 0) + 2.0 * smax_v * factor / in.dx) / in.dx;
+    denom = denom + (ADSys::max_eig_c(in.ph, 1) + 2.0 * smax_v * factor / in.dy) / in.dy;
+    return denom;
+  } else {
+    double denom = 0.0;
+    denom = denom + Sys::max_eig(in.ph, Q, 0) / in.dx;
+    denom = denom + Sys::max_eig(in.ph, Q, 1) / in.dy;
+    return denom;
+  }
+}
+
+template <class Sys, int N>
+struct CellCfg {
+  static constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1, V = Sys::V;
+  static constexpr int CPB = (256 / P2) < 1 ? 1 : (256 / P2);
+  static constexpr int THREADS = ((CPB * P2 + 31) / 32) * 32;
+  // per cell: U [V][P2], LY [V][S][P], LB [V][P][P], red [2][V][P2]
+  static constexpr int CELL_DBL = V * P2 + V * S * P + V * P * P + 2 * V * P2;
+  static constexpr int SMEM_BYTES = CPB * CELL_DBL * 8 + CPB * 8 /*cell max*/ + CPB * 4 /*flags*/ + 16;
+};
+
+template <class Sys, int N>
+__global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a, DevOps<N, double> op) {
+  using C = CellCfg<Sys, N>;
+  constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1, V = Sys::V, CPB = C::CPB;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* sm = reinterpret_cast<double*>(smem_raw);
+  unsigned long long* cmax = reinterpret_cast<unsigned long long*>(sm + CPB * C::CELL_DBL);
+  int* cflag = reinterpret_cast<int*>(cmax + CPB);
+
+  const int mode = a.mode;
+  const int t = threadIdx.x;
+  const int lc = t / P2;
+  const int node = t - lc * P2;
+  const int i = node % P, j = node / P;
+  const long long cell = (long long)blockIdx.x * CPB + lc;
+  const bool in_cta = lc < CPB;
+  const bool valid = in_cta && cell < a.ncells;
+  const int kc = valid ? find_inst_cell(a.inst, a.ninst, cell) : 0;
+  const InstDesc& in = a.inst[kc];
+  const InstState& st = a.st[kc];
+  const bool act = valid && (st.active || mode == kCellPrime || mode == kCellInitDmp || mode == kCellCfl);
+  const int par = parity(st);
+  const long long lcell = cell - in.cell_base;
+  const int ci = valid ? (int)(lcell % in.imax) : 0, cj = valid ? (int)(lcell / in.imax) : 0;
+  const bool limiter = Sys::ID != kSysAD && a.mm[0] != nullptr;
+
+  double* U = sm + (size_t)(in_cta ? lc : 0) * C::CELL_DBL;
+  double* LY = U + V * P2;
+  double* LB = LY + V * S * P;
+  double* RED = LB + V * P * P;
+
+  if (in_cta && node == 0) {
+    cmax[lc] = 0ull;
+    cflag[lc] = 0;
+  }
+  __syncthreads();
+
+  // ---------------------------------------------------------------- update
+  double u[V];
+  const size_t off = ((size_t)(valid ? cell : 0) * P2 + node) * V;
+  if (act) {
+    if (mode == kCellFused || mode == kCellSurface || mode == kCellUpdate) {
+      double d[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) d[v] = a.duh[off + v];
+      if (mode != kCellUpdate) {
+        // surface_integral.f90:20-35: x faces then y faces
+        const long long fxl = in.fx_base + ci + (long long)(in.imax + 1) * cj;
+        const long long fyb = in.fy_base + ci + (long long)in.imax * cj;
+        const long long fyt = fyb + in.imax;
+        const double* XL = a.fu;
+        const double* XR = (Sys::ID == kSysBN) ? a.fp : a.fu;
+        const double* YB = a.gu;
+        const double* YT = (Sys::ID == kSysBN) ? a.gp : a.gu;
+        const double cx = op.wd[j] / in.dx, cy = op.wd[i] / in.dy;
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          const double fl = XL[((size_t)fxl * P + j) * V + v], fr = XR[((size_t)(fxl + 1) * P + j) * V + v];
+          d[v] = d[v] - cx * (fr * op.FRd[i] - fl * op.FLd[i]);
+        }
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          const double gb = YB[((size_t)fyb * P + i) * V + v], gt = YT[((size_t)fyt * P + i) * V + v];
+          d[v] = d[v] - cy * (gt * op.FRd[j] - gb * op.FLd[j]);
+        }
+      }
+      if (mode == kCellSurface) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) a.duh[off + v] = d[v];
+      } else {
+        // element_update.f90:18-26
+        const double dt = st.dt;
+        const double* uo = a.uh[par] + off;
+        double* un = a.uh[par ^ 1] + off;
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          d[v] = d[v] / (op.wd[i] * op.wd[j]);
+          u[v] = uo[v] + dt * d[v];
+          un[v] = u[v];
+        }
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < V; ++v) u[v] = a.uh[par][off + v];
+    }
+  }
+  if (mode == kCellSurface) return;  // uniform per launch: no barrier follows
+
+  // ------------------------------------------------------------- CFL part
+  const bool want_cfl = mode != kCellInitDmp;
+  if (act && want_cfl) atomicMax(&cmax[lc], (unsigned long long)__double_as_longlong(cfl_denom<Sys, N>(in, u)));
+
+  // ------------------------------------------------------------- DMP part
+  const bool want_dmp = limiter && mode != kCellCfl;
+  if (want_dmp) {
+    // Cells whose limiter is active keep their min/max from the subcell data
+    // (get_min_max, Euler/limiter.f90:134-139) in the priming pass.
+    const bool from_lh = act && mode == kCellPrime && a.status[par][valid ? cell : 0] != 0;
+    if (act) {
+#pragma unroll
+      for (int v = 0; v < V; ++v) U[v * P2 + node] = u[v];
+    }
+    __syncthreads();
+    if (act && !from_lh) Proj<N, V>::ypass(U, LY, LB, op, node, P2);
+    __syncthreads();
+    double mn[V], mx[V];
+    bool posfail = false;
+#pragma unroll
+    for (int v = 0; v < V; ++v) { mn[v] = kInf; mx[v] = -kInf; }
+    if (act) {
+      if (from_lh) {
+        const double* L = a.lh[par] + (size_t)cell * S * S * V;
+        for (int idx = node; idx < S * S; idx += P2)
+#pragma unroll
+          for (int v = 0; v < V; ++v) { mn[v] = fmin(mn[v], L[idx * V + v]); mx[v] = fmax(mx[v], L[idx * V + v]); }
+      } else {
+        Proj<N, V>::template xpass_minmax<Sys>(U, LY, LB, op, in.ph, node, P2, mn, mx, posfail);
+      }
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        RED[v * P2 + node] = mn[v];
+        RED[(V + v) * P2 + node] = mx[v];
+      }
+      if (posfail) atomicOr(&cflag[lc], 1);
+    }
+    __syncthreads();
+    if (act && node < V) {
+      const int v = node;
+      double cmn = RED[v * P2], cmx = RED[(V + v) * P2];
+      for (int k = 1; k < P2; ++k) { cmn = fmin(cmn, RED[v * P2 + k]); cmx = fmax(cmx, RED[(V + v) * P2 + k]); }
+      if (mode == kCellPrime) {
+        a.mm[par][(size_t)cell * 2 * V + v] = cmn;
+        a.mm[par][(size_t)cell * 2 * V + V + v] = cmx;
+      } else {
+        double lmin, lmax, argmax;
+        if (mode == kCellInitDmp) {
+          // Euler/initialize.f90:291-294: the cell's own nodal min/max
+          lmin = U[v * P2];
+          lmax = U[v * P2];
+          for (int k = 1; k < P2; ++k) { lmin = fmin(lmin, U[v * P2 + k]); lmax = fmax(lmax, U[v * P2 + k]); }
+          argmax = 1.0e-1;
+        } else {
+          // get_min_max step 2 (Euler/limiter.f90:147-167): 3x3 Voronoi neighbourhood
+          const double* mmi = a.mm[par];
+          const long long base = in.cell_base;
+          lmin = mmi[(size_t)cell * 2 * V + v];
+          lmax = mmi[(size_t)cell * 2 * V + V + v];
+          for (int jj = -1; jj <= 1; ++jj)
+            for (int ii = -1; ii <= 1; ++ii) {
+              const int in_ = nb_index(ci, ii, in.imax, in.bc[0], in.bc[1]);
+              const int jn_ = nb_index(cj, jj, in.jmax, in.bc[2], in.bc[3]);
+              const long long nc = base + in_ + (long long)in.imax * jn_;
+              lmin = fmin(lmin, mmi[(size_t)nc * 2 * V + v]);
+              lmax = fmax(lmax, mmi[(size_t)nc * 2 * V + V + v]);
+            }
+          argmax = 0.0;
+          if (a.lminmax) {
+            a.lminmax[(size_t)cell * 2 * V + v] = lmin;
+            a.lminmax[(size_t)cell * 2 * V + V + v] = lmax;
+          }
+          // candidate min/max for the next step (status 0)
+          a.mm[par ^ 1][(size_t)cell * 2 * V + v] = cmn;
+          a.mm[par ^ 1][(size_t)cell * 2 * V + V + v] = cmx;
+        }
+        // Euler/limiter.f90:210-220
+        const double ldiff = fmax(fmax(1.0e-4, 1.0e-3 * (lmax - lmin)), argmax);
+        if (cmn < lmin - ldiff || cmx > lmax + ldiff) atomicOr(&cflag[lc], 2);
+      }
+    }
+    __syncthreads();
+    if (act && mode != kCellPrime) {
+      const bool bad = cflag[lc] != 0;
+      if (mode == kCellInitDmp) {
+        if (bad) {
+          // Euler/initialize.f90:296-317: status 1, Lh = NewLh = initial subcell data
+          if (node == 0) {
+            a.status[0][cell] = 1;
+            a.status[1][cell] = 1;
+            atomicAdd(&a.st[kc].n_recompute, 1);
+          }
+          if (a.lh_ic) {
+            const size_t o = (size_t)cell * S * S * V;
+            for (int idx = node; idx < S * S * V; idx += P2) {
+              a.lh[0][o + idx] = a.lh_ic[o + idx];
+              a.lh[1][o + idx] = a.lh_ic[o + idx];
+            }
+          }
+        }
+      } else if (node == 0) {
+        a.troubled[cell] = bad ? 1 : 0;
+        if (bad) atomicAdd(&a.st[kc].n_recompute, 1);
+      }
+    }
+  } else {
+    __syncthreads();
+  }
+
+  // ------------------------------------------------ CFL per cell / instance
+  if (!want_cfl) return;
+  if (limiter && (mode == kCellFused || mode == kCellUpdate)) {
+    if (act && node == 0) a.denom[cell] = __longlong_as_double((long long)cmax[lc]);
+    return;
+  }
+  if (t == 0) {
+    // fold the CTA's cells per instance, one atomic per instance
+    int cur = -1;
+    unsigned long long m = 0ull;
+    for (int c = 0; c < CPB; ++c) {
+      const long long cc = (long long)blockIdx.x * CPB + c;
+      if (cc >= a.ncells) break;
+      const int kk = find_inst_cell(a.inst, a.ninst, cc);
+      const bool ok = a.st[kk].active || mode == kCellPrime || mode == kCellCfl;
+      if (!ok) continue;
+      if (kk != cur) {
+        if (cur >= 0) atomicMax(&a.st[cur].denom_next, m);
+        cur = kk;
+        m = 0ull;
+      }
+      m = m > cmax[c] ? m : cmax[c];
+    }
+    if (cur >= 0) atomicMax(&a.st[cur].denom_next, m);
+  }
+}
+
+}  // namespace aderdg

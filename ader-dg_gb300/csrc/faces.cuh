@@ -1,0 +1,208 @@
+// faces.cuh -- K2: numerical fluxes once per face quadrature point, with the
+// boundary conditions inlined.
+//
+// Reference: Euler/riemann_problem.f90:10-116 (Rusanov, double Mach
+// reflection boundaries), Baer-Nunziato/riemann_problem.f90:9-80
+// (path-conservative Rusanov fluctuations Dm/Dp), and
+// Advection-Diffusion/riemann_problem.f90:8-113 (viscous LLF).  One thread per
+// (face, point); the x faces of all instances come first, then the y faces.
+// Compiled with --fmad=false: every value agrees bit for bit with the
+// reference expression evaluated in FP64 from the same face states.
+#pragma once
+
+#include "common.cuh"
+#include "physics.cuh"
+
+namespace aderdg {
+
+__device__ __forceinline__ int find_inst_fx(const InstDesc* inst, int n, long long f) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (inst[mid].fx_base <= f) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+__device__ __forceinline__ int find_inst_fy(const InstDesc* inst, int n, long long f) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (inst[mid].fy_base <= f) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <int V, class R>
+__device__ __forceinline__ void load_face_state(const R* qb, const R* fb, long long cell, int P, int l, int f, double* Q, double* F) {
+  const size_t o = (((size_t)cell * P + l) * 4 + f) * V;
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    Q[v] = (double)qb[o + v];
+    if (F) F[v] = (double)fb[o + v];
+  }
+}
+
+// Euler double Mach reflection boundary state: Q = prim2cons(Vp), F = flux(Q)
+// along axis d (matmul(Fbc, nv) of Euler/riemann_problem.f90:43-46).
+__device__ __forceinline__ void dmr_state(const Phys& ph, const double* Vp, int d, double* Q, double* F) {
+  double Fb[8];
+  EulerSys::prim2cons(ph, Vp, Q);
+  EulerSys::flux(ph, Q, Fb);
+  for (int v = 0; v < 4; ++v) F[v] = Fb[d * 4 + v];
+}
+
+template <class Sys, int N, class R>
+__global__ void __launch_bounds__(256) k_faces(BatchArgs a, FaceConst fc) {
+  constexpr int P = N + 1, V = Sys::V;
+  const long long nx = a.nfx * P, ny = a.nfy * P;
+  const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= nx + ny) return;
+  const R* qb = reinterpret_cast<const R*>(a.qbnd);
+  const R* fb = reinterpret_cast<const R*>(a.fbnd);
+  const bool xdir = gid < nx;
+  const long long g = xdir ? gid : gid - nx;
+  const long long face = g / P;
+  const int l = (int)(g - face * P);
+  const int k = xdir ? find_inst_fx(a.inst, a.ninst, face) : find_inst_fy(a.inst, a.ninst, face);
+  const InstDesc& in = a.inst[k];
+  if (!a.st[k].active) return;
+  const Phys ph = in.ph;
+  const int I = in.imax, J = in.jmax;
+  const long long lf = face - (xdir ? in.fx_base : in.fy_base);
+  int i, j;
+  if (xdir) { i = (int)(lf % (I + 1)); j = (int)(lf / (I + 1)); }
+  else { i = (int)(lf % I); j = (int)(lf / I); }
+  auto cid = [&](int ci, int cj) { return in.cell_base + (long long)ci + (long long)I * cj; };
+  const int d = xdir ? 0 : 1;
+  const int nfaces_side = xdir ? I : J;  // index of the last face along d is nfaces_side
+  const int pos = xdir ? i : j;
+  const int bcl = in.bc[xdir ? 0 : 2], bcr = in.bc[xdir ? 1 : 3];
+  const int fl = xdir ? 0 : 2, fr = xdir ? 1 : 3;  // left/bottom and right/top face ids
+  const size_t out = ((size_t)face * P + l) * V;
+
+  if constexpr (Sys::ID == kSysAD) {
+    // Advection-Diffusion/riemann_problem.f90 with PDEViscLLFRiemannSolver (pde.f90:121-152)
+    double QL[1], QR[1], gL[2], gR[2];
+    auto get = [&](long long c, int f, double* Q, double* gq) {
+      const size_t o = (((size_t)c * P + l) * 4 + f);
+      Q[0] = (double)qb[o];
+      gq[0] = (double)fb[o * 2 + 0];
+      gq[1] = (double)fb[o * 2 + 1];
+    };
+    const long long cL = xdir ? cid(i - 1, j) : cid(i, j - 1);
+    const long long cR = cid(i, j);
+    if (pos == 0) {
+      if (bcl == 1) {
+        get(cR, fl, QL, gL);
+        get(cR, fl, QR, gR);
+      } else if (bcl == 2) {
+        if (xdir) {
+          // QR from the right face of cell IMAX, QL = -QR + 2 sin(pi y),
+          // y = (j-1 + xi_l) dy (Advection-Diffusion/riemann_problem.f90:37-40)
+          get(cid(I - 1, j), 1, QR, gR);
+          const double y = ((double)j + fc.xi[l]) * in.dy;
+          QL[0] = -QR[0] + 2.0 * sin(fc.pi * y);
+        } else {
+          get(cR, fl, QR, gR);
+          QL[0] = -QR[0];
+        }
+        gL[0] = gR[0];
+        gL[1] = gR[1];
+      } else {
+        get(xdir ? cid(I - 1, j) : cid(i, J - 1), fr, QL, gL);
+        get(cR, fl, QR, gR);
+      }
+    } else if (pos == nfaces_side) {
+      const long long cLast = xdir ? cid(I - 1, j) : cid(i, J - 1);
+      if (bcr == 1) {
+        get(cLast, fr, QL, gL);
+        get(cLast, fr, QR, gR);
+      } else if (bcr == 2) {
+        get(cLast, fr, QL, gL);
+        QR[0] = -QL[0];
+        gR[0] = gL[0];
+        gR[1] = gL[1];
+      } else {
+        get(cLast, fr, QL, gL);
+        get(xdir ? cid(0, j) : cid(i, 0), fl, QR, gR);
+      }
+    } else {
+      get(cL, fr, QL, gL);
+      get(cR, fl, QR, gR);
+    }
+    const double nv0 = xdir ? 1.0 : 0.0, nv1 = xdir ? 0.0 : 1.0;
+    const double LL = ph.cx * nv0 + ph.cy * nv1, LR = LL;
+    const double factor = (double)(2 * N + 1);
+    const double eta = factor / (in.dx * sqrt(0.5 * fc.pi));
+    const double smax_c = fmax(fabs(LL), fabs(LR));
+    const double smax_v = fmax(ph.a, ph.a);
+    const double smax = smax_c + 2.0 * eta * smax_v;
+    const double FL0 = ph.cx * QL[0] + -ph.a * gL[0], FL1 = ph.cy * QL[0] + -ph.a * gL[1];
+    const double FR0 = ph.cx * QR[0] + -ph.a * gR[0], FR1 = ph.cy * QR[0] + -ph.a * gR[1];
+    double* dst = xdir ? a.fu : a.gu;
+    dst[out] = 0.5 * ((FL0 + FR0) * nv0 + (FL1 + FR1) * nv1) - 0.5 * smax * (QR[0] - QL[0]);
+  } else {
+    double QL[V], QR[V], FL[V], FR[V];
+    const bool is_dmr = (Sys::ID == kSysEuler) && in.bc_mode == 1;
+    const long long cL = xdir ? cid(i - 1, j) : cid(i, j - 1);
+    const long long cR = cid(i, j);
+    if (pos == 0) {
+      if (is_dmr) {
+        if (xdir) {  // inflow, Euler/riemann_problem.f90:41-48
+          dmr_state(ph, fc.Va, 0, QL, FL);
+          load_face_state<V, R>(qb, fb, cR, P, l, fl, QR, FR);
+        } else {     // transmissive / reflective wall, :76-86
+          load_face_state<V, R>(qb, fb, cR, P, l, fl, QL, FL);
+          if (!((double)(i + 1) * in.dx <= 1.0 / 6.0)) {
+            QL[2] = -QL[2];
+            FL[0] = -FL[0];
+            FL[1] = -FL[1];
+            FL[3] = -FL[3];
+          }
+          load_face_state<V, R>(qb, fb, cR, P, l, fl, QR, FR);
+        }
+      } else if (bcl == 3) {
+        load_face_state<V, R>(qb, fb, xdir ? cid(I - 1, j) : cid(i, J - 1), P, l, fr, QL, FL);
+        load_face_state<V, R>(qb, fb, cR, P, l, fl, QR, FR);
+      } else {
+        load_face_state<V, R>(qb, fb, cR, P, l, fl, QL, FL);
+        load_face_state<V, R>(qb, fb, cR, P, l, fl, QR, FR);
+      }
+    } else if (pos == nfaces_side) {
+      const long long cLast = xdir ? cid(I - 1, j) : cid(i, J - 1);
+      load_face_state<V, R>(qb, fb, cLast, P, l, fr, QL, FL);
+      if (is_dmr && !xdir) {  // time-dependent top boundary, :88-100
+        const double x_sw = fc.xsw0 + fc.xsw1 * a.st[k].time;
+        dmr_state(ph, ((double)(i + 1) * in.dx <= x_sw) ? fc.Va : fc.Vb, 1, QR, FR);
+      } else if (!is_dmr && bcr == 3) {
+        load_face_state<V, R>(qb, fb, xdir ? cid(0, j) : cid(i, 0), P, l, fl, QR, FR);
+      } else {
+        load_face_state<V, R>(qb, fb, cLast, P, l, fr, QR, FR);
+      }
+    } else {
+      load_face_state<V, R>(qb, fb, cL, P, l, fr, QL, FL);
+      load_face_state<V, R>(qb, fb, cR, P, l, fl, QR, FR);
+    }
+    // Rusanov: smax from both sides' eigenvalues (Euler/pde.f90:97-114)
+    const double smax = fmax(Sys::max_eig(ph, QL, d), Sys::max_eig(ph, QR, d));
+    if constexpr (Sys::ID == kSysBN) {
+      // path-conservative fluctuations, Baer-Nunziato/pde.f90:326-353
+      double D[9];
+      BNSys::roe_times_jump(ph, QL, QR, d, D);
+      double* dm = xdir ? a.fu : a.gu;
+      double* dp = xdir ? a.fp : a.gp;
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        const double base = 0.5 * (FL[v] + FR[v]) - 0.5 * smax * (QR[v] - QL[v]);
+        dm[out + v] = base - 0.5 * D[v];
+        dp[out + v] = base + 0.5 * D[v];
+      }
+    } else {
+      double* dst = xdir ? a.fu : a.gu;
+#pragma unroll
+      for (int v = 0; v < V; ++v) dst[out + v] = 0.5 * (FL[v] + FR[v]) - 0.5 * smax * (QR[v] - QL[v]);
+    }
+  }
+}
+
+}  // namespace aderdg

@@ -1,0 +1,392 @@
+// predictor.cuh -- K1: cell-local space-time predictor (Picard iteration),
+// fused with the volume integral and the face extrapolation.
+//
+// Reference: Euler/space_time_predictor.f90:8-123,
+// Baer-Nunziato/space_time_predictor.f90:8-143,
+// Advection-Diffusion/space_time_predictor.f90:10-155, and
+// volume_integral.f90 of each solver.
+//
+// Mapping: one thread per spatial node (i,j) of a cell, CPB cells per CTA.
+// Each thread keeps its node's time column q(l, v), l = 0..N, in registers;
+// the flux-derivative contractions in x and y are the only operations that
+// cross nodes and go through shared memory once per Picard iteration.
+//
+// Algebra (same as the reference, regrouped for fused multiply-adds):
+//   rhs(l)  = w_i w_j F0(l) u - w_l w_j dt/dx (Fx Kxi)_i - w_l w_i dt/dy (Fy Kxi)_j  [+ w_i w_j w_l dt S(l)]
+//   q(l')   = 1/(w_i w_j) sum_l iK1(l',l) rhs(l)
+//           = g(l') u - sum_l T(l',l) b_l,   b_l = sum_k Dx(i,k) Fx(k,j,l) + sum_k Dy(j,k) Fy(i,k,l) [- dt S(l)]
+// with T(l',l) = iK1(l',l) w_l, g = iK1 F0, Dx(i,k) = Kxi(k,i) dt/(dx w_i).
+// The first iteration starts from q(l) = u for every l, so its fluxes and
+// contractions are evaluated once instead of N+1 times.  The last iteration
+// only needs the time average qhi = sum_l' w_l' q(l'), contracted directly.
+// Fhi (and Shi) are the time averages of the last iteration's fluxes, as in
+// the reference, where lFh is not recomputed after the final iK1 update.
+#pragma once
+
+#include "common.cuh"
+#include "physics.cuh"
+
+namespace aderdg {
+
+template <class Sys, int N, class R>
+struct PredCfg {
+  static constexpr int P = N + 1, P2 = P * P, V = Sys::V;
+  // shared-memory elements per cell: flux buffer [P][2][V][P2] (+ BN volume
+  // fraction [P][P2]; AD: state [P][P2] + flux [P][2][P2])
+  static constexpr int CELL_ELEMS = (Sys::ID == kSysAD) ? 3 * P * P2 : (2 * V * P + (Sys::ID == kSysBN ? P : 0)) * P2;
+  static constexpr int MAX_THREADS = 256;
+  static constexpr int SMEM_BUDGET = 100 * 1024;
+  static constexpr int CPB_T = MAX_THREADS / P2;
+  static constexpr int CPB_S = SMEM_BUDGET / (CELL_ELEMS * (int)sizeof(R));
+  static constexpr int CPB = (CPB_T < CPB_S ? CPB_T : CPB_S) < 1 ? 1 : (CPB_T < CPB_S ? CPB_T : CPB_S);
+  static constexpr int THREADS = ((CPB * P2 + 31) / 32) * 32;
+  static constexpr int SMEM_BYTES = CPB * CELL_ELEMS * (int)sizeof(R);
+};
+
+// Flux-derivative contraction of time level l into b[v].
+template <int V, int P, class R>
+__device__ __forceinline__ void contract(const R* __restrict__ cs, int l, int i, int j, const R* Dx, const R* Dy, R* b) {
+  constexpr int P2 = P * P;
+  const R* fx = cs + (size_t)(l * 2 + 0) * V * P2;
+  const R* fy = cs + (size_t)(l * 2 + 1) * V * P2;
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    R s = R(0);
+#pragma unroll
+    for (int k = 0; k < P; ++k) s = fma(Dx[k], fx[v * P2 + k + P * j], s);
+#pragma unroll
+    for (int k = 0; k < P; ++k) s = fma(Dy[k], fy[v * P2 + i + P * k], s);
+    b[v] = s;
+  }
+}
+
+template <class Sys, int N, class R, bool kPhase>
+__global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS)
+    k_predictor(BatchArgs a, DevOps<N, R> op) {
+  using C = PredCfg<Sys, N, R>;
+  constexpr int P = N + 1, P2 = P * P, V = Sys::V, CPB = C::CPB;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R* sm = reinterpret_cast<R*>(smem_raw);
+
+  const int t = threadIdx.x;
+  const int lc = t / P2;
+  const int node = t - lc * P2;
+  const int i = node % P, j = node / P;
+  const long long cell = (long long)blockIdx.x * CPB + lc;
+  const bool in_cta = lc < CPB;
+  const bool valid = in_cta && cell < a.ncells;
+  R* cs = sm + (size_t)(in_cta ? lc : 0) * C::CELL_ELEMS;
+
+  int k_inst = valid ? find_inst_cell(a.inst, a.ninst, cell) : 0;
+  const InstDesc& in = a.inst[k_inst];
+  const bool act = valid && a.st[k_inst].active;
+  const double dt = act ? a.st[k_inst].dt : 0.0;
+  const double* uh_in = a.uh[valid ? parity(a.st[k_inst]) : 0];
+  const Phys ph = in.ph;
+
+  // per-thread contraction rows: Dx(i,k) = Kxi(k,i) dt/(dx w_i), Dy(j,k) likewise
+  R Dx[P], Dy[P], Gx[P], Gy[P];
+  {
+    const R cxw = R(dt / in.dx) / op.w[i];
+    const R cyw = R(dt / in.dy) / op.w[j];
+#pragma unroll
+    for (int k = 0; k < P; ++k) {
+      Dx[k] = op.Kxi[k + P * i] * cxw;
+      Dy[k] = op.Kxi[k + P * j] * cyw;
+      // gradient rows dudx(i,k)/dx (BN volume fraction, AD state)
+      Gx[k] = op.dudx[i + P * k] / R(in.dx);
+      Gy[k] = op.dudx[j + P * k] / R(in.dy);
+    }
+  }
+
+  R u[V];
+  {
+    const double* src = uh_in + ((size_t)(valid ? cell : 0) * P2 + node) * V;
+#pragma unroll
+    for (int v = 0; v < V; ++v) u[v] = act ? R(src[v]) : R(1);
+  }
+  const R rdt = R(dt);
+
+  R q[P][V];
+  R Fh[2][V];   // time-averaged fluxes of the last iteration
+  R Sh[V];      // BN: time-averaged -NCP of the last iteration
+  R Gh[2];      // AD: time-averaged gradient of the last iteration
+  R qh[V];      // time-averaged state
+
+  auto fidx = [&](int l, int d, int v) { return (size_t)((l * 2 + d) * V + v) * P2 + node; };
+
+  if constexpr (Sys::ID == kSysAD) {
+    // -------------------------------------------------------------- AD
+    // state buffer [P][P2] after the flux buffer [P][2][P2]
+    R* qs = cs + 2 * P * P2;
+    const R ca = R(ph.a), ccx = R(ph.cx), ccy = R(ph.cy);
+    const bool fused = ph.ad_fused != 0;
+    // iteration 1: constant in time
+    qs[node] = u[0];
+    __syncthreads();
+    {
+      R gx = R(0), gy = R(0);
+#pragma unroll
+      for (int k = 0; k < P; ++k) {
+        gx = fma(Gx[k], qs[k + P * j], gx);
+        gy = fma(Gy[k], qs[i + P * k], gy);
+      }
+      R fx = -ca * gx, fy = -ca * gy;
+      if (fused) {
+        fx = fma(ccx, u[0], fx);
+        fy = fma(ccy, u[0], fy);
+      }
+      cs[node] = fx;
+      cs[P2 + node] = fy;
+    }
+    __syncthreads();
+    {
+      R b[1];
+      contract<1, P>(cs, 0, i, j, Dx, Dy, b);
+#pragma unroll
+      for (int l = 0; l < P; ++l) q[l][0] = op.g[l] * u[0] - op.ts[l] * b[0];
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int it = 2; it <= P; ++it) {
+      const bool last = it == P;
+#pragma unroll
+      for (int l = 0; l < P; ++l) qs[l * P2 + node] = q[l][0];
+      __syncthreads();
+      if (last) { Fh[0][0] = Fh[1][0] = R(0); Gh[0] = Gh[1] = R(0); }
+#pragma unroll
+      for (int l = 0; l < P; ++l) {
+        R gx = R(0), gy = R(0);
+#pragma unroll
+        for (int k = 0; k < P; ++k) {
+          gx = fma(Gx[k], qs[l * P2 + k + P * j], gx);
+          gy = fma(Gy[k], qs[l * P2 + i + P * k], gy);
+        }
+        R fx = -ca * gx, fy = -ca * gy;
+        if (fused) {
+          fx = fma(ccx, q[l][0], fx);
+          fy = fma(ccy, q[l][0], fy);
+        }
+        cs[fidx(l, 0, 0)] = fx;
+        cs[fidx(l, 1, 0)] = fy;
+        if (last) {
+          Fh[0][0] = fma(op.w[l], fx, Fh[0][0]);
+          Fh[1][0] = fma(op.w[l], fy, Fh[1][0]);
+          Gh[0] = fma(op.w[l], gx, Gh[0]);
+          Gh[1] = fma(op.w[l], gy, Gh[1]);
+        }
+      }
+      __syncthreads();
+      if (!last) {
+#pragma unroll
+        for (int l = 0; l < P; ++l) q[l][0] = op.g[l] * u[0];
+#pragma unroll
+        for (int l = 0; l < P; ++l) {
+          R b[1];
+          contract<1, P>(cs, l, i, j, Dx, Dy, b);
+#pragma unroll
+          for (int lp = 0; lp < P; ++lp) q[lp][0] = fma(-op.T[lp + P * l], b[0], q[lp][0]);
+        }
+      } else {
+        qh[0] = op.wg * u[0];
+#pragma unroll
+        for (int l = 0; l < P; ++l) {
+          R b[1];
+          contract<1, P>(cs, l, i, j, Dx, Dy, b);
+          qh[0] = fma(-op.tw[l], b[0], qh[0]);
+        }
+      }
+      __syncthreads();
+    }
+  } else {
+    // ------------------------------------------------- Euler / Baer-Nunziato
+    constexpr bool BN = Sys::ID == kSysBN;
+    R* as = cs + (size_t)2 * V * P * P2;  // BN volume fraction [P][P2]
+    R pg[P], us[P], vs[P];                // BN: NCP scalars per time level
+    // iteration 1: the state is constant in time
+    {
+      R Fx[V], Fy[V];
+      if constexpr (BN) {
+        Sys::template pflux<R>(ph, u, Fx, Fy, pg[0], us[0], vs[0]);
+        as[node] = u[8];
+      } else {
+        Sys::template pflux<R>(ph, u, Fx, Fy);
+      }
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        cs[fidx(0, 0, v)] = Fx[v];
+        cs[fidx(0, 1, v)] = Fy[v];
+      }
+      __syncthreads();
+      R b[V];
+      contract<V, P>(cs, 0, i, j, Dx, Dy, b);
+      if constexpr (BN) {
+        R ax = R(0), ay = R(0);
+#pragma unroll
+        for (int k = 0; k < P; ++k) {
+          ax = fma(Gx[k], as[k + P * j], ax);
+          ay = fma(Gy[k], as[i + P * k], ay);
+        }
+        R n[9];
+        BNSys::pncp<R>(pg[0], us[0], vs[0], ax, ay, n);
+#pragma unroll
+        for (int v = 0; v < V; ++v) b[v] = fma(rdt, n[v], b[v]);
+      }
+#pragma unroll
+      for (int l = 0; l < P; ++l)
+#pragma unroll
+        for (int v = 0; v < V; ++v) q[l][v] = op.g[l] * u[v] - op.ts[l] * b[v];
+      __syncthreads();
+    }
+#pragma unroll 1
+    for (int it = 2; it <= P; ++it) {
+      const bool last = it == P;
+      if (last) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) { Fh[0][v] = R(0); Fh[1][v] = R(0); }
+      }
+#pragma unroll
+      for (int l = 0; l < P; ++l) {
+        R Fx[V], Fy[V];
+        if constexpr (BN) {
+          Sys::template pflux<R>(ph, q[l], Fx, Fy, pg[l], us[l], vs[l]);
+          as[l * P2 + node] = q[l][8];
+        } else {
+          Sys::template pflux<R>(ph, q[l], Fx, Fy);
+        }
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          cs[fidx(l, 0, v)] = Fx[v];
+          cs[fidx(l, 1, v)] = Fy[v];
+          if (last) {
+            Fh[0][v] = fma(op.w[l], Fx[v], Fh[0][v]);
+            Fh[1][v] = fma(op.w[l], Fy[v], Fh[1][v]);
+          }
+        }
+      }
+      __syncthreads();
+      if (!last) {
+#pragma unroll
+        for (int l = 0; l < P; ++l)
+#pragma unroll
+          for (int v = 0; v < V; ++v) q[l][v] = op.g[l] * u[v];
+      } else {
+#pragma unroll
+        for (int v = 0; v < V; ++v) { qh[v] = op.wg * u[v]; Sh[v] = R(0); }
+      }
+#pragma unroll
+      for (int l = 0; l < P; ++l) {
+        R b[V];
+        contract<V, P>(cs, l, i, j, Dx, Dy, b);
+        if constexpr (BN) {
+          R ax = R(0), ay = R(0);
+#pragma unroll
+          for (int k = 0; k < P; ++k) {
+            ax = fma(Gx[k], as[l * P2 + k + P * j], ax);
+            ay = fma(Gy[k], as[l * P2 + i + P * k], ay);
+          }
+          R n[9];
+          BNSys::pncp<R>(pg[l], us[l], vs[l], ax, ay, n);
+#pragma unroll
+          for (int v = 0; v < V; ++v) {
+            b[v] = fma(rdt, n[v], b[v]);
+            if (last) Sh[v] = fma(-op.w[l], n[v], Sh[v]);
+          }
+        }
+        if (!last) {
+#pragma unroll
+          for (int lp = 0; lp < P; ++lp)
+#pragma unroll
+            for (int v = 0; v < V; ++v) q[lp][v] = fma(-op.T[lp + P * l], b[v], q[lp][v]);
+        } else {
+#pragma unroll
+          for (int v = 0; v < V; ++v) qh[v] = fma(-op.tw[l], b[v], qh[v]);
+        }
+      }
+      __syncthreads();
+    }
+  }
+
+  // ------------------------------------------------------------- epilogue
+  // shared layout per cell: Q [V][P2], FX [V][P2], FY [V][P2] (AD: + GX, GY)
+  R* sQ = cs;
+  R* sX = cs + V * P2;
+  R* sY = cs + 2 * V * P2;
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    sQ[v * P2 + node] = qh[v];
+    sX[v * P2 + node] = Fh[0][v];
+    sY[v * P2 + node] = Fh[1][v];
+  }
+  if constexpr (Sys::ID == kSysAD) {
+    cs[3 * P2 + node] = Gh[0];
+    cs[4 * P2 + node] = Gh[1];
+  }
+  __syncthreads();
+  if (!act) return;
+
+  if constexpr (kPhase) {
+    // qhi(v,i,j), Fhi(v,d,i,j), Shi(v,i,j) in the reference layout
+    const size_t base = (size_t)cell * P2 + node;
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      a.qhi[base * V + v] = (double)qh[v];
+      a.fhi[(base * 2 + 0) * V + v] = (double)Fh[0][v];
+      a.fhi[(base * 2 + 1) * V + v] = (double)Fh[1][v];
+      if constexpr (Sys::ID == kSysBN) a.shi[base * V + v] = (double)Sh[v];
+    }
+  } else {
+    // volume integral: duh = (w_j/dx) sum_k Kxi(i,k) Fhi_x(k,j) + (w_i/dy) sum_k Kxi(j,k) Fhi_y(i,k) [+ w_i w_j Shi]
+    const R vx = op.w[j] / R(in.dx), vy = op.w[i] / R(in.dy);
+    double* dst = a.duh + ((size_t)cell * P2 + node) * V;
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      R sxv = R(0), syv = R(0);
+#pragma unroll
+      for (int k = 0; k < P; ++k) {
+        sxv = fma(op.Kxi[i + P * k], sX[v * P2 + k + P * j], sxv);
+        syv = fma(op.Kxi[j + P * k], sY[v * P2 + i + P * k], syv);
+      }
+      R d = sxv * vx + syv * vy;
+      if constexpr (Sys::ID == kSysBN) d = fma(op.w[i] * op.w[j], Sh[v], d);
+      dst[v] = (double)d;
+    }
+  }
+
+  // face extrapolation: faces 0 left, 1 right (x), 2 bottom, 3 top (y); point l
+  R* qb = reinterpret_cast<R*>(a.qbnd);
+  R* fb = reinterpret_cast<R*>(a.fbnd);
+  for (int idx = node; idx < 4 * P; idx += P2) {
+    const int f = idx / P, l = idx - f * P;
+    const R* c = (f == 0 || f == 2) ? op.FL : op.FR;
+    const size_t o = ((size_t)cell * P + l) * 4 + f;
+    const bool xdir = f < 2;
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      R sq = R(0), sf = R(0);
+#pragma unroll
+      for (int m = 0; m < P; ++m) {
+        const int nd = xdir ? (m + P * l) : (l + P * m);
+        sq = fma(c[m], sQ[v * P2 + nd], sq);
+        if constexpr (Sys::ID != kSysAD) sf = fma(c[m], (xdir ? sX : sY)[v * P2 + nd], sf);
+      }
+      qb[o * V + v] = sq;
+      if constexpr (Sys::ID != kSysAD) fb[o * V + v] = sf;
+    }
+    if constexpr (Sys::ID == kSysAD) {
+      // gradQbnd(v,d,f,l)
+#pragma unroll
+      for (int d = 0; d < 2; ++d) {
+        R sg = R(0);
+#pragma unroll
+        for (int m = 0; m < P; ++m) {
+          const int nd = xdir ? (m + P * l) : (l + P * m);
+          sg = fma(c[m], cs[(3 + d) * P2 + nd], sg);
+        }
+        fb[o * 2 + d] = sg;
+      }
+    }
+  }
+}
+
+}  // namespace aderdg

@@ -1,0 +1,115 @@
+// predictor_tu.cu -- instantiates the space-time predictor (K1) for one
+// (system, N), selected by -DADERDG_SYS=<0|1|2> -DADERDG_N=<1..5>.
+// Compiled with fused multiply-adds (the predictor's contractions are FMA
+// chains; its results agree with the reference to rounding, not bit for bit).
+#include <cmath>
+
+#include "predictor.cuh"
+#include "tables.h"
+
+#ifndef ADERDG_SYS
+#error "ADERDG_SYS must be defined"
+#endif
+#ifndef ADERDG_N
+#error "ADERDG_N must be defined"
+#endif
+
+namespace aderdg {
+namespace {
+
+#if ADERDG_SYS == 0
+using Sys = ADSys;
+#elif ADERDG_SYS == 1
+using Sys = EulerSys;
+#else
+using Sys = BNSys;
+#endif
+constexpr int N = ADERDG_N;
+
+template <class R>
+void make_ops(const HostOps& h, void* out) {
+  constexpr int P = N + 1, S = 2 * N + 1;
+  DevOps<N, R> o;
+  for (int a = 0; a < P; ++a) {
+    o.w[a] = (R)h.w[a];
+    o.FL[a] = (R)h.FL[a];
+    o.FR[a] = (R)h.FR[a];
+    o.wd[a] = h.w[a];
+    o.FLd[a] = h.FL[a];
+    o.FRd[a] = h.FR[a];
+    o.xid[a] = h.xi[a];
+  }
+  for (int k = 0; k < P * P; ++k) {
+    o.Kxi[k] = (R)h.Kxi[k];
+    o.dudx[k] = (R)h.dudx[k];
+  }
+  // derived time operators (FP64, no contraction: identical on every host)
+  double T[P][P];
+  for (int lp = 0; lp < P; ++lp)
+    for (int l = 0; l < P; ++l) T[lp][l] = h.iK1[lp + P * l] * h.w[l];
+  double wg = 0.0;
+  for (int lp = 0; lp < P; ++lp) {
+    double g = 0.0, ts = 0.0;
+    for (int l = 0; l < P; ++l) {
+      g += h.iK1[lp + P * l] * h.F0[l];
+      ts += T[lp][l];
+      o.T[lp + P * l] = (R)T[lp][l];
+    }
+    o.g[lp] = (R)g;
+    o.ts[lp] = (R)ts;
+    wg += h.w[lp] * g;
+  }
+  for (int l = 0; l < P; ++l) {
+    double tw = 0.0;
+    for (int lp = 0; lp < P; ++lp) tw += h.w[lp] * T[lp][l];
+    o.tw[l] = (R)tw;
+  }
+  o.wg = (R)wg;
+  for (int k = 0; k < S * P; ++k) {
+    o.uh2lim[k] = h.uh2lim[k];
+    o.lim2uh[k] = h.lim2uh[k];
+  }
+  for (int k = 0; k < P * P; ++k) o.uh2lob[k] = h.uh2lob[k];
+  *reinterpret_cast<DevOps<N, R>*>(out) = o;
+}
+
+template <class R, bool kPhase>
+cudaError_t launch_pred(const BatchArgs& a, const void* ops, cudaStream_t s) {
+  using C = PredCfg<Sys, N, R>;
+  auto kern = k_predictor<Sys, N, R, kPhase>;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  const long long grid = (a.ncells + C::CPB - 1) / C::CPB;
+  if (grid <= 0) return cudaSuccess;
+  kern<<<(unsigned)grid, C::THREADS, C::SMEM_BYTES, s>>>(a, *reinterpret_cast<const DevOps<N, R>*>(ops));
+  return cudaGetLastError();
+}
+
+cudaError_t predictor(const BatchArgs& a, const void* ops, int fp32, bool phase, cudaStream_t s) {
+  if (fp32) return phase ? cudaErrorNotSupported : launch_pred<float, false>(a, ops, s);
+  return phase ? launch_pred<double, true>(a, ops, s) : launch_pred<double, false>(a, ops, s);
+}
+
+}  // namespace
+
+#define ADERDG_CAT2(a, b, c) a##b##_##c
+#define ADERDG_CAT(a, b, c) ADERDG_CAT2(a, b, c)
+void ADERDG_CAT(register_predictor_, ADERDG_SYS, ADERDG_N)(KernelTable& t) {
+  t.sys = ADERDG_SYS;
+  t.N = N;
+  t.ops64_size = sizeof(DevOps<N, double>);
+  t.ops32_size = sizeof(DevOps<N, float>);
+  t.make_ops64 = &make_ops<double>;
+  t.make_ops32 = &make_ops<float>;
+  t.predictor = &predictor;
+  t.pred_cells_per_cta[0] = PredCfg<Sys, N, double>::CPB;
+  t.pred_cells_per_cta[1] = PredCfg<Sys, N, float>::CPB;
+  t.pred_threads[0] = PredCfg<Sys, N, double>::THREADS;
+  t.pred_threads[1] = PredCfg<Sys, N, float>::THREADS;
+}
+
+}  // namespace aderdg

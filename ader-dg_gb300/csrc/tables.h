@@ -1,0 +1,38 @@
+// tables.h -- host-side launch table for one (system, N) kernel family.
+//
+// The kernels are templates on the PDE system and the degree N; each
+// (system, N) pair is compiled in two translation units (predictor_tu.cu with
+// fused multiply-adds, exact_tu.cu with --fmad=false) that fill one table.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+#include "common.cuh"
+#include "setup.h"
+
+namespace aderdg {
+
+struct KernelTable {
+  int sys = -1, N = 0;
+  // predictor translation unit
+  size_t ops64_size = 0, ops32_size = 0;
+  void (*make_ops64)(const HostOps&, void* out) = nullptr;
+  void (*make_ops32)(const HostOps&, void* out) = nullptr;
+  cudaError_t (*predictor)(const BatchArgs&, const void* ops, int fp32, bool phase, cudaStream_t) = nullptr;
+  int pred_cells_per_cta[2] = {0, 0};
+  int pred_threads[2] = {0, 0};
+  // exact translation unit
+  cudaError_t (*faces)(const BatchArgs&, const FaceConst&, int fp32, cudaStream_t) = nullptr;
+  cudaError_t (*cells)(const BatchArgs&, const void* ops64, cudaStream_t) = nullptr;
+  cudaError_t (*volume)(const BatchArgs&, const void* ops64, cudaStream_t) = nullptr;
+  cudaError_t (*mark)(const BatchArgs&, cudaStream_t) = nullptr;
+  cudaError_t (*subcell)(const BatchArgs&, const void* ops64, const FaceConst&, int grid, cudaStream_t) = nullptr;
+  int (*subcell_grid)(int num_sms) = nullptr;
+};
+
+// Returns the table for (sys, N) or nullptr when that pair was not built.
+const KernelTable* kernel_table(int sys, int N);
+
+}  // namespace aderdg

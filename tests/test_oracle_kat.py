@@ -1,0 +1,172 @@
+"""Known-answer tests pinning the CPU oracle.
+
+The reference ships no tests, golden vectors or fixtures and cannot be
+compiled here (no Fortran compiler), so the oracle is pinned by the
+mathematics the reference's algorithm satisfies: operator identities,
+free-stream preservation, conservation, and convergence to exact solutions.
+"""
+import numpy as np
+import pytest
+
+import pyoracle as po
+
+
+def ops(N):
+    o = po.Oracle(po.make_config(po.SYS_EULER, N, 2, 2))
+    P, S = N + 1, 2 * N + 1
+    g = lambda w, r, c: o.operator(w).reshape(r, c, order="F")  # noqa: E731
+    return dict(xi=o.operator(po.OP_XI), w=o.operator(po.OP_W), MM=g(po.OP_MM, P, P), Kxi=g(po.OP_KXI, P, P),
+                dudx=g(po.OP_DUDX, P, P), K1=g(po.OP_K1, P, P), iK1=g(po.OP_IK1, P, P), F0=o.operator(po.OP_F0),
+                FL=o.operator(po.OP_FL), FR=o.operator(po.OP_FR), uh2lim=g(po.OP_UH2LIM, S, P),
+                lim2uh=g(po.OP_LIM2UH, P, S), uh2lob=g(po.OP_UH2LOB, P, P), xilob=o.operator(po.OP_XILOB),
+                wlob=o.operator(po.OP_WLOB), bary=o.operator(po.OP_XILIMBARY))
+
+
+@pytest.mark.parametrize("N", [1, 2, 3, 4, 5])
+def test_operator_identities(N):
+    P, S = N + 1, 2 * N + 1
+    o = ops(N)
+    # Gauss-Legendre: weights sum to 1, nodes symmetric, exact for degree 2N+1
+    assert abs(o["w"].sum() - 1.0) < 1e-14  # weights use the previous Newton iterate (quadrature.f90:33-38)
+    assert np.allclose(o["xi"] + o["xi"][::-1], 1.0, atol=1e-15)
+    for k in range(2 * N + 2):
+        assert abs((o["w"] * o["xi"] ** k).sum() - 1.0 / (k + 1)) < 1e-14
+    # nodal basis: MM = diag(w)
+    assert np.abs(o["MM"] - np.diag(o["w"])).max() < 1e-15
+    # stiffness: Kxi(k,l) = int phi_k' phi_l; row sums = phi_k(1) - phi_k(0)
+    assert np.abs(o["Kxi"].sum(axis=1) - (o["FR"] - o["FL"])).max() < 1e-12
+    # K1 iK1 = I
+    assert np.abs(o["K1"] @ o["iK1"] - np.eye(P)).max() < 1e-12
+    # iK1 F0 = 1 (the constant is a fixed point of the time predictor)
+    assert np.abs(o["iK1"] @ o["F0"] - 1.0).max() < 1e-12
+    # dudx differentiates polynomials of degree N exactly
+    for k in range(N + 1):
+        f = o["xi"] ** k
+        df = k * o["xi"] ** (k - 1) if k else 0 * f
+        assert np.abs(o["dudx"] @ f - df).max() < 1e-10
+    # extrapolation to the faces
+    assert abs(o["FL"].sum() - 1) < 1e-14 and abs(o["FR"].sum() - 1) < 1e-14
+    # subcell maps: averages of the polynomial, and the constrained LSQ inverse
+    assert np.abs(o["uh2lim"].sum(axis=1) - 1.0).max() < 1e-13
+    assert np.abs(o["lim2uh"] @ o["uh2lim"] - np.eye(P)).max() < 1e-12
+    # put_subcell_data preserves the cell average (the w-constraint row)
+    rng = np.random.default_rng(N)
+    lim = rng.normal(size=S)
+    assert abs(o["w"] @ (o["lim2uh"] @ lim) - lim.mean()) < 1e-13
+    # Gauss-Lobatto: end points included, weights sum to 1
+    assert abs(o["xilob"].min()) < 1e-15 and abs(o["xilob"].max() - 1) < 1e-15
+    assert abs(o["wlob"].sum() - 1.0) < 1e-14
+    assert np.abs(o["uh2lob"].sum(axis=1) - 1.0).max() < 1e-13
+    assert np.allclose(o["bary"], (np.arange(S) + 0.5) / S, atol=1e-15)
+
+
+def _run(cfg, uh, steps, tend=1e9, lh=None):
+    o = po.Oracle(cfg)
+    o.set(po.UH, uh)
+    if lh is not None:
+        o.init_limiter(lh)
+    t = 0.0
+    for _ in range(steps):
+        t, dt, n = o.step(t, tend)
+    return o, t
+
+
+@pytest.mark.parametrize("system,V", [(po.SYS_EULER, 4), (po.SYS_BN, 9)])
+def test_free_stream_preserved(system, V):
+    cfg = po.make_config(system, 3, 6, 5, xl=(0, 0), xr=(1.0, 0.8), bc=(3, 3, 1, 1))
+    o = po.Oracle(cfg)
+    if system == po.SYS_EULER:
+        q = np.array([1.3, 0.4, -0.2, 2.9])
+    else:
+        q = np.zeros(9)
+        prim = dict(rs=1.1, us=0.3, vs=-0.1, ps=1.2, rg=0.7, ug=0.3, vg=-0.1, pg=0.9, a=0.6)
+        q = po.initial_field(cfg, po.IC_BN_CYLINDER, (0, 0, 0.0, 0.6, 1.1, 1.2, 0.7, 0.9, 0.6, 1.1, 1.2, 0.7, 0.9),
+                             0.3, 0.3)
+        del prim
+    uh = np.tile(q, cfg.imax * cfg.jmax * 16)
+    o.set(po.UH, uh)
+    t = 0.0
+    for _ in range(3):
+        t, dt, n = o.step(t, 10.0)
+        assert n == 0
+    u = o.get(po.UH)
+    assert np.abs(u - uh).max() < 1e-12 * max(1.0, np.abs(uh).max())
+
+
+def test_euler_conservation_periodic():
+    cfg = po.make_config(po.SYS_EULER, 3, 12, 12, xl=(0, 0), xr=(10, 10), bc=(3, 3, 3, 3), limiter=0)
+    o = po.Oracle(cfg)
+    uh, _ = o.project_ic(po.IC_EULER_VORTEX, (5, 5, 5, 1, 1, 1, 1))
+    o2, t = _run(cfg, uh, 4)
+    w = ops(3)["w"]
+    W = np.outer(w, w).ravel()
+    tot = lambda a: (a.reshape(-1, 16, 4) * W[None, :, None]).sum(axis=(0, 1))  # noqa: E731
+    assert np.abs(tot(o2.get(po.UH)) - tot(uh)).max() < 1e-12 * np.abs(tot(uh)).max()
+
+
+def _ad_error(n, N, tend):
+    cfg = po.make_config(po.SYS_ADVDIFF, N, n, n, xl=(0, 0), xr=(1, 1), bc=(3, 3, 3, 3), cx=1.0, cy=1.0, a=1e-3,
+                         ad_flux_mode=1, limiter=0)
+    o = po.Oracle(cfg)
+    uh, _ = o.project_ic(po.IC_AD_SINE, (1.0,))
+    o.set(po.UH, uh)
+    t = 0.0
+    while t < tend:
+        t, dt, _ = o.step(t, tend)
+    # exact: translated by c t and damped by exp(-8 pi^2 a t)
+    xi = o.operator(po.OP_XI)
+    P, h = N + 1, 1.0 / n
+    ii, jj = np.meshgrid(np.arange(n), np.arange(n), indexing="xy")
+    x = (ii[:, :, None, None] + xi[None, None, None, :]) * h
+    y = (jj[:, :, None, None] + xi[None, None, :, None]) * h
+    ex = np.exp(-8 * np.pi ** 2 * 1e-3 * t) * np.sin(2 * np.pi * (x - t)) * np.sin(2 * np.pi * (y - t))
+    ex = ex.reshape(n * n, P * P)
+    u = o.get(po.UH).reshape(n * n, P * P)
+    return np.abs(u - ex).max()
+
+
+def test_ad_convergence_order():
+    """Fused-flux advection-diffusion converges with order close to N+1."""
+    N = 2
+    e1, e2 = _ad_error(8, N, 0.05), _ad_error(16, N, 0.05)
+    order = np.log2(e1 / e2)
+    assert order > N + 1 - 0.6, (e1, e2, order)
+
+
+def test_dmr_initial_limiter_marks_the_shock():
+    """The initial DMP (argmax 0.1) limits cells cut by the DMR discontinuity only."""
+    cfg = po.make_config(po.SYS_EULER, 2, 24, 6, xl=(0, 0), xr=(4, 1), bc=(1, 1, 1, 1), bc_mode=1)
+    o = po.Oracle(cfg)
+    uh, lh = o.project_ic(po.IC_EULER_DMR, ())
+    o.set(po.UH, uh)
+    n = o.init_limiter(lh)
+    st = o.get_int(po.STATUS).reshape(6, 24)
+    assert 0 < n < 24 * 6 // 2
+    # limited cells straddle x = 1/6 + y / tan(60 deg)
+    dx = 4 / 24
+    for j in range(6):
+        for i in range(24):
+            x0, x1 = i * dx, (i + 1) * dx
+            ys = ((j) / 6, (j + 1) / 6)
+            xs = [1 / 6 + y / np.tan(np.pi / 3) for y in ys]
+            cut = min(xs) < x1 and max(xs) > x0
+            if st[j, i]:
+                assert cut
+
+
+def test_oracle_step_rp2d_limiter_runs():
+    cfg = po.make_config(po.SYS_EULER, 3, 16, 16, bc=(1, 1, 1, 1))
+    o = po.Oracle(cfg)
+    p = (0.5, 0.5, 1.5, 0.0, 0.0, 1.5, 0.5323, 1.206, 0.0, 0.3, 0.138, 1.206, 1.206, 0.029, 0.5323, 0.0, 1.206, 0.3)
+    uh, lh = o.project_ic(po.IC_EULER_RP2D, p)
+    o.set(po.UH, uh)
+    o.init_limiter(lh)
+    t = 0.0
+    counts = []
+    for _ in range(3):
+        t, dt, n = o.step(t, 0.25)
+        counts.append(n)
+        u = o.get(po.UH)
+        assert np.isfinite(u).all()
+    assert max(counts) > 0  # the discontinuities trigger the limiter
+    assert o.get_int(po.STATUS).sum() > 0
