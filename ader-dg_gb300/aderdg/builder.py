@@ -18,6 +18,7 @@ INCLUDE = os.path.join(REPO_ROOT, "include")
 BUILD_DIR = os.path.join(PKG_ROOT, "_build")
 LIB_NAME = "libaderdg_gpu.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
+DRIVER_PATH = os.path.join(BUILD_DIR, "aderdg_driver")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SYSTEMS = (0, 1, 2)
@@ -28,6 +29,10 @@ def _nvcc():
     cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
     p = os.path.join(cuda, "bin", "nvcc")
     return p if os.path.exists(p) else (shutil.which("nvcc") or "nvcc")
+
+
+def _cxx():
+    return shutil.which("g++") or "g++"
 
 
 def _common_flags():
@@ -54,7 +59,7 @@ def _jobs():
 
 def _stamp():
     h = hashlib.sha256()
-    for d in (CSRC, INCLUDE):
+    for d in (CSRC, INCLUDE, os.path.join(PKG_ROOT, "host")):
         for f in sorted(os.listdir(d)):
             p = os.path.join(d, f)
             if os.path.isfile(p):
@@ -93,6 +98,11 @@ def build(force=False, verbose=False, max_workers=None):
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed: %s\n%s%s" % (" ".join(link), r.stdout, r.stderr))
+    drv = [_cxx(), "-O2", "-std=c++17", "-I" + INCLUDE, os.path.join(PKG_ROOT, "host", "aderdg_driver.cpp"),
+           "-o", DRIVER_PATH, "-L" + BUILD_DIR, "-laderdg_gpu", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(drv, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("driver build failed: %s\n%s%s" % (" ".join(drv), r.stdout, r.stderr))
     with open(stamp_path, "w") as fh:
         fh.write(stamp)
     return LIB_PATH

@@ -147,7 +147,8 @@ def load(build_if_missing=False):
         "aderdg_last_error": (ctypes.c_char_p, [vp]),
         "aderdg_project_initial_condition": (i, [cfgp, i, dp, dp, dp]),
         "aderdg_probe_peaks": (i, [dp, dp]), "aderdg_set_array": (i, [vp, i, vp]),
-        "aderdg_operator": (i, [i, i, dp]),
+        "aderdg_operator": (i, [i, i, dp]), "aderdg_step_host": (i, [vp, dp, dp, d, dp, ip]),
+        "aderdg_time_steps": (i, [vp, dp, d, i, i, dp]), "aderdg_profile_step": (i, [vp, dp, d, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -163,7 +164,7 @@ EXPORTED = ("aderdg_create", "aderdg_destroy", "aderdg_upload", "aderdg_init_lim
             "aderdg_riemann_problem", "aderdg_surface_integral", "aderdg_element_update", "aderdg_limiter",
             "aderdg_step", "aderdg_run", "aderdg_array_size", "aderdg_get_array", "aderdg_get_info",
             "aderdg_last_error", "aderdg_project_initial_condition", "aderdg_probe_peaks", "aderdg_set_array",
-            "aderdg_operator")
+            "aderdg_operator", "aderdg_step_host", "aderdg_time_steps", "aderdg_profile_step")
 
 
 def _dp(a):
@@ -318,6 +319,32 @@ class Solver:
         n = ctypes.c_int(0)
         self._ck(self.L.aderdg_run(self.h, ctypes.byref(t), tend, max_steps, sync_every, ctypes.byref(n)))
         return t.value, n.value
+
+    def step_host(self, uh, time, tend):
+        """One step with host arrays: uh is updated in place (float64, C-contiguous)."""
+        assert uh.dtype == np.float64 and uh.flags.c_contiguous and uh.size == self.cfg.dofs
+        t = ctypes.c_double(time)
+        dt = ctypes.c_double(0)
+        n = ctypes.c_int(0)
+        self._ck(self.L.aderdg_step_host(self.h, _dp(uh), ctypes.byref(t), tend, ctypes.byref(dt), ctypes.byref(n)))
+        return t.value, dt.value, n.value
+
+    # measurement
+    def time_steps(self, time, tend, steps, flush_l2=True):
+        """Device milliseconds of each of `steps` fused steps."""
+        t = ctypes.c_double(time)
+        ms = np.zeros(steps, dtype=np.float64)
+        self._ck(self.L.aderdg_time_steps(self.h, ctypes.byref(t), tend, steps, 1 if flush_l2 else 0, _dp(ms)))
+        return t.value, ms
+
+    PHASES = ("begin", "predictor", "faces", "cells", "mark", "subcell", "end")
+
+    def profile_step(self, time, tend):
+        """Device milliseconds of each launch of one fused step."""
+        t = ctypes.c_double(time)
+        ms = np.zeros(7, dtype=np.float64)
+        self._ck(self.L.aderdg_profile_step(self.h, ctypes.byref(t), tend, _dp(ms)))
+        return t.value, dict(zip(self.PHASES, ms))
 
     # introspection
     def get(self, which):

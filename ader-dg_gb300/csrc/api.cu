@@ -40,6 +40,8 @@ struct aderdg_ctx {
   bool uploaded = false;
   bool pending = false;  // between element_update and the limiter commit (phase API)
   cudaGraphExec_t gexec = nullptr;
+  void* flush_buf = nullptr;
+  size_t flush_bytes = 0;
   std::string err;
 };
 
@@ -163,10 +165,32 @@ int launch_step(aderdg_ctx* c) {
 
 void free_all(aderdg_ctx* c) {
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->flush_buf) cudaFree(c->flush_buf);
   for (void* p : c->allocs) cudaFree(p);
   c->allocs.clear();
   if (c->h_st) cudaFreeHost(c->h_st);
   if (c->stream) cudaStreamDestroy(c->stream);
+}
+
+int ensure_graph(aderdg_ctx* c) {
+  if (c->gexec) return ADERDG_OK;
+  cudaGraph_t g = nullptr;
+  CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  int r = launch_step(c);
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  if (r) {
+    if (g) cudaGraphDestroy(g);
+    return r;
+  }
+  if (e != cudaSuccess) return fail_cuda(c, "cudaStreamEndCapture", e);
+  e = cudaGraphInstantiate(&c->gexec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail_cuda(c, "cudaGraphInstantiate", e);
+  return ADERDG_OK;
+}
+
+__global__ void k_flush(unsigned int* p, size_t n, unsigned int v) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) p[k] = v + (unsigned)k;
 }
 
 int ensure_phase_buffers(aderdg_ctx* c) {
@@ -535,20 +559,8 @@ int aderdg_run(aderdg_ctx* c, double* time, double tend, int max_steps, int sync
   if (sync_every <= 0) sync_every = 64;
   int r = set_clock(c, *time, tend);
   if (r) return r;
-  if (!c->gexec) {
-    cudaGraph_t g = nullptr;
-    CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    r = launch_step(c);
-    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
-    if (r) {
-      if (g) cudaGraphDestroy(g);
-      return r;
-    }
-    if (e != cudaSuccess) return fail_cuda(c, "cudaStreamEndCapture", e);
-    e = cudaGraphInstantiate(&c->gexec, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) return fail_cuda(c, "cudaGraphInstantiate", e);
-  }
+  r = ensure_graph(c);
+  if (r) return r;
   const long long steps0 = c->h_st->steps;
   int launched = 0;
   while (launched < max_steps) {
@@ -562,6 +574,105 @@ int aderdg_run(aderdg_ctx* c, double* time, double tend, int max_steps, int sync
   *time = c->h_st->time;
   if (steps_done) *steps_done = (int)(c->h_st->steps - steps0);
   if (c->h_st->nonfinite) return fail(c, ADERDG_ENONFINITE, "the time step became non-finite");
+  return ADERDG_OK;
+}
+
+int aderdg_step_host(aderdg_ctx* c, double* uh, double* time, double tend, double* dt, int* n_recompute) {
+  if (!c || !uh || !time) return fail(c, ADERDG_EINVAL, "null argument");
+  if (!c->uploaded) return fail(c, ADERDG_ESTATE, "upload uh first");
+  if (c->pending) return fail(c, ADERDG_ESTATE, "finish the phase-API step first");
+  const size_t n = (size_t)c->ncells * c->P * c->P * c->V * sizeof(double);
+  CK(c, cudaMemcpyAsync(c->args.uh[cur_par(c)], uh, n, cudaMemcpyHostToDevice, c->stream));
+  int r = prime(c);
+  if (!r) r = set_clock(c, *time, tend);
+  if (!r) r = ensure_graph(c);
+  if (r) return r;
+  CK(c, cudaGraphLaunch(c->gexec, c->stream));
+  CK(c, cudaMemcpyAsync(c->h_st, c->d_st, sizeof(InstState), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  CK(c, cudaMemcpyAsync(uh, c->args.uh[cur_par(c)], n, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  *time = c->h_st->time;
+  if (dt) *dt = c->h_st->dt;
+  if (n_recompute) *n_recompute = c->h_st->n_recompute;
+  if (c->h_st->nonfinite) return fail(c, ADERDG_ENONFINITE, "the time step became non-finite");
+  return ADERDG_OK;
+}
+
+int aderdg_time_steps(aderdg_ctx* c, double* time, double tend, int steps, int flush_l2, double* step_ms) {
+  if (!c || !time || !step_ms) return fail(c, ADERDG_EINVAL, "null argument");
+  if (!c->uploaded) return fail(c, ADERDG_ESTATE, "upload uh first");
+  if (c->pending) return fail(c, ADERDG_ESTATE, "finish the phase-API step first");
+  int r = set_clock(c, *time, tend);
+  if (!r) r = ensure_graph(c);
+  if (r) return r;
+  if (flush_l2 && !c->flush_buf) {
+    int l2 = 0;
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c->device);
+    c->flush_bytes = (size_t)std::max(l2, 1 << 20) * 2;
+    CK(c, cudaMalloc(&c->flush_buf, c->flush_bytes));
+  }
+  std::vector<cudaEvent_t> ev(2 * (size_t)steps);
+  for (auto& e : ev) CK(c, cudaEventCreate(&e));
+  CK(c, cudaStreamSynchronize(c->stream));
+  for (int s = 0; s < steps; ++s) {
+    if (flush_l2) {
+      const size_t nw = c->flush_bytes / 4;
+      k_flush<<<c->num_sms * 4, 256, 0, c->stream>>>(static_cast<unsigned int*>(c->flush_buf), nw, (unsigned)s);
+      CK(c, cudaGetLastError());
+    }
+    CK(c, cudaEventRecord(ev[2 * s], c->stream));
+    CK(c, cudaGraphLaunch(c->gexec, c->stream));
+    CK(c, cudaEventRecord(ev[2 * s + 1], c->stream));
+  }
+  CK(c, cudaStreamSynchronize(c->stream));
+  for (int s = 0; s < steps; ++s) {
+    float ms = 0.f;
+    CK(c, cudaEventElapsedTime(&ms, ev[2 * s], ev[2 * s + 1]));
+    step_ms[s] = ms;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  r = pull_state(c);
+  if (r) return r;
+  *time = c->h_st->time;
+  if (c->h_st->nonfinite) return fail(c, ADERDG_ENONFINITE, "the time step became non-finite");
+  return ADERDG_OK;
+}
+
+int aderdg_profile_step(aderdg_ctx* c, double* time, double tend, double* phase_ms) {
+  if (!c || !time || !phase_ms) return fail(c, ADERDG_EINVAL, "null argument");
+  if (!c->uploaded) return fail(c, ADERDG_ESTATE, "upload uh first");
+  if (c->pending) return fail(c, ADERDG_ESTATE, "finish the phase-API step first");
+  int r = set_clock(c, *time, tend);
+  if (r) return r;
+  cudaEvent_t ev[8];
+  for (auto& e : ev) CK(c, cudaEventCreate(&e));
+  CK(c, cudaEventRecord(ev[0], c->stream));
+  CK(c, control(c, aderdg::kCtlBegin));
+  CK(c, cudaEventRecord(ev[1], c->stream));
+  CK(c, c->kt->predictor(c->args, pred_ops(c), c->fp32 ? 1 : 0, false, c->stream));
+  CK(c, cudaEventRecord(ev[2], c->stream));
+  CK(c, c->kt->faces(c->args, c->fc, c->fp32 ? 1 : 0, c->stream));
+  CK(c, cudaEventRecord(ev[3], c->stream));
+  r = cells(c, aderdg::kCellFused);
+  if (r) return r;
+  CK(c, cudaEventRecord(ev[4], c->stream));
+  if (c->limiter) CK(c, c->kt->mark(c->args, c->stream));
+  CK(c, cudaEventRecord(ev[5], c->stream));
+  if (c->limiter) CK(c, c->kt->subcell(c->args, c->ops64.data(), c->fc, c->subcell_grid, c->stream));
+  CK(c, cudaEventRecord(ev[6], c->stream));
+  CK(c, control(c, aderdg::kCtlEnd));
+  CK(c, cudaEventRecord(ev[7], c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < 7; ++k) {
+    float ms = 0.f;
+    CK(c, cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+    phase_ms[k] = ms;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  r = pull_state(c);
+  if (r) return r;
+  *time = c->h_st->time;
   return ADERDG_OK;
 }
 

@@ -40,7 +40,10 @@ struct PredCfg {
   static constexpr int CPB_S = SMEM_BUDGET / (CELL_ELEMS * (int)sizeof(R));
   static constexpr int CPB = (CPB_T < CPB_S ? CPB_T : CPB_S) < 1 ? 1 : (CPB_T < CPB_S ? CPB_T : CPB_S);
   static constexpr int THREADS = ((CPB * P2 + 31) / 32) * 32;
-  static constexpr int SMEM_BYTES = CPB * CELL_ELEMS * (int)sizeof(R);
+  // threads past CPB*P2 (the tail of the last warp) take part in the barriers
+  // and get a scratch slot of their own so they never touch a real cell's data
+  static constexpr int SLOTS = CPB + (THREADS > CPB * P2 ? 1 : 0);
+  static constexpr int SMEM_BYTES = SLOTS * CELL_ELEMS * (int)sizeof(R);
 };
 
 // Flux-derivative contraction of time level l into b[v].
@@ -75,7 +78,7 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS)
   const long long cell = (long long)blockIdx.x * CPB + lc;
   const bool in_cta = lc < CPB;
   const bool valid = in_cta && cell < a.ncells;
-  R* cs = sm + (size_t)(in_cta ? lc : 0) * C::CELL_ELEMS;
+  R* cs = sm + (size_t)(lc < CPB ? lc : CPB) * C::CELL_ELEMS;  // lc >= CPB: the scratch slot
 
   int k_inst = valid ? find_inst_cell(a.inst, a.ninst, cell) : 0;
   const InstDesc& in = a.inst[k_inst];

@@ -150,6 +150,24 @@ int aderdg_step(aderdg_ctx* ctx, double* time, double tend, double* dt, int* n_r
  * (<= 0: a default).  *steps_done (nullable) receives the count. */
 int aderdg_run(aderdg_ctx* ctx, double* time, double tend, int max_steps, int sync_every, int* steps_done);
 
+/* The drop-in for one reference step called with host arrays: copies
+ * uh(nVar,P,P,IMAX,JMAX) to the device, recomputes the DMP min/max and the
+ * CFL denominators of that state, runs one fused step and copies uh back. */
+int aderdg_step_host(aderdg_ctx* ctx, double* uh, double* time, double tend, double* dt, int* n_recompute);
+
+/* ---- measurement ---- */
+
+/* Runs `steps` fused steps (graph replays) and returns the device time of
+ * each in step_ms[steps], measured with CUDA events on the context's stream.
+ * With flush_l2, a write over a buffer larger than L2 precedes every step,
+ * outside the timed interval.  *time advances as in aderdg_run. */
+int aderdg_time_steps(aderdg_ctx* ctx, double* time, double tend, int steps, int flush_l2, double* step_ms);
+
+/* Runs one fused step eagerly with CUDA events between its launches and
+ * returns each launch's device time in phase_ms[7]: begin, predictor, faces,
+ * cells (surface + update + DMP), mark, subcell, end. */
+int aderdg_profile_step(aderdg_ctx* ctx, double* time, double tend, double* phase_ms);
+
 /* ---- introspection for parity checks ---- */
 enum aderdg_array {
   ADERDG_A_UH = 0,       /* uh(nVar,P,P,I,J) */
