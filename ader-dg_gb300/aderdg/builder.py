@@ -52,6 +52,7 @@ def _jobs():
                          "exact_%d_%d.o" % (s, n)))
     for src in ("registry.cu", "api.cu", "probe.cu"):
         jobs.append(([nv] + _common_flags() + ["-c", os.path.join(CSRC, src)], src.replace(".cu", ".o")))
+    jobs.append(([nv] + _common_flags() + ["--fmad=false", "-c", os.path.join(CSRC, "noalloc.cu")], "noalloc.o"))
     jobs.append((["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I" + INCLUDE, "-c",
                   os.path.join(CSRC, "setup.cpp")], "setup.o"))
     return jobs

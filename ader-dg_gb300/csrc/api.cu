@@ -204,6 +204,10 @@ int ensure_phase_buffers(aderdg_ctx* c) {
 
 }  // namespace
 
+namespace aderdg {
+void set_last_error(const std::string& msg) { g_err = msg; }
+}  // namespace aderdg
+
 extern "C" {
 
 const char* aderdg_last_error(aderdg_ctx* ctx) { return ctx ? ctx->err.c_str() : g_err.c_str(); }

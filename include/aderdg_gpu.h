@@ -233,6 +233,21 @@ enum aderdg_operator_id {
 };
 int aderdg_operator(int N, int which, double* out);
 
+/* The time step of aderdg_calc_time_step for callers that cannot allocate
+ * device memory (a host framework owns every device allocation, or an
+ * allocation's implicit synchronisation is not allowed).  No counterpart in
+ * the reference: it exists for such embedders.  uh is the caller's device
+ * copy of uh(nVar,N+1,N+1,IMAX,JMAX), dt a caller-owned device double that
+ * receives dt, stream a cudaStream_t (NULL: the legacy default stream).  It
+ * allocates nothing: its scratch is a fixed device array inside the library
+ * (8193 x 8 bytes, held by every GPU that loads the library until exit),
+ * which limits grids to 2,097,152 cells; larger grids return ADERDG_ENOSPACE.
+ * The first call on each device looks up that array's address (make it before
+ * any stream capture).  Calls share the array: calls whose kernels overlap on
+ * the GPU race, so serialise them. */
+int aderdg_calc_time_step_noalloc(const aderdg_config* cfg, const double* uh, double time, double tend, double* dt,
+                                  void* stream);
+
 /* Measured device peaks for roofline reporting: FP64 and FP32 FMA throughput
  * (GFLOP/s) from dependent-FMA microkernels on the current device. */
 int aderdg_probe_peaks(double* fp64_gflops, double* fp32_gflops);
