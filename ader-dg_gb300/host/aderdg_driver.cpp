@@ -7,7 +7,9 @@
 // runs the initial limiter, and advances `do while (time < tend)` calling one
 // C-ABI function per reference phase (--phases) or the fused step (default).
 //
-//   aderdg_driver euler|bn|ad params.ini [--phases] [--N n] [--max-steps k] [--quiet]
+//   aderdg_driver euler|bn|ad params.ini [--phases] [--N n] [--max-steps k] [--quiet] [--dump file]
+//
+// --dump writes the final uh (Fortran layout, raw FP64) and the step count.
 //
 // An optional extension block after the reference fields sets what the
 // reference fixes at compile time or hard-wires (lines `key = value`):
@@ -169,11 +171,13 @@ int main(int argc, char** argv) {
   }
   bool phases = false, quiet = false;
   long max_steps = -1;
+  const char* dump = nullptr;
   for (int a = 3; a < argc; ++a) {
     if (!std::strcmp(argv[a], "--phases")) phases = true;
     else if (!std::strcmp(argv[a], "--quiet")) quiet = true;
     else if (!std::strcmp(argv[a], "--N") && a + 1 < argc) p.cfg.N = std::atoi(argv[++a]);
     else if (!std::strcmp(argv[a], "--max-steps") && a + 1 < argc) max_steps = std::atol(argv[++a]);
+    else if (!std::strcmp(argv[a], "--dump") && a + 1 < argc) dump = argv[++a];
   }
   const aderdg_config& c = p.cfg;
   const int V = c.system == ADERDG_SYS_ADVDIFF ? 1 : c.system == ADERDG_SYS_EULER ? 4 : 9;
@@ -218,6 +222,14 @@ int main(int argc, char** argv) {
   std::printf(" steps = %ld  initially limited = %d  wall time = %.6f s  DOF-updates/s = %.4e\n", steps, nlim, secs,
               (double)V * P * P * cells * steps / (secs > 0 ? secs : 1));
   if ((r = aderdg_download(ctx, uh.data(), nullptr))) return die(ctx, r, "aderdg_download");
+  if (dump) {
+    FILE* f = std::fopen(dump, "wb");
+    if (!f) return std::fprintf(stderr, "cannot write %s\n", dump), 1;
+    std::fwrite(&steps, sizeof(long), 1, f);
+    std::fwrite(&time, sizeof(double), 1, f);
+    std::fwrite(uh.data(), sizeof(double), uh.size(), f);
+    std::fclose(f);
+  }
   aderdg_destroy(ctx);
   return 0;
 }
