@@ -50,7 +50,7 @@ def _jobs():
                          "pred_%d_%d.o" % (s, n)))
             jobs.append(([nv] + _common_flags() + ["--fmad=false"] + d + ["-c", os.path.join(CSRC, "exact_tu.cu")],
                          "exact_%d_%d.o" % (s, n)))
-    for src in ("registry.cu", "api.cu", "probe.cu"):
+    for src in ("registry.cu", "api.cu", "probe.cu", "batch.cu"):
         jobs.append(([nv] + _common_flags() + ["-c", os.path.join(CSRC, src)], src.replace(".cu", ".o")))
     jobs.append(([nv] + _common_flags() + ["--fmad=false", "-c", os.path.join(CSRC, "noalloc.cu")], "noalloc.o"))
     jobs.append((["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I" + INCLUDE, "-c",

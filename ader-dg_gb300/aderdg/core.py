@@ -149,6 +149,16 @@ def load(build_if_missing=False):
         "aderdg_probe_peaks": (i, [dp, dp]), "aderdg_set_array": (i, [vp, i, vp]),
         "aderdg_operator": (i, [i, i, dp]), "aderdg_step_host": (i, [vp, dp, dp, d, dp, ip]),
         "aderdg_time_steps": (i, [vp, dp, d, i, i, dp]), "aderdg_profile_step": (i, [vp, dp, d, dp]),
+        "aderdg_batch_unit_bytes": (ctypes.c_long, [i, i, i, i]),
+        "aderdg_batch_create": (i, [i, i, i, i, ctypes.c_long, i, ctypes.POINTER(vp)]),
+        "aderdg_batch_destroy": (i, [vp]),
+        "aderdg_batch_admit": (i, [vp, cfgp, dp, dp, d, ctypes.c_long, ip]),
+        "aderdg_batch_release": (i, [vp, i]), "aderdg_batch_launch": (i, [vp, i]), "aderdg_batch_sync": (i, [vp, ip]),
+        "aderdg_batch_query": (i, [vp, i, dp, dp, ctypes.POINTER(ctypes.c_long), ip]),
+        "aderdg_batch_download": (i, [vp, i, dp]),
+        "aderdg_batch_info": (i, [vp, ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long),
+                                  ctypes.POINTER(ctypes.c_long), ip]),
+        "aderdg_batch_last_error": (ctypes.c_char_p, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -164,7 +174,10 @@ EXPORTED = ("aderdg_create", "aderdg_destroy", "aderdg_upload", "aderdg_init_lim
             "aderdg_riemann_problem", "aderdg_surface_integral", "aderdg_element_update", "aderdg_limiter",
             "aderdg_step", "aderdg_run", "aderdg_array_size", "aderdg_get_array", "aderdg_get_info",
             "aderdg_last_error", "aderdg_project_initial_condition", "aderdg_probe_peaks", "aderdg_set_array",
-            "aderdg_operator", "aderdg_step_host", "aderdg_time_steps", "aderdg_profile_step")
+            "aderdg_operator", "aderdg_step_host", "aderdg_time_steps", "aderdg_profile_step",
+            "aderdg_batch_unit_bytes", "aderdg_batch_create", "aderdg_batch_destroy", "aderdg_batch_admit",
+            "aderdg_batch_release", "aderdg_batch_launch", "aderdg_batch_sync", "aderdg_batch_query",
+            "aderdg_batch_download", "aderdg_batch_info", "aderdg_batch_last_error")
 
 
 def _dp(a):
@@ -365,3 +378,89 @@ class Solver:
         i = _Info()
         self._ck(self.L.aderdg_get_info(self.h, ctypes.byref(i)))
         return {k: getattr(i, k) for k, _ in _Info._fields_}
+
+
+class Batch:
+    """Many independent simulations of one (system, N, precision, limiter) on
+    the GPU, stepped together; admit and release them between steps."""
+
+    def __init__(self, system, N, precision=FP64, limiter=1, capacity_units=1 << 16, max_instances=256):
+        self.L = load()
+        self.system, self.N, self.precision = system, N, precision
+        self.limiter = 1 if (limiter and system != SYS_ADVDIFF) else 0
+        self.capacity_units = int(capacity_units)
+        h = ctypes.c_void_p()
+        r = self.L.aderdg_batch_create(system, N, precision, self.limiter, self.capacity_units, max_instances,
+                                       ctypes.byref(h))
+        if r:
+            raise AderdgError(r, self.L.aderdg_last_error(None).decode())
+        self.h = h
+        self.cfgs = {}
+
+    @staticmethod
+    def units(cfg):
+        return (cfg.imax + 1) * (cfg.jmax + 1)
+
+    @staticmethod
+    def unit_bytes(system, N, precision=FP64, limiter=1):
+        return int(load().aderdg_batch_unit_bytes(system, N, precision, limiter))
+
+    def _ck(self, r):
+        if r:
+            raise AderdgError(r, self.L.aderdg_batch_last_error(self.h).decode())
+        return r
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.aderdg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def admit(self, cfg, uh, lh_ic=None, tend=1e30, max_steps=0):
+        """Returns the slot id, or None when the batch has no room."""
+        c = cfg.to_c()
+        uh = np.ascontiguousarray(uh, dtype=np.float64).ravel()
+        lh = None if lh_ic is None else np.ascontiguousarray(lh_ic, dtype=np.float64).ravel()
+        slot = ctypes.c_int(-1)
+        r = self.L.aderdg_batch_admit(self.h, ctypes.byref(c), _dp(uh), None if lh is None else _dp(lh), tend,
+                                      int(max_steps), ctypes.byref(slot))
+        if r == -8:
+            return None
+        self._ck(r)
+        self.cfgs[slot.value] = cfg
+        return slot.value
+
+    def release(self, slot):
+        self._ck(self.L.aderdg_batch_release(self.h, slot))
+        self.cfgs.pop(slot, None)
+
+    def launch(self, steps):
+        self._ck(self.L.aderdg_batch_launch(self.h, steps))
+
+    def sync(self):
+        n = ctypes.c_int(0)
+        self._ck(self.L.aderdg_batch_sync(self.h, ctypes.byref(n)))
+        return n.value
+
+    def query(self, slot):
+        t, dt, st, done = ctypes.c_double(0), ctypes.c_double(0), ctypes.c_long(0), ctypes.c_int(0)
+        r = self.L.aderdg_batch_query(self.h, slot, ctypes.byref(t), ctypes.byref(dt), ctypes.byref(st),
+                                      ctypes.byref(done))
+        return dict(time=t.value, dt=dt.value, steps=st.value, done=bool(done.value), status=r)
+
+    def download(self, slot):
+        cfg = self.cfgs[slot]
+        uh = np.empty(cfg.dofs, dtype=np.float64)
+        self._ck(self.L.aderdg_batch_download(self.h, slot, _dp(uh)))
+        return uh
+
+    def info(self):
+        u, c, b = ctypes.c_long(0), ctypes.c_long(0), ctypes.c_long(0)
+        n = ctypes.c_int(0)
+        self._ck(self.L.aderdg_batch_info(self.h, ctypes.byref(u), ctypes.byref(c), ctypes.byref(b), ctypes.byref(n)))
+        return dict(used_units=u.value, capacity_units=c.value, device_bytes=b.value, instances=n.value)

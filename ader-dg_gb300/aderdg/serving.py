@@ -1,0 +1,162 @@
+"""Continuous-batching request server for ADER-DG simulations.
+
+Requests (independent simulations: system, N, grid, initial-field parameters,
+end time) arrive over time.  Each is admitted, as soon as it has arrived and
+its group has room, into the batch of its (system, N) group; a batch steps all
+its simulations with one set of launches, each simulation with its own CFL
+time step, and groups run concurrently on their own CUDA streams.  Finished
+simulations are downloaded and released, freeing room for waiting requests
+while the others keep running on the GPU.  Initial fields are projected on a
+host thread pool so that admission does not stall the loop.
+
+Reported per run: aggregate DOF-updates/s over the makespan and the p50/p99
+time-to-solution (arrival to result on the host) of the requests.
+"""
+import collections
+import concurrent.futures
+import math
+import time
+
+import numpy as np
+
+from .core import FP64, SYS_ADVDIFF, Batch, project_initial_condition
+from . import workloads
+
+
+class Request:
+    __slots__ = ("rid", "name", "N", "side", "params", "tend", "max_steps", "arrival", "cfg", "ic", "prepared",
+                 "admitted", "finished", "steps", "dofs", "group", "slot", "result", "time")
+
+    def __init__(self, rid, spec, arrival, precision, max_steps):
+        self.rid = rid
+        self.name, self.N, self.side = spec["name"], spec["N"], spec["side"]
+        self.params, self.tend = spec["params"], spec["tend"]
+        self.max_steps = max_steps
+        self.arrival = arrival
+        self.cfg, self.ic, _, _ = workloads.make(self.name, side=self.side, N=self.N, precision=precision)
+        self.prepared = None
+        self.admitted = self.finished = None
+        self.steps = 0
+        self.dofs = self.cfg.dofs
+        self.group = (self.cfg.system, self.N)
+        self.slot = None
+        self.result = None
+        self.time = 0.0
+
+
+def poisson_arrivals(n, rate, seed):
+    rng = np.random.default_rng(seed + 1000)
+    return np.cumsum(rng.exponential(1.0 / rate, size=n)) - 0.0
+
+
+class Server:
+    """Admits requests into per-(system, N) batches under an HBM budget."""
+
+    def __init__(self, hbm_budget_bytes, precision=FP64, max_instances=256, sync_every=4, workers=8,
+                 keep_results=False):
+        self.budget = int(hbm_budget_bytes)
+        self.precision = precision
+        self.max_instances = max_instances
+        self.sync_every = sync_every
+        self.keep_results = keep_results
+        self.groups = {}
+        self.pool = concurrent.futures.ThreadPoolExecutor(max_workers=workers)
+
+    def _group(self, req, n_groups, need_units):
+        g = self.groups.get(req.group)
+        if g is None:
+            system, N = req.group
+            lim = 0 if system == SYS_ADVDIFF else 1
+            ub = Batch.unit_bytes(system, N, self.precision, lim)
+            # an equal share of the budget, and never less than the group's largest request
+            units = max(int(self.budget / max(n_groups, 1) / ub), need_units)
+            g = Batch(system, N, self.precision, lim, capacity_units=units, max_instances=self.max_instances)
+            self.groups[req.group] = g
+        return g
+
+    @staticmethod
+    def _prepare(req):
+        uh, lh = project_initial_condition(req.cfg, req.ic, req.params)
+        return uh, (lh if req.cfg.limiter and req.cfg.system != SYS_ADVDIFF else None)
+
+    def run(self, specs, rate=100.0, seed=0, max_steps=0):
+        """Serve `specs` (workloads.request_mix entries) arriving as a Poisson
+        process of `rate` requests/s; each runs to its end time or max_steps."""
+        arrivals = poisson_arrivals(len(specs), rate, seed)
+        reqs = [Request(k, s, float(a), self.precision, max_steps) for k, (s, a) in enumerate(zip(specs, arrivals))]
+        need = collections.defaultdict(int)
+        for r in reqs:
+            need[r.group] = max(need[r.group], Batch.units(r.cfg))
+        for r in reqs:  # all batches exist before the clock starts
+            self._group(r, len(need), need[r.group])
+        pending = collections.deque(reqs)
+        waiting = {g: collections.deque() for g in self.groups}
+        running = {g: {} for g in self.groups}
+        done = []
+        t0 = time.perf_counter()
+        clock = lambda: time.perf_counter() - t0  # noqa: E731
+        futures = {}
+        total_steps_dofs = 0
+        while pending or any(waiting.values()) or any(running.values()):
+            now = clock()
+            while pending and pending[0].arrival <= now:
+                r = pending.popleft()
+                futures[r.rid] = self.pool.submit(self._prepare, r)
+                waiting[r.group].append(r)
+            # admit in arrival order per group while there is room
+            for g, q in waiting.items():
+                b = self.groups[g]
+                while q:
+                    r = q[0]
+                    f = futures[r.rid]
+                    if not f.done():
+                        break
+                    uh, lh = f.result()
+                    slot = b.admit(r.cfg, uh, lh, r.tend, r.max_steps)
+                    if slot is None:
+                        break
+                    q.popleft()
+                    del futures[r.rid]
+                    r.slot, r.admitted = slot, clock()
+                    running[g][slot] = r
+            active = [g for g in self.groups if running[g]]
+            if not active:
+                if pending:
+                    time.sleep(max(0.0, min(pending[0].arrival - clock(), 0.01)))
+                else:
+                    time.sleep(0.0005)
+                continue
+            for g in active:
+                self.groups[g].launch(self.sync_every)
+            for g in active:
+                b = self.groups[g]
+                b.sync()
+                for slot in list(running[g]):
+                    r = running[g][slot]
+                    q = b.query(slot)
+                    if q["done"]:
+                        if self.keep_results:
+                            r.result = b.download(slot)
+                        r.steps, r.time, r.finished = q["steps"], q["time"], clock()
+                        total_steps_dofs += r.steps * r.dofs
+                        b.release(slot)
+                        del running[g][slot]
+                        done.append(r)
+        makespan = clock()
+        tts = np.array([r.finished - r.arrival for r in done])
+        return {
+            "requests": len(done),
+            "dof_updates": int(total_steps_dofs),
+            "makespan_s": makespan,
+            "dof_updates_per_s": total_steps_dofs / makespan if makespan > 0 else math.nan,
+            "tts_p50_s": float(np.percentile(tts, 50)),
+            "tts_p99_s": float(np.percentile(tts, 99)),
+            "groups": len(self.groups),
+            "requests_done": done,
+        }
+
+    def close(self):
+        for b in self.groups.values():
+            b.close()
+        self.groups.clear()
+        self.pool.shutdown(wait=False)

@@ -105,7 +105,7 @@ int validate(const aderdg_config* c, std::string* why) {
 }
 
 cudaError_t control(aderdg_ctx* c, int mode) {
-  aderdg::k_control<<<1, 32, 0, c->stream>>>(c->d_inst, c->d_st, 1, c->args.list_count, mode);
+  aderdg::k_control<<<1, 32, 0, c->stream>>>(c->d_inst, c->d_st, 1, c->args.list_count, mode, -1);
   return cudaGetLastError();
 }
 
@@ -124,7 +124,7 @@ int cur_par(aderdg_ctx* c) { return (int)(c->h_st->steps & 1); }
 
 int cells(aderdg_ctx* c, int mode) {
   c->args.mode = mode;
-  CK(c, c->kt->cells(c->args, c->ops64.data(), c->stream));
+  CK(c, c->kt->cells(c->args, c->ops64.data(), c->fp32 ? 1 : 0, c->stream));
   return ADERDG_OK;
 }
 
@@ -206,6 +206,24 @@ int ensure_phase_buffers(aderdg_ctx* c) {
 
 namespace aderdg {
 void set_last_error(const std::string& msg) { g_err = msg; }
+int validate_config(const aderdg_config* c, std::string* why) { return validate(c, why); }
+FaceConst make_face_const(const HostOps& ops) {
+  const double pi = 4.0 * std::atan(1.0);
+  FaceConst fc{};
+  fc.Va[0] = 8.0;
+  fc.Va[1] = 8.25 * std::cos(pi / 6.0);
+  fc.Va[2] = -8.25 * std::sin(pi / 6.0);
+  fc.Va[3] = 116.5;
+  fc.Vb[0] = 1.4;
+  fc.Vb[1] = 0.0;
+  fc.Vb[2] = 0.0;
+  fc.Vb[3] = 1.0;
+  fc.xsw0 = 1.0 / 6.0 + 1.0 / std::tan(pi / 3.0);  // Euler/riemann_problem.f90:1-8
+  fc.xsw1 = 10.0 / std::sin(pi / 3.0);
+  fc.pi = pi;
+  for (int k = 0; k < ops.P && k < 10; ++k) fc.xi[k] = ops.xi[k];
+  return fc;
+}
 }  // namespace aderdg
 
 extern "C" {
@@ -288,6 +306,8 @@ int aderdg_create(const aderdg_config* cfg, aderdg_ctx** out) {
   a.inst = c->d_inst;
   a.st = c->d_st;
   a.ninst = 1;
+  a.cell0 = 0;
+  a.only_inst = -1;
   a.ncells = c->ncells;
   a.nfx = c->nfx;
   a.nfy = c->nfy;
@@ -317,20 +337,7 @@ int aderdg_create(const aderdg_config* cfg, aderdg_ctx** out) {
   e = cudaMemcpy(c->d_inst, &in, sizeof(InstDesc), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return bail(fail_cuda(nullptr, "cudaMemcpy inst", e));
 
-  const double pi = 4.0 * std::atan(1.0);
-  aderdg::FaceConst& fc = c->fc;
-  fc.Va[0] = 8.0;
-  fc.Va[1] = 8.25 * std::cos(pi / 6.0);
-  fc.Va[2] = -8.25 * std::sin(pi / 6.0);
-  fc.Va[3] = 116.5;
-  fc.Vb[0] = 1.4;
-  fc.Vb[1] = 0.0;
-  fc.Vb[2] = 0.0;
-  fc.Vb[3] = 1.0;
-  fc.xsw0 = 1.0 / 6.0 + 1.0 / std::tan(pi / 3.0);
-  fc.xsw1 = 10.0 / std::sin(pi / 3.0);
-  fc.pi = pi;
-  for (int k = 0; k < P; ++k) fc.xi[k] = c->ops.xi[k];
+  c->fc = aderdg::make_face_const(c->ops);
 
   c->ops64.assign(kt->ops64_size, 0);
   kt->make_ops64(c->ops, c->ops64.data());
@@ -345,7 +352,7 @@ int aderdg_create(const aderdg_config* cfg, aderdg_ctx** out) {
     z.ncells = 0;
     z.nfx = z.nfy = 0;
     if (kt->predictor(z, pred_ops(c), c->fp32 ? 1 : 0, false, c->stream) != cudaSuccess ||
-        kt->cells(z, c->ops64.data(), c->stream) != cudaSuccess)
+        kt->cells(z, c->ops64.data(), 0, c->stream) != cudaSuccess || kt->cells(z, c->ops64.data(), 1, c->stream) != cudaSuccess)
       return bail(fail(nullptr, ADERDG_ECUDA, "kernel attribute setup failed"));
     if (!c->fp32) kt->predictor(z, pred_ops(c), 0, true, c->stream);
   }

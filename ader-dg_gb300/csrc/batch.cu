@@ -1,0 +1,514 @@
+// batch.cu -- many independent simulations of one (system, N, precision,
+// limiter) stepped by the same launches.
+//
+// A batch owns a pool of "units" (one unit = one cell slot in every per-cell
+// array).  A simulation with an IMAX x JMAX grid occupies (IMAX+1)(JMAX+1)
+// consecutive units from a first-fit free list: its cells, x faces and
+// y faces all index from the same base, so one sorted instance table serves
+// every kernel.  Gaps between simulations are skipped by the kernels (no
+// instance owns them).  Each simulation keeps its own time, CFL time step,
+// end time, step budget and limiter state; finished ones stop by themselves
+// and are released by the host, new ones are admitted while others run.
+//
+// Stepping is asynchronous: aderdg_batch_launch enqueues graph replays of one
+// step on the batch's stream and returns; aderdg_batch_sync waits and reads
+// the per-simulation state back.  Batches of different (system, N) thus run
+// concurrently on their own streams.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/aderdg_gpu.h"
+#include "control.cuh"
+#include "tables.h"
+
+namespace aderdg {
+void set_last_error(const std::string& msg);
+int validate_config(const aderdg_config* c, std::string* why);
+FaceConst make_face_const(const HostOps& ops);
+}  // namespace aderdg
+
+using aderdg::BatchArgs;
+using aderdg::InstDesc;
+using aderdg::InstState;
+
+struct aderdg_batch {
+  int system = 0, N = 0, precision = 0, limiter = 0, V = 0, P = 0, S = 0;
+  long long capacity = 0;  // units
+  int max_inst = 0, n_used = 0;
+  const aderdg::KernelTable* kt = nullptr;
+  aderdg::HostOps ops;
+  std::vector<unsigned char> ops64, ops32;
+  aderdg::FaceConst fc{};
+  cudaStream_t stream = nullptr;
+  int num_sms = 0, subcell_grid = 0;
+  InstDesc* d_inst = nullptr;
+  InstState* d_st = nullptr;
+  InstState* h_st = nullptr;          // pinned, max_inst entries (table order)
+  std::vector<InstDesc> h_inst;       // table order: used entries sorted by base, then unused
+  std::vector<int> slot_at;           // table position -> slot id
+  std::vector<int> pos_of;            // slot id -> table position (-1: free)
+  std::vector<std::pair<long long, long long>> free_ranges;  // (base, size), sorted
+  long long hw = 0;                   // end of the highest occupied unit
+  BatchArgs args{};
+  std::vector<void*> allocs;
+  size_t bytes = 0;
+  cudaGraphExec_t gexec = nullptr;
+  long long graph_hw = -1;
+  std::string err;
+};
+
+namespace {
+
+constexpr long long kUnusedBase = (1ll << 62);
+
+int bfail(aderdg_batch* b, int code, const std::string& msg) {
+  if (b) b->err = msg;
+  aderdg::set_last_error(msg);
+  return code;
+}
+int bcuda(aderdg_batch* b, const char* what, cudaError_t e) {
+  return bfail(b, ADERDG_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define BK(b, call)                                          \
+  do {                                                       \
+    cudaError_t e_ = (call);                                 \
+    if (e_ != cudaSuccess) return bcuda((b), #call, e_);     \
+  } while (0)
+
+int nvar(int sys) { return sys == ADERDG_SYS_ADVDIFF ? 1 : sys == ADERDG_SYS_EULER ? 4 : 9; }
+
+// bytes per unit of every per-cell array of a batch
+long long unit_bytes(int system, int N, int precision, int limiter) {
+  const long long V = nvar(system), P = N + 1, S = 2 * N + 1;
+  const long long rb = precision == ADERDG_FP32_MIXED ? 4 : 8;
+  long long b = 8 * V * P * P * 3;                                   // uh[2], duh
+  b += rb * P * 4 * V * (system == ADERDG_SYS_ADVDIFF ? 3 : 2);     // qbnd, fbnd / gradQbnd
+  b += 8 * P * V * (system == ADERDG_SYS_BN ? 4 : 2);               // face fluxes
+  if (limiter && system != ADERDG_SYS_ADVDIFF)
+    b += 8 * V * S * S * 2 + 4 * 2 + 8 * 2 * V * 3 + 1 + 4 + 4 + 8;  // Lh[2], status[2], mm[2], lminmax, flags, list, denom
+  return b;
+}
+
+template <class T>
+int balloc(aderdg_batch* b, T** p, size_t n) {
+  *p = nullptr;
+  if (n == 0) return ADERDG_OK;
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, n * sizeof(T));
+  if (e != cudaSuccess) return bfail(b, ADERDG_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  e = cudaMemset(q, 0, n * sizeof(T));
+  if (e != cudaSuccess) return bcuda(b, "cudaMemset", e);
+  b->allocs.push_back(q);
+  b->bytes += n * sizeof(T);
+  *p = static_cast<T*>(q);
+  return ADERDG_OK;
+}
+
+void bfree_all(aderdg_batch* b) {
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  for (void* p : b->allocs) cudaFree(p);
+  b->allocs.clear();
+  if (b->h_st) cudaFreeHost(b->h_st);
+  if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+cudaError_t bcontrol(aderdg_batch* b, int mode, int only) {
+  const int threads = 128, blocks = (b->max_inst + threads - 1) / threads;
+  aderdg::k_control<<<blocks, threads, 0, b->stream>>>(b->d_inst, b->d_st, b->max_inst, b->args.list_count, mode, only);
+  return cudaGetLastError();
+}
+
+int push_table(aderdg_batch* b) {
+  BK(b, cudaMemcpyAsync(b->d_inst, b->h_inst.data(), sizeof(InstDesc) * b->max_inst, cudaMemcpyHostToDevice, b->stream));
+  BK(b, cudaMemcpyAsync(b->d_st, b->h_st, sizeof(InstState) * b->max_inst, cudaMemcpyHostToDevice, b->stream));
+  BK(b, cudaStreamSynchronize(b->stream));
+  return ADERDG_OK;
+}
+int pull_states(aderdg_batch* b) {
+  BK(b, cudaMemcpyAsync(b->h_st, b->d_st, sizeof(InstState) * b->max_inst, cudaMemcpyDeviceToHost, b->stream));
+  BK(b, cudaStreamSynchronize(b->stream));
+  return ADERDG_OK;
+}
+
+const void* bpred_ops(aderdg_batch* b) { return b->precision ? b->ops32.data() : b->ops64.data(); }
+
+int blaunch_step(aderdg_batch* b) {
+  BatchArgs a = b->args;
+  a.ncells = b->hw;
+  a.nfx = b->hw;
+  a.nfy = b->hw;
+  a.mode = aderdg::kCellFused;
+  const int fp32 = b->precision ? 1 : 0;
+  BK(b, bcontrol(b, aderdg::kCtlBegin, -1));
+  BK(b, b->kt->predictor(a, bpred_ops(b), fp32, false, b->stream));
+  BK(b, b->kt->faces(a, b->fc, fp32, b->stream));
+  BK(b, b->kt->cells(a, b->ops64.data(), fp32, b->stream));
+  if (b->limiter) {
+    BK(b, b->kt->mark(a, b->stream));
+    BK(b, b->kt->subcell(a, b->ops64.data(), b->fc, b->subcell_grid, b->stream));
+  }
+  BK(b, bcontrol(b, aderdg::kCtlEnd, -1));
+  return ADERDG_OK;
+}
+
+int bensure_graph(aderdg_batch* b) {
+  if (b->gexec && b->graph_hw == b->hw) return ADERDG_OK;
+  if (b->gexec) {
+    cudaGraphExecDestroy(b->gexec);
+    b->gexec = nullptr;
+  }
+  cudaGraph_t g = nullptr;
+  BK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  int r = blaunch_step(b);
+  cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+  if (r) {
+    if (g) cudaGraphDestroy(g);
+    return r;
+  }
+  if (e != cudaSuccess) return bcuda(b, "cudaStreamEndCapture", e);
+  e = cudaGraphInstantiate(&b->gexec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return bcuda(b, "cudaGraphInstantiate", e);
+  b->graph_hw = b->hw;
+  return ADERDG_OK;
+}
+
+// K3 over one instance's cells only (priming modes)
+int bcells_one(aderdg_batch* b, int pos, int mode, const double* lh_ic) {
+  const InstDesc& in = b->h_inst[pos];
+  BatchArgs a = b->args;
+  a.mode = mode;
+  a.cell0 = in.cell_base;
+  a.ncells = in.cell_base + (long long)in.imax * in.jmax;
+  a.only_inst = pos;
+  a.lh_ic = lh_ic;
+  BK(b, b->kt->cells(a, b->ops64.data(), b->precision ? 1 : 0, b->stream));
+  return ADERDG_OK;
+}
+
+int bprime_one(aderdg_batch* b, int pos) {
+  BK(b, bcontrol(b, aderdg::kCtlPrimeReset, pos));
+  int r = bcells_one(b, pos, aderdg::kCellPrime, nullptr);
+  if (r) return r;
+  BK(b, bcontrol(b, aderdg::kCtlPrimeCommit, pos));
+  return ADERDG_OK;
+}
+
+void recompute_hw(aderdg_batch* b) {
+  b->hw = 0;
+  for (int p = 0; p < b->n_used; ++p) {
+    const InstDesc& d = b->h_inst[p];
+    b->hw = std::max(b->hw, d.cell_base + (long long)(d.imax + 1) * (d.jmax + 1));
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+long aderdg_batch_unit_bytes(int system, int N, int precision, int limiter) {
+  if (system < 0 || system > 2 || N < 1 || N > 5) return ADERDG_EINVAL;
+  return (long)unit_bytes(system, N, precision, limiter);
+}
+
+int aderdg_batch_create(int system, int N, int precision, int limiter, long capacity_units, int max_instances,
+                        aderdg_batch** out) {
+  if (!out) return bfail(nullptr, ADERDG_EINVAL, "null output pointer");
+  *out = nullptr;
+  if (system < 0 || system > 2 || N < 1 || N > 5 || capacity_units < 4 || max_instances < 1 ||
+      (precision != ADERDG_FP64 && precision != ADERDG_FP32_MIXED))
+    return bfail(nullptr, ADERDG_EINVAL, "bad batch parameters");
+  const aderdg::KernelTable* kt = aderdg::kernel_table(system, N);
+  if (!kt) return bfail(nullptr, ADERDG_EUNSUPPORTED, "no kernels built for this (system, N)");
+  aderdg_batch* b = new aderdg_batch();
+  b->system = system;
+  b->N = N;
+  b->precision = precision;
+  b->limiter = (limiter != 0 && system != ADERDG_SYS_ADVDIFF) ? 1 : 0;
+  b->V = nvar(system);
+  b->P = N + 1;
+  b->S = 2 * N + 1;
+  b->capacity = capacity_units;
+  b->max_inst = max_instances;
+  b->kt = kt;
+  std::string why;
+  auto bail = [&](int code) {
+    bfree_all(b);
+    delete b;
+    return code;
+  };
+  if (!aderdg::build_ops(N, b->ops, &why)) return bail(bfail(nullptr, ADERDG_EINVAL, why));
+  b->fc = aderdg::make_face_const(b->ops);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMallocHost(&b->h_st, sizeof(InstState) * max_instances);
+  if (e != cudaSuccess) return bail(bcuda(nullptr, "batch set-up", e));
+  std::memset(b->h_st, 0, sizeof(InstState) * max_instances);
+  const size_t U = (size_t)capacity_units, V = b->V, P = b->P, S = b->S;
+  const size_t rb = precision ? 4 : 8;
+  BatchArgs& a = b->args;
+  std::memset(&a, 0, sizeof(a));
+  int r = balloc(b, &b->d_inst, (size_t)max_instances);
+  if (!r) r = balloc(b, &b->d_st, (size_t)max_instances);
+  if (!r) r = balloc(b, &a.uh[0], U * P * P * V);
+  if (!r) r = balloc(b, &a.uh[1], U * P * P * V);
+  if (!r) r = balloc(b, &a.duh, U * P * P * V);
+  unsigned char *qb = nullptr, *fb = nullptr;
+  if (!r) r = balloc(b, &qb, U * P * 4 * V * rb);
+  if (!r) r = balloc(b, &fb, U * P * 4 * V * rb * (system == ADERDG_SYS_ADVDIFF ? 2 : 1));
+  a.qbnd = qb;
+  a.fbnd = fb;
+  if (!r) r = balloc(b, &a.fu, U * P * V);
+  if (!r) r = balloc(b, &a.gu, U * P * V);
+  if (!r && system == ADERDG_SYS_BN) r = balloc(b, &a.fp, U * P * V);
+  if (!r && system == ADERDG_SYS_BN) r = balloc(b, &a.gp, U * P * V);
+  if (!r) r = balloc(b, &a.list_count, 1);
+  if (b->limiter) {
+    if (!r) r = balloc(b, &a.status[0], U);
+    if (!r) r = balloc(b, &a.status[1], U);
+    if (!r) r = balloc(b, &a.lh[0], U * S * S * V);
+    if (!r) r = balloc(b, &a.lh[1], U * S * S * V);
+    if (!r) r = balloc(b, &a.mm[0], U * 2 * V);
+    if (!r) r = balloc(b, &a.mm[1], U * 2 * V);
+    if (!r) r = balloc(b, &a.lminmax, U * 2 * V);
+    if (!r) r = balloc(b, &a.troubled, U);
+    if (!r) r = balloc(b, &a.recompute, U);
+    if (!r) r = balloc(b, &a.list, U);
+    if (!r) r = balloc(b, &a.denom, U);
+  }
+  if (r) return bail(r);
+  a.inst = b->d_inst;
+  a.st = b->d_st;
+  a.ninst = max_instances;
+  a.only_inst = -1;
+  b->h_inst.assign(max_instances, InstDesc{});
+  for (auto& d : b->h_inst) {
+    d.imax = d.jmax = 1;
+    d.cell_base = d.fx_base = d.fy_base = kUnusedBase;
+  }
+  b->slot_at.assign(max_instances, -1);
+  b->pos_of.assign(max_instances, -1);
+  b->free_ranges.push_back({0, capacity_units});
+  b->ops64.assign(kt->ops64_size, 0);
+  kt->make_ops64(b->ops, b->ops64.data());
+  if (precision) {
+    b->ops32.assign(kt->ops32_size, 0);
+    kt->make_ops32(b->ops, b->ops32.data());
+  }
+  if (b->limiter) b->subcell_grid = kt->subcell_grid(b->num_sms);
+  {  // kernel attributes before any capture
+    BatchArgs z = a;
+    z.ncells = z.nfx = z.nfy = 0;
+    kt->predictor(z, bpred_ops(b), precision ? 1 : 0, false, b->stream);
+    kt->cells(z, b->ops64.data(), precision ? 1 : 0, b->stream);
+  }
+  r = push_table(b);
+  if (r) return bail(r);
+  *out = b;
+  return ADERDG_OK;
+}
+
+int aderdg_batch_destroy(aderdg_batch* b) {
+  if (!b) return ADERDG_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  bfree_all(b);
+  delete b;
+  return ADERDG_OK;
+}
+
+int aderdg_batch_admit(aderdg_batch* b, const aderdg_config* cfg, const double* uh, const double* lh_ic, double tend,
+                       long max_steps, int* slot) {
+  if (!b || !cfg || !uh || !slot) return bfail(b, ADERDG_EINVAL, "null argument");
+  std::string why;
+  int r = aderdg::validate_config(cfg, &why);
+  if (r) return bfail(b, r, why);
+  const int lim = (cfg->limiter != 0 && cfg->system != ADERDG_SYS_ADVDIFF) ? 1 : 0;
+  if (cfg->system != b->system || cfg->N != b->N || cfg->precision != b->precision || lim != b->limiter)
+    return bfail(b, ADERDG_EINVAL, "simulation does not match the batch's (system, N, precision, limiter)");
+  if (b->n_used >= b->max_inst) return bfail(b, ADERDG_ENOSPACE, "batch instance table full");
+  const long long need = (long long)(cfg->imax + 1) * (cfg->jmax + 1);
+  long long base = -1;
+  for (auto it = b->free_ranges.begin(); it != b->free_ranges.end(); ++it)
+    if (it->second >= need) {
+      base = it->first;
+      it->first += need;
+      it->second -= need;
+      if (it->second == 0) b->free_ranges.erase(it);
+      break;
+    }
+  if (base < 0) return bfail(b, ADERDG_ENOSPACE, "no free range of " + std::to_string(need) + " units");
+  r = pull_states(b);
+  if (r) return r;
+  // insert into the table, keeping it sorted by base
+  int pos = 0;
+  while (pos < b->n_used && b->h_inst[pos].cell_base < base) ++pos;
+  for (int p = b->n_used; p > pos; --p) {
+    b->h_inst[p] = b->h_inst[p - 1];
+    b->h_st[p] = b->h_st[p - 1];
+    b->slot_at[p] = b->slot_at[p - 1];
+    b->pos_of[b->slot_at[p]] = p;
+  }
+  int s = 0;
+  while (b->pos_of[s] >= 0) ++s;
+  b->slot_at[pos] = s;
+  b->pos_of[s] = pos;
+  ++b->n_used;
+  InstDesc& in = b->h_inst[pos];
+  in = InstDesc{};
+  in.imax = cfg->imax;
+  in.jmax = cfg->jmax;
+  in.cell_base = in.fx_base = in.fy_base = base;
+  in.dx = (cfg->xr[0] - cfg->xl[0]) / cfg->imax;
+  in.dy = (cfg->xr[1] - cfg->xl[1]) / cfg->jmax;
+  in.xl0 = cfg->xl[0];
+  in.xl1 = cfg->xl[1];
+  for (int k = 0; k < 4; ++k) in.bc[k] = cfg->bc[k];
+  in.bc_mode = cfg->bc_mode;
+  in.cfl_pnpm = cfg->cfl * aderdg::pnpm_cfl(cfg->N);
+  in.ph.gamma = cfg->gamma;
+  in.ph.gs = cfg->gamma_s;
+  in.ph.gg = cfg->gamma_g;
+  in.ph.ps = cfg->pi_s;
+  in.ph.pg = cfg->pi_g;
+  in.ph.cx = cfg->cx;
+  in.ph.cy = cfg->cy;
+  in.ph.a = cfg->a;
+  in.ph.ad_fused = cfg->ad_flux_mode;
+  InstState& st = b->h_st[pos];
+  std::memset(&st, 0, sizeof(st));
+  st.time = 0.0;
+  st.tend = tend;
+  st.max_steps = max_steps;
+  recompute_hw(b);
+  r = push_table(b);
+  if (r) return r;
+  // state of the new simulation (parity 0)
+  const size_t cells = (size_t)cfg->imax * cfg->jmax, P2V = (size_t)b->P * b->P * b->V, S2V = (size_t)b->S * b->S * b->V;
+  BK(b, cudaMemcpyAsync(b->args.uh[0] + (size_t)base * P2V, uh, cells * P2V * sizeof(double), cudaMemcpyHostToDevice,
+                        b->stream));
+  if (b->limiter) {
+    BK(b, cudaMemsetAsync(b->args.status[0] + base, 0, cells * sizeof(int), b->stream));
+    BK(b, cudaMemsetAsync(b->args.status[1] + base, 0, cells * sizeof(int), b->stream));
+  }
+  r = bprime_one(b, pos);
+  if (r) return r;
+  if (b->limiter && lh_ic) {
+    // stage the subcell candidates in the next-parity Lh slab of this simulation
+    BK(b, cudaMemcpyAsync(b->args.lh[1] + (size_t)base * S2V, lh_ic, cells * S2V * sizeof(double),
+                          cudaMemcpyHostToDevice, b->stream));
+    BK(b, bcontrol(b, aderdg::kCtlPrimeReset, pos));
+    r = bcells_one(b, pos, aderdg::kCellInitDmp, b->args.lh[1]);
+    if (r) return r;
+    r = bprime_one(b, pos);
+    if (r) return r;
+  }
+  r = pull_states(b);
+  if (r) return r;
+  *slot = s;
+  return ADERDG_OK;
+}
+
+int aderdg_batch_release(aderdg_batch* b, int slot) {
+  if (!b || slot < 0 || slot >= b->max_inst || b->pos_of[slot] < 0) return bfail(b, ADERDG_EINVAL, "bad slot");
+  int r = pull_states(b);
+  if (r) return r;
+  const int pos = b->pos_of[slot];
+  const InstDesc in = b->h_inst[pos];
+  const long long size = (long long)(in.imax + 1) * (in.jmax + 1);
+  for (int p = pos; p < b->n_used - 1; ++p) {
+    b->h_inst[p] = b->h_inst[p + 1];
+    b->h_st[p] = b->h_st[p + 1];
+    b->slot_at[p] = b->slot_at[p + 1];
+    b->pos_of[b->slot_at[p]] = p;
+  }
+  --b->n_used;
+  InstDesc& d = b->h_inst[b->n_used];
+  d = InstDesc{};
+  d.imax = d.jmax = 1;
+  d.cell_base = d.fx_base = d.fy_base = kUnusedBase;
+  std::memset(&b->h_st[b->n_used], 0, sizeof(InstState));
+  b->slot_at[b->n_used] = -1;
+  b->pos_of[slot] = -1;
+  // return the range to the free list, merging neighbours
+  auto& fr = b->free_ranges;
+  fr.push_back({in.cell_base, size});
+  std::sort(fr.begin(), fr.end());
+  std::vector<std::pair<long long, long long>> merged;
+  for (auto& x : fr) {
+    if (!merged.empty() && merged.back().first + merged.back().second == x.first) merged.back().second += x.second;
+    else merged.push_back(x);
+  }
+  fr.swap(merged);
+  recompute_hw(b);
+  return push_table(b);
+}
+
+int aderdg_batch_launch(aderdg_batch* b, int steps) {
+  if (!b) return bfail(b, ADERDG_EINVAL, "null batch");
+  if (steps <= 0 || b->n_used == 0) return ADERDG_OK;
+  int r = bensure_graph(b);
+  if (r) return r;
+  for (int s = 0; s < steps; ++s) BK(b, cudaGraphLaunch(b->gexec, b->stream));
+  return ADERDG_OK;
+}
+
+int aderdg_batch_sync(aderdg_batch* b, int* n_running) {
+  if (!b) return bfail(b, ADERDG_EINVAL, "null batch");
+  int r = pull_states(b);
+  if (r) return r;
+  int n = 0;
+  for (int p = 0; p < b->n_used; ++p) {
+    const InstState& s = b->h_st[p];
+    const bool done = !(s.time < s.tend) || s.nonfinite || (s.max_steps > 0 && s.steps >= s.max_steps);
+    n += done ? 0 : 1;
+  }
+  if (n_running) *n_running = n;
+  return ADERDG_OK;
+}
+
+int aderdg_batch_query(aderdg_batch* b, int slot, double* time, double* dt, long* steps, int* done) {
+  if (!b || slot < 0 || slot >= b->max_inst || b->pos_of[slot] < 0) return bfail(b, ADERDG_EINVAL, "bad slot");
+  const InstState& s = b->h_st[b->pos_of[slot]];
+  if (time) *time = s.time;
+  if (dt) *dt = s.dt;
+  if (steps) *steps = (long)s.steps;
+  if (done) *done = (!(s.time < s.tend) || s.nonfinite || (s.max_steps > 0 && s.steps >= s.max_steps)) ? 1 : 0;
+  if (s.nonfinite) return bfail(b, ADERDG_ENONFINITE, "the time step became non-finite");
+  return ADERDG_OK;
+}
+
+int aderdg_batch_download(aderdg_batch* b, int slot, double* uh) {
+  if (!b || !uh || slot < 0 || slot >= b->max_inst || b->pos_of[slot] < 0) return bfail(b, ADERDG_EINVAL, "bad slot");
+  int r = pull_states(b);
+  if (r) return r;
+  const int pos = b->pos_of[slot];
+  const InstDesc& in = b->h_inst[pos];
+  const int par = (int)(b->h_st[pos].steps & 1);
+  const size_t cells = (size_t)in.imax * in.jmax, P2V = (size_t)b->P * b->P * b->V;
+  BK(b, cudaMemcpyAsync(uh, b->args.uh[par] + (size_t)in.cell_base * P2V, cells * P2V * sizeof(double),
+                        cudaMemcpyDeviceToHost, b->stream));
+  BK(b, cudaStreamSynchronize(b->stream));
+  return ADERDG_OK;
+}
+
+int aderdg_batch_info(aderdg_batch* b, long* used_units, long* capacity_units, long* device_bytes, int* n_instances) {
+  if (!b) return bfail(b, ADERDG_EINVAL, "null batch");
+  long long used = 0;
+  for (int p = 0; p < b->n_used; ++p) used += (long long)(b->h_inst[p].imax + 1) * (b->h_inst[p].jmax + 1);
+  if (used_units) *used_units = (long)used;
+  if (capacity_units) *capacity_units = (long)b->capacity;
+  if (device_bytes) *device_bytes = (long)b->bytes;
+  if (n_instances) *n_instances = b->n_used;
+  return ADERDG_OK;
+}
+
+const char* aderdg_batch_last_error(aderdg_batch* b) { return b ? b->err.c_str() : ""; }
+
+}  // extern "C"

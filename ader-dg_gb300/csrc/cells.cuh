@@ -25,6 +25,17 @@ namespace aderdg {
 
 #define kInf __longlong_as_double(0x7ff0000000000000LL)
 
+// Doubles mapped to integers of the same order (negative values have their
+// magnitude bits flipped), so min/max run on the integer pipe instead of the
+// FP64 pipe; the value returned is one of the inputs, as with fmin/fmax.
+__device__ __forceinline__ long long okey(double x) {
+  const long long b = __double_as_longlong(x);
+  return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ double okey_inv(long long k) {
+  return __longlong_as_double(k >= 0 ? k : (k ^ 0x7fffffffffffffffLL));
+}
+
 // Subcell / Gauss-Lobatto projections of one cell (get_subcell_data and
 // get_lobatto_data, Euler/limiter.f90:12-68), sum-factorised y then x with
 // the reference's summation order.  A "team" of nr threads with rank r works
@@ -32,7 +43,14 @@ namespace aderdg {
 template <int N, int V>
 struct Proj {
   static constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1;
+  // acc + a*b: exact-order mul then add, or one fused multiply-add (kFast)
+  template <bool kFast>
+  __device__ __forceinline__ static double madd(double acc, double a, double b) {
+    if constexpr (kFast) return fma(a, b, acc);
+    else return acc + a * b;
+  }
   // y pass: LY[v][s][i] = sum_k U[v][i + P k] uh2lim(s,k); LB[v][s][i] likewise with uh2lob
+  template <bool kFast = false>
   __device__ static void ypass(const double* U, double* LY, double* LB, const DevOps<N, double>& op, int r, int nr) {
     for (int idx = r; idx < P * S; idx += nr) {
       const int ii = idx % P, s = idx / P;
@@ -40,7 +58,7 @@ struct Proj {
       for (int v = 0; v < V; ++v) {
         double acc = 0.0;
 #pragma unroll
-        for (int k = 0; k < P; ++k) acc = acc + U[v * P2 + ii + P * k] * op.uh2lim[s + S * k];
+        for (int k = 0; k < P; ++k) acc = madd<kFast>(acc, U[v * P2 + ii + P * k], op.uh2lim[s + S * k]);
         LY[(v * S + s) * P + ii] = acc;
       }
     }
@@ -50,52 +68,63 @@ struct Proj {
       for (int v = 0; v < V; ++v) {
         double acc = 0.0;
 #pragma unroll
-        for (int k = 0; k < P; ++k) acc = acc + U[v * P2 + ii + P * k] * op.uh2lob[s + P * k];
+        for (int k = 0; k < P; ++k) acc = madd<kFast>(acc, U[v * P2 + ii + P * k], op.uh2lob[s + P * k]);
         LB[(v * P + s) * P + ii] = acc;
       }
     }
   }
   // subcell value (s1, s2) from the y pass
+  template <bool kFast = false>
   __device__ static void subcell(const double* LY, const DevOps<N, double>& op, int s1, int s2, double* out) {
 #pragma unroll
     for (int v = 0; v < V; ++v) {
       double acc = 0.0;
 #pragma unroll
-      for (int k = 0; k < P; ++k) acc = acc + LY[(v * S + s2) * P + k] * op.uh2lim[s1 + S * k];
+      for (int k = 0; k < P; ++k) acc = madd<kFast>(acc, LY[(v * S + s2) * P + k], op.uh2lim[s1 + S * k]);
       out[v] = acc;
     }
   }
+  template <bool kFast = false>
   __device__ static void lobatto(const double* LB, const DevOps<N, double>& op, int s1, int s2, double* out) {
 #pragma unroll
     for (int v = 0; v < V; ++v) {
       double acc = 0.0;
 #pragma unroll
-      for (int k = 0; k < P; ++k) acc = acc + LB[(v * P + s2) * P + k] * op.uh2lob[s1 + P * k];
+      for (int k = 0; k < P; ++k) acc = madd<kFast>(acc, LB[(v * P + s2) * P + k], op.uh2lob[s1 + P * k]);
       out[v] = acc;
     }
   }
-  // x pass fused with min/max and the positivity test of every subcell
-  template <class Sys>
+  // x pass fused with min/max (integer keys) and the positivity test of every subcell
+  template <class Sys, bool kFast = false>
   __device__ static void xpass_minmax(const double* U, const double* LY, const double* LB, const DevOps<N, double>& op,
                                       const Phys& ph, int r, int nr, double* mn, double* mx, bool& posfail) {
     double val[V];
-    for (int idx = r; idx < S * S; idx += nr) {
-      subcell(LY, op, idx % S, idx / S, val);
+    long long kmn[V], kmx[V];
 #pragma unroll
-      for (int v = 0; v < V; ++v) { mn[v] = fmin(mn[v], val[v]); mx[v] = fmax(mx[v], val[v]); }
+    for (int v = 0; v < V; ++v) { kmn[v] = okey(mn[v]); kmx[v] = okey(mx[v]); }
+    for (int idx = r; idx < S * S; idx += nr) {
+      subcell<kFast>(LY, op, idx % S, idx / S, val);
+#pragma unroll
+      for (int v = 0; v < V; ++v) { const long long k = okey(val[v]); kmn[v] = min(kmn[v], k); kmx[v] = max(kmx[v], k); }
       if constexpr (Sys::ID != kSysAD) {
-        if (!Sys::positive(ph, val)) posfail = true;
+        if (!Sys::positive_fast(ph, val)) posfail = true;
       }
     }
     for (int idx = r; idx < P * P; idx += nr) {
-      lobatto(LB, op, idx % P, idx / P, val);
+      lobatto<kFast>(LB, op, idx % P, idx / P, val);
 #pragma unroll
-      for (int v = 0; v < V; ++v) { mn[v] = fmin(mn[v], val[v]); mx[v] = fmax(mx[v], val[v]); }
+      for (int v = 0; v < V; ++v) { const long long k = okey(val[v]); kmn[v] = min(kmn[v], k); kmx[v] = max(kmx[v], k); }
     }
     for (int idx = r; idx < P2; idx += nr) {
 #pragma unroll
-      for (int v = 0; v < V; ++v) { mn[v] = fmin(mn[v], U[v * P2 + idx]); mx[v] = fmax(mx[v], U[v * P2 + idx]); }
+      for (int v = 0; v < V; ++v) {
+        const long long k = okey(U[v * P2 + idx]);
+        kmn[v] = min(kmn[v], k);
+        kmx[v] = max(kmx[v], k);
+      }
     }
+#pragma unroll
+    for (int v = 0; v < V; ++v) { mn[v] = okey_inv(kmn[v]); mx[v] = okey_inv(kmx[v]); }
   }
 };
 
@@ -108,8 +137,9 @@ __device__ __forceinline__ int nb_index(int x, int d, int n, int bc_lo, int bc_h
   return y;
 }
 
-// CFL denominator at one node (calc_time_step.f90: Euler/BN :31-45, AD :37-50)
-template <class Sys, int N>
+// CFL denominator at one node (calc_time_step.f90: Euler/BN :31-45, AD :37-50);
+// kFast: eigenvalues in FP32 (the FP32-mixed mode), sums and reduction in FP64
+template <class Sys, int N, bool kFast = false>
 __device__ __forceinline__ double cfl_denom(const InstDesc& in, const double* Q) {
   if constexpr (Sys::ID == kSysAD) {
     const double factor = (double)(2 * N + 1);
@@ -119,9 +149,12 @@ __device__ __forceinline__ double cfl_denom(const InstDesc& in, const double* Q)
     denom = denom + (ADSys::max_eig_c(in.ph, 1) + 2.0 * smax_v * factor / in.dy) / in.dy;
     return denom;
   } else {
+    double ex, ey;
+    if constexpr (kFast) Sys::max_eig2_f32(in.ph, Q, ex, ey);
+    else Sys::max_eig2(in.ph, Q, ex, ey);
     double denom = 0.0;
-    denom = denom + Sys::max_eig(in.ph, Q, 0) / in.dx;
-    denom = denom + Sys::max_eig(in.ph, Q, 1) / in.dy;
+    denom = denom + ex / in.dx;
+    denom = denom + ey / in.dy;
     return denom;
   }
 }
@@ -136,7 +169,7 @@ struct CellCfg {
   static constexpr int SMEM_BYTES = CPB * CELL_DBL * 8 + CPB * 8 /*cell max*/ + CPB * 4 /*flags*/ + 16;
 };
 
-template <class Sys, int N>
+template <class Sys, int N, bool kFast>
 __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a, DevOps<N, double> op) {
   using C = CellCfg<Sys, N>;
   constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1, V = Sys::V, CPB = C::CPB;
@@ -150,13 +183,16 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
   const int lc = t / P2;
   const int node = t - lc * P2;
   const int i = node % P, j = node / P;
-  const long long cell = (long long)blockIdx.x * CPB + lc;
+  const long long cell = a.cell0 + (long long)blockIdx.x * CPB + lc;
   const bool in_cta = lc < CPB;
-  const bool valid = in_cta && cell < a.ncells;
-  const int kc = valid ? find_inst_cell(a.inst, a.ninst, cell) : 0;
+  const int k_found = (in_cta && cell < a.ncells) ? find_inst_cell(a.inst, a.ninst, cell) : -1;
+  const bool valid = k_found >= 0;
+  const int kc = valid ? k_found : 0;
   const InstDesc& in = a.inst[kc];
   const InstState& st = a.st[kc];
-  const bool act = valid && (st.active || mode == kCellPrime || mode == kCellInitDmp || mode == kCellCfl);
+  const bool priming = mode == kCellPrime || mode == kCellInitDmp || mode == kCellCfl;
+  const bool act = valid && (priming ? (a.only_inst < 0 || kc == a.only_inst) : st.active != 0);
+  if (!__syncthreads_or(act)) return;  // nothing to do in this CTA
   const int par = parity(st);
   const long long lcell = cell - in.cell_base;
   const int ci = valid ? (int)(lcell % in.imax) : 0, cj = valid ? (int)(lcell / in.imax) : 0;
@@ -191,15 +227,28 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
         const double* YB = a.gu;
         const double* YT = (Sys::ID == kSysBN) ? a.gp : a.gu;
         const double cx = op.wd[j] / in.dx, cy = op.wd[i] / in.dy;
+        if constexpr (kFast) {
+          // FP32-mixed: the surface contraction in FP32, added to the FP64 update
+          const float cxf = (float)cx, cyf = (float)cy;
 #pragma unroll
-        for (int v = 0; v < V; ++v) {
-          const double fl = XL[((size_t)fxl * P + j) * V + v], fr = XR[((size_t)(fxl + 1) * P + j) * V + v];
-          d[v] = d[v] - cx * (fr * op.FRd[i] - fl * op.FLd[i]);
-        }
+          for (int v = 0; v < V; ++v) {
+            const float fl = (float)XL[((size_t)fxl * P + j) * V + v], fr = (float)XR[((size_t)(fxl + 1) * P + j) * V + v];
+            const float gb = (float)YB[((size_t)fyb * P + i) * V + v], gt = (float)YT[((size_t)fyt * P + i) * V + v];
+            const float sx = fr * (float)op.FRd[i] - fl * (float)op.FLd[i];
+            const float sy = gt * (float)op.FRd[j] - gb * (float)op.FLd[j];
+            d[v] = d[v] - (double)(cxf * sx + cyf * sy);
+          }
+        } else {
 #pragma unroll
-        for (int v = 0; v < V; ++v) {
-          const double gb = YB[((size_t)fyb * P + i) * V + v], gt = YT[((size_t)fyt * P + i) * V + v];
-          d[v] = d[v] - cy * (gt * op.FRd[j] - gb * op.FLd[j]);
+          for (int v = 0; v < V; ++v) {
+            const double fl = XL[((size_t)fxl * P + j) * V + v], fr = XR[((size_t)(fxl + 1) * P + j) * V + v];
+            d[v] = d[v] - cx * (fr * op.FRd[i] - fl * op.FLd[i]);
+          }
+#pragma unroll
+          for (int v = 0; v < V; ++v) {
+            const double gb = YB[((size_t)fyb * P + i) * V + v], gt = YT[((size_t)fyt * P + i) * V + v];
+            d[v] = d[v] - cy * (gt * op.FRd[j] - gb * op.FLd[j]);
+          }
         }
       }
       if (mode == kCellSurface) {
@@ -212,7 +261,8 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
         double* un = a.uh[par ^ 1] + off;
 #pragma unroll
         for (int v = 0; v < V; ++v) {
-          d[v] = d[v] / (op.wd[i] * op.wd[j]);
+          if constexpr (kFast) d[v] = d[v] * op.iww[i + P * j];
+          else d[v] = d[v] / (op.wd[i] * op.wd[j]);
           u[v] = uo[v] + dt * d[v];
           un[v] = u[v];
         }
@@ -226,7 +276,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
 
   // ------------------------------------------------------------- CFL part
   const bool want_cfl = mode != kCellInitDmp;
-  if (act && want_cfl) atomicMax(&cmax[lc], (unsigned long long)__double_as_longlong(cfl_denom<Sys, N>(in, u)));
+  if (act && want_cfl) atomicMax(&cmax[lc], (unsigned long long)__double_as_longlong(cfl_denom<Sys, N, kFast>(in, u)));
 
   // ------------------------------------------------------------- DMP part
   const bool want_dmp = limiter && mode != kCellCfl;
@@ -239,7 +289,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
       for (int v = 0; v < V; ++v) U[v * P2 + node] = u[v];
     }
     __syncthreads();
-    if (act && !from_lh) Proj<N, V>::ypass(U, LY, LB, op, node, P2);
+    if (act && !from_lh) Proj<N, V>::template ypass<kFast>(U, LY, LB, op, node, P2);
     __syncthreads();
     double mn[V], mx[V];
     bool posfail = false;
@@ -252,7 +302,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
 #pragma unroll
           for (int v = 0; v < V; ++v) { mn[v] = fmin(mn[v], L[idx * V + v]); mx[v] = fmax(mx[v], L[idx * V + v]); }
       } else {
-        Proj<N, V>::template xpass_minmax<Sys>(U, LY, LB, op, in.ph, node, P2, mn, mx, posfail);
+        Proj<N, V>::template xpass_minmax<Sys, kFast>(U, LY, LB, op, in.ph, node, P2, mn, mx, posfail);
       }
 #pragma unroll
       for (int v = 0; v < V; ++v) {
@@ -344,10 +394,11 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
     int cur = -1;
     unsigned long long m = 0ull;
     for (int c = 0; c < CPB; ++c) {
-      const long long cc = (long long)blockIdx.x * CPB + c;
+      const long long cc = a.cell0 + (long long)blockIdx.x * CPB + c;
       if (cc >= a.ncells) break;
       const int kk = find_inst_cell(a.inst, a.ninst, cc);
-      const bool ok = a.st[kk].active || mode == kCellPrime || mode == kCellCfl;
+      if (kk < 0) continue;
+      const bool ok = priming ? (a.only_inst < 0 || kk == a.only_inst) : a.st[kk].active != 0;
       if (!ok) continue;
       if (kk != cur) {
         if (cur >= 0) atomicMax(&a.st[cur].denom_next, m);

@@ -52,6 +52,7 @@ struct InstState {
   int n_list;                        // cells with recompute > 0
   int nonfinite;                     // set when dt came out non-finite
   long long steps;
+  long long max_steps;               // > 0: stop after this many steps
 };
 
 // Host-computed constants of the face kernel (transcendentals are evaluated
@@ -77,6 +78,7 @@ struct DevOps {
   R wg;              // sum_l' w(l') g(l')
   R FL[P], FR[P];
   double wd[P], FLd[P], FRd[P];
+  double iww[P * P];     // 1 / (w_i w_j) at [i + P*j]
   double xid[P];
   double uh2lim[S * P];  // (s,k) at [s + S*k]
   double lim2uh[P * S];  // (k,s) at [k + P*s]
@@ -119,17 +121,23 @@ struct BatchArgs {
   double* denom;                     // per-cell CFL denominator
   const double* lh_ic;               // initial-limiter candidates
   int mode;                          // kernel mode switch
+  long long cell0;                   // first cell of a launch over part of the cell range (K1, K3)
+  int only_inst;                     // >= 0: the priming modes of K3 touch this instance only
 };
 
 __device__ __forceinline__ int parity(const InstState& s) { return (int)(s.steps & 1); }
 
-// Locate the instance owning a global cell (binary search on cell_base).
+// Locate the instance owning a global cell (binary search on cell_base, the
+// table sorted by it); -1 when the cell lies in no instance (instances of a
+// batch occupy ranges of a shared pool, with gaps between them).
 __device__ __forceinline__ int find_inst_cell(const InstDesc* inst, int n, long long cell) {
   int lo = 0, hi = n - 1;
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
     if (inst[mid].cell_base <= cell) lo = mid; else hi = mid - 1;
   }
+  const InstDesc& d = inst[lo];
+  if (cell < d.cell_base || cell - d.cell_base >= (long long)d.imax * d.jmax) return -1;
   return lo;
 }
 

@@ -27,10 +27,12 @@ __device__ __forceinline__ double dt_from_denom(double cfl_pnpm, double maxd) {
   return dt;
 }
 
-__global__ void k_control(InstDesc* inst, InstState* st, int ninst, int* list_count, int mode) {
+// only >= 0: the priming modes (reset, commit) act on that instance alone
+static __global__ void k_control(InstDesc* inst, InstState* st, int ninst, int* list_count, int mode, int only) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k == 0 && list_count && (mode == kCtlBegin || mode == kCtlPrimeReset)) *list_count = 0;
+  if (k == 0 && list_count && (mode == kCtlBegin || (mode == kCtlPrimeReset && only < 0))) *list_count = 0;
   if (k >= ninst) return;
+  if (only >= 0 && k != only) return;
   InstState& s = st[k];
   switch (mode) {
     case kCtlBegin: {
@@ -39,7 +41,8 @@ __global__ void k_control(InstDesc* inst, InstState* st, int ninst, int* list_co
       const double maxd = __longlong_as_double((long long)s.denom_bits);
       // a NaN denominator anywhere folds to the largest bit pattern
       if (isnan(maxd)) s.nonfinite = 1;
-      if (s.time < s.tend && !s.nonfinite) {
+      const bool budget = s.max_steps <= 0 || s.steps < s.max_steps;
+      if (s.time < s.tend && !s.nonfinite && budget) {
         double dt = dt_from_denom(inst[k].cfl_pnpm, maxd);
         if (s.time + dt > s.tend) dt = s.tend - s.time;
         if (!isfinite(dt) || !(dt > 0.0)) {

@@ -34,6 +34,7 @@ __global__ void __launch_bounds__(256) k_volume(BatchArgs a, DevOps<N, double> o
   const int node = (int)(gid - cell * P2);
   const int i = node % P, j = node / P;
   const int k = find_inst_cell(a.inst, a.ninst, cell);
+  if (k < 0) return;
   const InstDesc& in = a.inst[k];
   if (!a.st[k].active) return;
   const double* F = a.fhi + (size_t)cell * P2 * 2 * V;  // Fhi(v,d,i,j)
@@ -61,18 +62,26 @@ cudaError_t faces(const BatchArgs& a, const FaceConst& fc, int fp32, cudaStream_
   return cudaGetLastError();
 }
 
-cudaError_t cells(const BatchArgs& a, const void* ops, cudaStream_t s) {
+template <bool kFast>
+cudaError_t launch_cells(const BatchArgs& a, const void* ops, cudaStream_t s) {
   using C = CellCfg<Sys, N>;
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_cells<Sys, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_cells<Sys, N, kFast>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  const long long grid = (a.ncells + C::CPB - 1) / C::CPB;
+  const long long grid = (a.ncells - a.cell0 + C::CPB - 1) / C::CPB;
   if (grid <= 0) return cudaSuccess;
-  k_cells<Sys, N><<<(unsigned)grid, C::THREADS, C::SMEM_BYTES, s>>>(a, *reinterpret_cast<const DevOps<N, double>*>(ops));
+  k_cells<Sys, N, kFast><<<(unsigned)grid, C::THREADS, C::SMEM_BYTES, s>>>(a, *reinterpret_cast<const DevOps<N, double>*>(ops));
   return cudaGetLastError();
+}
+
+// fast = 1 (FP32-mixed precision): FP64 with fused multiply-adds in the DMP
+// projections and a reciprocal mass matrix; fast = 0: reference order
+cudaError_t cells(const BatchArgs& a, const void* ops, int fast, cudaStream_t s) {
+  return fast ? launch_cells<true>(a, ops, s) : launch_cells<false>(a, ops, s);
 }
 
 cudaError_t volume(const BatchArgs& a, const void* ops, cudaStream_t s) {

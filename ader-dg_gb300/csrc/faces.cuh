@@ -15,12 +15,15 @@
 
 namespace aderdg {
 
+// instance owning an x / y face, or -1 (faces between instances of a batch)
 __device__ __forceinline__ int find_inst_fx(const InstDesc* inst, int n, long long f) {
   int lo = 0, hi = n - 1;
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
     if (inst[mid].fx_base <= f) lo = mid; else hi = mid - 1;
   }
+  const InstDesc& d = inst[lo];
+  if (f < d.fx_base || f - d.fx_base >= (long long)(d.imax + 1) * d.jmax) return -1;
   return lo;
 }
 __device__ __forceinline__ int find_inst_fy(const InstDesc* inst, int n, long long f) {
@@ -29,6 +32,8 @@ __device__ __forceinline__ int find_inst_fy(const InstDesc* inst, int n, long lo
     int mid = (lo + hi + 1) >> 1;
     if (inst[mid].fy_base <= f) lo = mid; else hi = mid - 1;
   }
+  const InstDesc& d = inst[lo];
+  if (f < d.fy_base || f - d.fy_base >= (long long)d.imax * (d.jmax + 1)) return -1;
   return lo;
 }
 
@@ -51,6 +56,91 @@ __device__ __forceinline__ void dmr_state(const Phys& ph, const double* Vp, int 
   for (int v = 0; v < 4; ++v) F[v] = Fb[d * 4 + v];
 }
 
+// Euler Rusanov pieces in the compute type T (FP32 in the mixed mode)
+template <class T>
+__device__ __forceinline__ T euler_max_eig_t(T gamma, const T* Q, int d) {
+  const T u = (d == 0 ? Q[1] : Q[2]) / Q[0];
+  const T p = (gamma - T(1)) * (Q[3] - T(0.5) * (Q[1] * Q[1] + Q[2] * Q[2]) / Q[0]);
+  const T c = sqrt(gamma * p / Q[0]);
+  return fmax(fmax(fabs(u - c), fabs(u)), fabs(u + c));
+}
+template <class T>
+__device__ __forceinline__ void euler_bc_state_t(T gamma, const double* Vp, int d, T* Q, T* F) {
+  Q[0] = T(Vp[0]);
+  Q[1] = T(Vp[0] * Vp[1]);
+  Q[2] = T(Vp[0] * Vp[2]);
+  Q[3] = T(Vp[3] / (double(gamma) - 1) + 0.5 * Vp[0] * (Vp[1] * Vp[1] + Vp[2] * Vp[2]));
+  const T irho = T(1) / Q[0];
+  const T p = (gamma - T(1)) * (Q[3] - T(0.5) * (Q[1] * Q[1] + Q[2] * Q[2]) * irho);
+  const T un = (d == 0 ? Q[1] : Q[2]);
+  F[0] = un;
+  F[1] = irho * un * Q[1] + (d == 0 ? p : T(0));
+  F[2] = irho * un * Q[2] + (d == 1 ? p : T(0));
+  F[3] = irho * un * (Q[3] + p);
+}
+
+// FP32-mixed faces for Euler: boundary logic as in k_faces, arithmetic in FP32
+template <int N>
+__device__ void faces_euler_fp32(const BatchArgs& a, const FaceConst& fc, const InstDesc& in, int k, bool xdir, int i,
+                                 int j, int l, long long face) {
+  constexpr int P = N + 1, V = 4;
+  const float* qb = reinterpret_cast<const float*>(a.qbnd);
+  const float* fb = reinterpret_cast<const float*>(a.fbnd);
+  const int I = in.imax, J = in.jmax;
+  auto cid = [&](int ci, int cj) { return in.cell_base + (long long)ci + (long long)I * cj; };
+  auto load = [&](long long c, int f, float* Q, float* F) {
+    const size_t o = (((size_t)c * P + l) * 4 + f) * V;
+#pragma unroll
+    for (int v = 0; v < V; ++v) { Q[v] = qb[o + v]; F[v] = fb[o + v]; }
+  };
+  const float gamma = (float)in.ph.gamma;
+  const int d = xdir ? 0 : 1, pos = xdir ? i : j, last = xdir ? I : J;
+  const int bcl = in.bc[xdir ? 0 : 2], bcr = in.bc[xdir ? 1 : 3];
+  const int fl = xdir ? 0 : 2, fr = xdir ? 1 : 3;
+  const bool is_dmr = in.bc_mode == 1;
+  float QL[V], QR[V], FL[V], FR[V];
+  const long long cR = cid(i, j);
+  if (pos == 0) {
+    if (is_dmr && xdir) {
+      euler_bc_state_t<float>(gamma, fc.Va, 0, QL, FL);
+      load(cR, fl, QR, FR);
+    } else if (is_dmr) {
+      load(cR, fl, QL, FL);
+      if (!((double)(i + 1) * in.dx <= 1.0 / 6.0)) {
+        QL[2] = -QL[2];
+        FL[0] = -FL[0];
+        FL[1] = -FL[1];
+        FL[3] = -FL[3];
+      }
+      load(cR, fl, QR, FR);
+    } else if (bcl == 3) {
+      load(xdir ? cid(I - 1, j) : cid(i, J - 1), fr, QL, FL);
+      load(cR, fl, QR, FR);
+    } else {
+      load(cR, fl, QL, FL);
+      load(cR, fl, QR, FR);
+    }
+  } else if (pos == last) {
+    const long long cLast = xdir ? cid(I - 1, j) : cid(i, J - 1);
+    load(cLast, fr, QL, FL);
+    if (is_dmr && !xdir) {
+      const double x_sw = fc.xsw0 + fc.xsw1 * a.st[k].time;
+      euler_bc_state_t<float>(gamma, ((double)(i + 1) * in.dx <= x_sw) ? fc.Va : fc.Vb, 1, QR, FR);
+    } else if (!is_dmr && bcr == 3) {
+      load(xdir ? cid(0, j) : cid(i, 0), fl, QR, FR);
+    } else {
+      load(cLast, fr, QR, FR);
+    }
+  } else {
+    load(xdir ? cid(i - 1, j) : cid(i, j - 1), fr, QL, FL);
+    load(cR, fl, QR, FR);
+  }
+  const float smax = fmaxf(euler_max_eig_t<float>(gamma, QL, d), euler_max_eig_t<float>(gamma, QR, d));
+  double* dst = (xdir ? a.fu : a.gu) + ((size_t)face * P + l) * V;
+#pragma unroll
+  for (int v = 0; v < V; ++v) dst[v] = (double)(0.5f * (FL[v] + FR[v]) - 0.5f * smax * (QR[v] - QL[v]));
+}
+
 template <class Sys, int N, class R>
 __global__ void __launch_bounds__(256) k_faces(BatchArgs a, FaceConst fc) {
   constexpr int P = N + 1, V = Sys::V;
@@ -64,6 +154,7 @@ __global__ void __launch_bounds__(256) k_faces(BatchArgs a, FaceConst fc) {
   const long long face = g / P;
   const int l = (int)(g - face * P);
   const int k = xdir ? find_inst_fx(a.inst, a.ninst, face) : find_inst_fy(a.inst, a.ninst, face);
+  if (k < 0) return;
   const InstDesc& in = a.inst[k];
   if (!a.st[k].active) return;
   const Phys ph = in.ph;
@@ -79,6 +170,10 @@ __global__ void __launch_bounds__(256) k_faces(BatchArgs a, FaceConst fc) {
   const int bcl = in.bc[xdir ? 0 : 2], bcr = in.bc[xdir ? 1 : 3];
   const int fl = xdir ? 0 : 2, fr = xdir ? 1 : 3;  // left/bottom and right/top face ids
   const size_t out = ((size_t)face * P + l) * V;
+  if constexpr (Sys::ID == kSysEuler && sizeof(R) == 4) {
+    faces_euler_fp32<N>(a, fc, in, k, xdir, i, j, l, face);
+    return;
+  }
 
   if constexpr (Sys::ID == kSysAD) {
     // Advection-Diffusion/riemann_problem.f90 with PDEViscLLFRiemannSolver (pde.f90:121-152)

@@ -20,9 +20,8 @@ namespace aderdg {
 template <class Sys, int N>
 __global__ void __launch_bounds__(256) k_mark(BatchArgs a) {
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool ok = c < a.ncells;
-  const int k = ok ? find_inst_cell(a.inst, a.ninst, c) : -1;
-  const bool act = ok && a.st[k].active;
+  const int k = c < a.ncells ? find_inst_cell(a.inst, a.ninst, c) : -1;
+  const bool act = k >= 0 && a.st[k].active;
   unsigned long long val = 0ull;
   if (act) {
     const InstDesc& in = a.inst[k];

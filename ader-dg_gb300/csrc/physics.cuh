@@ -42,6 +42,25 @@ struct EulerSys {
     double c = sqrt(ph.gamma * p / Q[0]);
     return fmax(fmax(fabs(u - c), fabs(u)), fabs(u + c));
   }
+  // both axes at once: the pressure and sound speed do not depend on the
+  // normal, so they are formed once (same expressions, same rounding)
+  __device__ static void max_eig2(const Phys& ph, const double* Q, double& ex, double& ey) {
+    double p = (ph.gamma - 1.0) * (Q[3] - 0.5 * (Q[1] * Q[1] + Q[2] * Q[2]) / Q[0]);
+    double c = sqrt(ph.gamma * p / Q[0]);
+    double u = Q[1] / Q[0], v = Q[2] / Q[0];
+    ex = fmax(fmax(fabs(u - c), fabs(u)), fabs(u + c));
+    ey = fmax(fmax(fabs(v - c), fabs(v)), fabs(v + c));
+  }
+  // FP32 eigenvalues for the mixed-precision CFL (the max reduction stays FP64)
+  __device__ static void max_eig2_f32(const Phys& ph, const double* Qd, double& ex, double& ey) {
+    const float q0 = (float)Qd[0], q1 = (float)Qd[1], q2 = (float)Qd[2], q3 = (float)Qd[3];
+    const float iq = 1.0f / q0;
+    const float p = (float)(ph.gamma - 1.0) * (q3 - 0.5f * (q1 * q1 + q2 * q2) * iq);
+    const float c = sqrtf((float)ph.gamma * p * iq);
+    const float u = q1 * iq, v = q2 * iq;
+    ex = (double)(fabsf(u) + c);
+    ey = (double)(fabsf(v) + c);
+  }
   // Euler/pde.f90:29-40
   __device__ static void prim2cons(const Phys& ph, const double* Vp, double* Q) {
     Q[0] = Vp[0];
@@ -55,13 +74,32 @@ struct EulerSys {
     double p = (ph.gamma - 1) * (Q[3] - 0.5 * (Q[1] * Q[1] + Q[2] * Q[2]) * irho);
     return !(Q[0] <= 1.0e-12) && !(p <= 1.0e-12);
   }
+  // Same answer as positive(): an FP32 evaluation with a margin 20x its
+  // rounding error settles the clearly admissible states, the exact FP64
+  // expression decides the rest.
+  __device__ static bool positive_fast(const Phys& ph, const double* Q) {
+    if (Q[0] <= 1.0e-12) return false;
+    const float q0 = (float)Q[0], q1 = (float)Q[1], q2 = (float)Q[2], q3 = (float)Q[3];
+    const float ke = 0.5f * (q1 * q1 + q2 * q2) / q0;
+    const float g1 = (float)(ph.gamma - 1.0);
+    const float pf = g1 * (q3 - ke);
+    const float margin = g1 * 1.0e-5f * (fabsf(q3) + ke);
+    if (q0 > 1.0e-30f && q0 < 1.0e30f && pf - margin > 2.0e-12f && margin < 1.0e30f) return true;
+    return positive(ph, Q);
+  }
 
+  // physical constants of the predictor flux in its compute precision
+  template <class R>
+  struct PConst {
+    R gm1;
+    __device__ explicit PConst(const Phys& ph) : gm1(R(ph.gamma - 1.0)) {}
+  };
   // predictor flux: Fx, Fy of the same state
   template <class R>
-  __device__ __forceinline__ static void pflux(const Phys& ph, const R* Q, R* Fx, R* Fy) {
+  __device__ __forceinline__ static void pflux(const PConst<R>& pc, const R* Q, R* Fx, R* Fy) {
     const R ir = R(1) / Q[0];
     const R u = Q[1] * ir, v = Q[2] * ir;
-    const R p = R(ph.gamma - 1.0) * (Q[3] - R(0.5) * (Q[1] * u + Q[2] * v));
+    const R p = pc.gm1 * (Q[3] - R(0.5) * (Q[1] * u + Q[2] * v));
     const R e = Q[3] + p;
     Fx[0] = Q[1];
     Fx[1] = Q[1] * u + p;
@@ -134,6 +172,36 @@ struct BNSys {
     m = fmax(m, fabs(u_g));
     m = fmax(m, fabs(u_s));
     return m;
+  }
+  __device__ static void max_eig2(const Phys& ph, const double* Q, double& ex, double& ey) {
+    double Vp[9];
+    cons2prim(ph, Q, Vp);
+    double a_s = sqrt(ph.gs * (Vp[3] + ph.ps) / Vp[0]);
+    double a_g = sqrt(ph.gg * (Vp[7] + ph.pg) / Vp[4]);
+    for (int d = 0; d < 2; ++d) {
+      double u_s = (d == 0) ? Vp[1] * 1.0 + Vp[2] * 0.0 : Vp[1] * 0.0 + Vp[2] * 1.0;
+      double u_g = (d == 0) ? Vp[5] * 1.0 + Vp[6] * 0.0 : Vp[5] * 0.0 + Vp[6] * 1.0;
+      double m = fabs(u_g - a_g);
+      m = fmax(m, fabs(u_g + a_g));
+      m = fmax(m, fabs(u_s - a_s));
+      m = fmax(m, fabs(u_s + a_s));
+      m = fmax(m, fabs(u_g));
+      m = fmax(m, fabs(u_s));
+      (d == 0 ? ex : ey) = m;
+    }
+  }
+  __device__ static void max_eig2_f32(const Phys& ph, const double* Qd, double& ex, double& ey) {
+    float q[9];
+    for (int v = 0; v < 9; ++v) q[v] = (float)Qd[v];
+    const float a = q[8], b = 1.0f - q[8];
+    const float irs = 1.0f / q[0], irg = 1.0f / q[4];
+    const float us = q[1] * irs, vs = q[2] * irs, ug = q[5] * irg, vg = q[6] * irg;
+    const float rs = q[0] / a, rg = q[4] / b;
+    const float ps = (float)(ph.gs - 1.0) * (q[3] / a - 0.5f * rs * (us * us + vs * vs)) - (float)(ph.gs * ph.ps);
+    const float pg = (float)(ph.gg - 1.0) * (q[7] / b - 0.5f * rg * (ug * ug + vg * vg)) - (float)(ph.gg * ph.pg);
+    const float as = sqrtf((float)ph.gs * (ps + (float)ph.ps) / rs), ag = sqrtf((float)ph.gg * (pg + (float)ph.pg) / rg);
+    ex = (double)fmaxf(fabsf(ug) + ag, fabsf(us) + as);
+    ey = (double)fmaxf(fabsf(vg) + ag, fabsf(vs) + as);
   }
   // column 9 of PDEMatrixB (Baer-Nunziato/pde.f90:150-186); the other columns are zero
   __device__ static void matrixB_col9(const Phys& ph, const double* Q, int d, double* b) {
@@ -211,17 +279,48 @@ struct BNSys {
     bad = bad || (Vp[8] <= 0.0 || Vp[8] >= 1.0);
     return !bad;
   }
+  // Same answer as positive(), with an FP32 pre-check (margin 20x its
+  // rounding error) that settles clearly admissible states.
+  __device__ static bool positive_fast(const Phys& ph, const double* Q) {
+    if (!(Q[8] > 0.0) || !(Q[8] < 1.0)) return positive(ph, Q);
+    float q[9];
+    for (int v = 0; v < 9; ++v) {
+      q[v] = (float)Q[v];
+      const float aq = fabsf(q[v]);
+      if (!(aq < 1.0e30f) || (aq != 0.0f && aq < 1.0e-30f)) return positive(ph, Q);
+    }
+    const float a = q[8], b = 1.0f - q[8];
+    if (!(a > 1.0e-6f) || !(b > 1.0e-6f)) return positive(ph, Q);
+    const float rs = q[0] / a, rg = q[4] / b;
+    const float kes = 0.5f * (q[1] * q[1] + q[2] * q[2]) / q[0];  // 0.5 rho_s |u_s|^2 * phi_s
+    const float keg = 0.5f * (q[5] * q[5] + q[6] * q[6]) / q[4];
+    const float es = q[3] / a, eg = q[7] / b;
+    const float gs1 = (float)(ph.gs - 1.0), gg1 = (float)(ph.gg - 1.0);
+    const float ps = gs1 * (es - kes / a) - (float)(ph.gs * ph.ps) + (float)ph.ps;  // p_s + pi_s
+    const float pg = gg1 * (eg - keg / b) - (float)(ph.gg * ph.pg) + (float)ph.pg;  // p_g + pi_g
+    const float ms = 1.0e-5f * (gs1 * (fabsf(es) + kes / a) + (float)fabs(ph.gs * ph.ps) + (float)fabs(ph.ps));
+    const float mg = 1.0e-5f * (gg1 * (fabsf(eg) + keg / b) + (float)fabs(ph.gg * ph.pg) + (float)fabs(ph.pg));
+    const bool clear = rs > 2.0e-12f * (1.0f + 1.0e-5f) + 1.0e-5f * rs && rg > 2.0e-12f + 1.0e-5f * rg &&
+                       ps - ms > 2.0e-12f && pg - mg > 2.0e-12f && ms < 1.0e30f && mg < 1.0e30f;
+    return clear ? true : positive(ph, Q);
+  }
 
+  template <class R>
+  struct PConst {
+    R gs1, gg1, gsps, ggpg;
+    __device__ explicit PConst(const Phys& ph)
+        : gs1(R(ph.gs - 1.0)), gg1(R(ph.gg - 1.0)), gsps(R(ph.gs * ph.ps)), ggpg(R(ph.gg * ph.pg)) {}
+  };
   // predictor flux plus the three scalars the NCP needs (p_g, u_s, v_s)
   template <class R>
-  __device__ __forceinline__ static void pflux(const Phys& ph, const R* Q, R* Fx, R* Fy, R& p_g, R& u_s, R& v_s) {
+  __device__ __forceinline__ static void pflux(const PConst<R>& pc, const R* Q, R* Fx, R* Fy, R& p_g, R& u_s, R& v_s) {
     const R a = Q[8], b = R(1) - Q[8];
     const R irs = R(1) / Q[0], irg = R(1) / Q[4];
     u_s = Q[1] * irs;
     v_s = Q[2] * irs;
     const R u_g = Q[5] * irg, v_g = Q[6] * irg;
-    const R Ps = R(ph.gs - 1.0) * (Q[3] - R(0.5) * (Q[1] * u_s + Q[2] * v_s)) - a * R(ph.gs * ph.ps);  // phi_s p_s
-    const R Pg = R(ph.gg - 1.0) * (Q[7] - R(0.5) * (Q[5] * u_g + Q[6] * v_g)) - b * R(ph.gg * ph.pg);  // phi_g p_g
+    const R Ps = pc.gs1 * (Q[3] - R(0.5) * (Q[1] * u_s + Q[2] * v_s)) - a * pc.gsps;  // phi_s p_s
+    const R Pg = pc.gg1 * (Q[7] - R(0.5) * (Q[5] * u_g + Q[6] * v_g)) - b * pc.ggpg;  // phi_g p_g
     p_g = Pg / b;
     const R es = Q[3] + Ps, eg = Q[7] + Pg;
     Fx[0] = Q[1];
@@ -263,6 +362,10 @@ struct BNSys {
 struct ADSys {
   static constexpr int V = 1;
   static constexpr int ID = kSysAD;
+  template <class R>
+  struct PConst {
+    __device__ explicit PConst(const Phys&) {}
+  };
   // Advection-Diffusion/pde.f90:70-80 (|cx nv1 + cy nv2|)
   __device__ static double max_eig_c(const Phys& ph, int d) {
     return fabs(d == 0 ? ph.cx * 1.0 + ph.cy * 0.0 : ph.cx * 0.0 + ph.cy * 1.0);

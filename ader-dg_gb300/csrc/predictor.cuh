@@ -31,43 +31,80 @@ namespace aderdg {
 template <class Sys, int N, class R>
 struct PredCfg {
   static constexpr int P = N + 1, P2 = P * P, V = Sys::V;
-  // shared-memory elements per cell: flux buffer [P][2][V][P2] (+ BN volume
-  // fraction [P][P2]; AD: state [P][P2] + flux [P][2][P2])
-  static constexpr int CELL_ELEMS = (Sys::ID == kSysAD) ? 3 * P * P2 : (2 * V * P + (Sys::ID == kSysBN ? P : 0)) * P2;
+  // variables of one node padded to whole 16-byte vectors (AD: scalar)
+  static constexpr int VEC = 16 / (int)sizeof(R);
+  // FP32: pad to whole float4; FP64: double2 only when V is even (padding
+  // Baer-Nunziato's 9 doubles costs more registers than it saves loads)
+  static constexpr int VP = (V == 1) ? 1 : (sizeof(R) == 4 ? ((V + VEC - 1) / VEC) * VEC : V);
+  // shared-memory elements per cell: flux buffer [P][2][P2][VP] (+ BN volume
+  // fraction [P][P2]; AD: flux [P][2][P2] + state [P][P2]), rounded to 16 bytes;
+  // the epilogue reuses it as [V][P2] x 3 (AD: x 5)
+  static constexpr int RAW = (Sys::ID == kSysAD) ? 3 * P * P2 : (2 * VP * P + (Sys::ID == kSysBN ? P : 0)) * P2;
+  static constexpr int CELL_ELEMS = ((RAW + VEC - 1) / VEC) * VEC;
   static constexpr int MAX_THREADS = 256;
   static constexpr int SMEM_BUDGET = 100 * 1024;
   static constexpr int CPB_T = MAX_THREADS / P2;
   static constexpr int CPB_S = SMEM_BUDGET / (CELL_ELEMS * (int)sizeof(R));
   static constexpr int CPB = (CPB_T < CPB_S ? CPB_T : CPB_S) < 1 ? 1 : (CPB_T < CPB_S ? CPB_T : CPB_S);
   static constexpr int THREADS = ((CPB * P2 + 31) / 32) * 32;
+  // FP32 is latency-bound at one CTA per SM: ask for two (FP64 is pipe-bound either way)
+  static constexpr int MIN_BLOCKS = (sizeof(R) == 4 && THREADS > 128) ? 2 : 1;
   // threads past CPB*P2 (the tail of the last warp) take part in the barriers
   // and get a scratch slot of their own so they never touch a real cell's data
   static constexpr int SLOTS = CPB + (THREADS > CPB * P2 ? 1 : 0);
   static constexpr int SMEM_BYTES = SLOTS * CELL_ELEMS * (int)sizeof(R);
 };
 
-// Flux-derivative contraction of time level l into b[v].
-template <int V, int P, class R>
+// Loads the VP (padded) variables of one node with 16-byte vector loads.
+template <class R, int VP>
+__device__ __forceinline__ void vload(const R* __restrict__ p, R* out) {
+  if constexpr (VP % (16 / sizeof(R)) != 0) {
+#pragma unroll
+    for (int q = 0; q < VP; ++q) out[q] = p[q];
+  } else if constexpr (sizeof(R) == 4) {
+#pragma unroll
+    for (int q = 0; q < VP / 4; ++q) {
+      const float4 t = reinterpret_cast<const float4*>(p)[q];
+      out[4 * q] = t.x; out[4 * q + 1] = t.y; out[4 * q + 2] = t.z; out[4 * q + 3] = t.w;
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < VP / 2; ++q) {
+      const double2 t = reinterpret_cast<const double2*>(p)[q];
+      out[2 * q] = t.x; out[2 * q + 1] = t.y;
+    }
+  }
+}
+
+// Flux-derivative contraction of time level l into b[v]; flux buffer [P][2][P2][VP].
+template <int V, int VP, int P, class R>
 __device__ __forceinline__ void contract(const R* __restrict__ cs, int l, int i, int j, const R* Dx, const R* Dy, R* b) {
   constexpr int P2 = P * P;
-  const R* fx = cs + (size_t)(l * 2 + 0) * V * P2;
-  const R* fy = cs + (size_t)(l * 2 + 1) * V * P2;
+  const R* fx = cs + (size_t)(l * 2 + 0) * P2 * VP;
+  const R* fy = cs + (size_t)(l * 2 + 1) * P2 * VP;
 #pragma unroll
-  for (int v = 0; v < V; ++v) {
-    R s = R(0);
+  for (int v = 0; v < V; ++v) b[v] = R(0);
 #pragma unroll
-    for (int k = 0; k < P; ++k) s = fma(Dx[k], fx[v * P2 + k + P * j], s);
+  for (int k = 0; k < P; ++k) {
+    R f[VP];
+    vload<R, VP>(fx + (k + P * j) * VP, f);
 #pragma unroll
-    for (int k = 0; k < P; ++k) s = fma(Dy[k], fy[v * P2 + i + P * k], s);
-    b[v] = s;
+    for (int v = 0; v < V; ++v) b[v] = fma(Dx[k], f[v], b[v]);
+  }
+#pragma unroll
+  for (int k = 0; k < P; ++k) {
+    R f[VP];
+    vload<R, VP>(fy + (i + P * k) * VP, f);
+#pragma unroll
+    for (int v = 0; v < V; ++v) b[v] = fma(Dy[k], f[v], b[v]);
   }
 }
 
 template <class Sys, int N, class R, bool kPhase>
-__global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS)
+__global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R>::MIN_BLOCKS)
     k_predictor(BatchArgs a, DevOps<N, R> op) {
   using C = PredCfg<Sys, N, R>;
-  constexpr int P = N + 1, P2 = P * P, V = Sys::V, CPB = C::CPB;
+  constexpr int P = N + 1, P2 = P * P, V = Sys::V, CPB = C::CPB, VP = C::VP;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R* sm = reinterpret_cast<R*>(smem_raw);
 
@@ -75,17 +112,20 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS)
   const int lc = t / P2;
   const int node = t - lc * P2;
   const int i = node % P, j = node / P;
-  const long long cell = (long long)blockIdx.x * CPB + lc;
+  const long long cell = a.cell0 + (long long)blockIdx.x * CPB + lc;
   const bool in_cta = lc < CPB;
-  const bool valid = in_cta && cell < a.ncells;
+  const int k_found = (in_cta && cell < a.ncells) ? find_inst_cell(a.inst, a.ninst, cell) : -1;
+  const bool valid = k_found >= 0;
   R* cs = sm + (size_t)(lc < CPB ? lc : CPB) * C::CELL_ELEMS;  // lc >= CPB: the scratch slot
 
-  int k_inst = valid ? find_inst_cell(a.inst, a.ninst, cell) : 0;
+  const int k_inst = valid ? k_found : 0;
   const InstDesc& in = a.inst[k_inst];
   const bool act = valid && a.st[k_inst].active;
+  if (!__syncthreads_or(act)) return;  // nothing to do in this CTA (finished or absent instances)
   const double dt = act ? a.st[k_inst].dt : 0.0;
   const double* uh_in = a.uh[valid ? parity(a.st[k_inst]) : 0];
   const Phys ph = in.ph;
+  const typename Sys::template PConst<R> pc(ph);
 
   // per-thread contraction rows: Dx(i,k) = Kxi(k,i) dt/(dx w_i), Dy(j,k) likewise
   R Dx[P], Dy[P], Gx[P], Gy[P];
@@ -116,7 +156,7 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS)
   R Gh[2];      // AD: time-averaged gradient of the last iteration
   R qh[V];      // time-averaged state
 
-  auto fidx = [&](int l, int d, int v) { return (size_t)((l * 2 + d) * V + v) * P2 + node; };
+  auto fidx = [&](int l, int d, int v) { return ((size_t)(l * 2 + d) * P2 + node) * VP + v; };
 
   if constexpr (Sys::ID == kSysAD) {
     // -------------------------------------------------------------- AD
@@ -145,7 +185,7 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS)
     __syncthreads();
     {
       R b[1];
-      contract<1, P>(cs, 0, i, j, Dx, Dy, b);
+      contract<1, VP, P>(cs, 0, i, j, Dx, Dy, b);
 #pragma unroll
       for (int l = 0; l < P; ++l) q[l][0] = op.g[l] * u[0] - op.ts[l] * b[0];
     }
@@ -186,7 +226,7 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS)
 #pragma unroll
         for (int l = 0; l < P; ++l) {
           R b[1];
-          contract<1, P>(cs, l, i, j, Dx, Dy, b);
+          contract<1, VP, P>(cs, l, i, j, Dx, Dy, b);
 #pragma unroll
           for (int lp = 0; lp < P; ++lp) q[lp][0] = fma(-op.T[lp + P * l], b[0], q[lp][0]);
         }
@@ -195,7 +235,7 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS)
 #pragma unroll
         for (int l = 0; l < P; ++l) {
           R b[1];
-          contract<1, P>(cs, l, i, j, Dx, Dy, b);
+          contract<1, VP, P>(cs, l, i, j, Dx, Dy, b);
           qh[0] = fma(-op.tw[l], b[0], qh[0]);
         }
       }
@@ -204,16 +244,16 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS)
   } else {
     // ------------------------------------------------- Euler / Baer-Nunziato
     constexpr bool BN = Sys::ID == kSysBN;
-    R* as = cs + (size_t)2 * V * P * P2;  // BN volume fraction [P][P2]
+    R* as = cs + (size_t)2 * VP * P * P2;  // BN volume fraction [P][P2]
     R pg[P], us[P], vs[P];                // BN: NCP scalars per time level
     // iteration 1: the state is constant in time
     {
       R Fx[V], Fy[V];
       if constexpr (BN) {
-        Sys::template pflux<R>(ph, u, Fx, Fy, pg[0], us[0], vs[0]);
+        Sys::template pflux<R>(pc, u, Fx, Fy, pg[0], us[0], vs[0]);
         as[node] = u[8];
       } else {
-        Sys::template pflux<R>(ph, u, Fx, Fy);
+        Sys::template pflux<R>(pc, u, Fx, Fy);
       }
 #pragma unroll
       for (int v = 0; v < V; ++v) {
@@ -222,7 +262,7 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS)
       }
       __syncthreads();
       R b[V];
-      contract<V, P>(cs, 0, i, j, Dx, Dy, b);
+      contract<V, VP, P>(cs, 0, i, j, Dx, Dy, b);
       if constexpr (BN) {
         R ax = R(0), ay = R(0);
 #pragma unroll
@@ -252,10 +292,10 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS)
       for (int l = 0; l < P; ++l) {
         R Fx[V], Fy[V];
         if constexpr (BN) {
-          Sys::template pflux<R>(ph, q[l], Fx, Fy, pg[l], us[l], vs[l]);
+          Sys::template pflux<R>(pc, q[l], Fx, Fy, pg[l], us[l], vs[l]);
           as[l * P2 + node] = q[l][8];
         } else {
-          Sys::template pflux<R>(ph, q[l], Fx, Fy);
+          Sys::template pflux<R>(pc, q[l], Fx, Fy);
         }
 #pragma unroll
         for (int v = 0; v < V; ++v) {
@@ -280,7 +320,7 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS)
 #pragma unroll
       for (int l = 0; l < P; ++l) {
         R b[V];
-        contract<V, P>(cs, l, i, j, Dx, Dy, b);
+        contract<V, VP, P>(cs, l, i, j, Dx, Dy, b);
         if constexpr (BN) {
           R ax = R(0), ay = R(0);
 #pragma unroll

@@ -39,6 +39,8 @@ void make_ops(const HostOps& h, void* out) {
     o.FRd[a] = h.FR[a];
     o.xid[a] = h.xi[a];
   }
+  for (int j = 0; j < P; ++j)
+    for (int i = 0; i < P; ++i) o.iww[i + P * j] = 1.0 / (h.w[i] * h.w[j]);
   for (int k = 0; k < P * P; ++k) {
     o.Kxi[k] = (R)h.Kxi[k];
     o.dudx[k] = (R)h.dudx[k];
@@ -83,7 +85,7 @@ cudaError_t launch_pred(const BatchArgs& a, const void* ops, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  const long long grid = (a.ncells + C::CPB - 1) / C::CPB;
+  const long long grid = (a.ncells - a.cell0 + C::CPB - 1) / C::CPB;
   if (grid <= 0) return cudaSuccess;
   kern<<<(unsigned)grid, C::THREADS, C::SMEM_BYTES, s>>>(a, *reinterpret_cast<const DevOps<N, R>*>(ops));
   return cudaGetLastError();

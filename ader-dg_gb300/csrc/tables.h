@@ -25,7 +25,7 @@ struct KernelTable {
   int pred_threads[2] = {0, 0};
   // exact translation unit
   cudaError_t (*faces)(const BatchArgs&, const FaceConst&, int fp32, cudaStream_t) = nullptr;
-  cudaError_t (*cells)(const BatchArgs&, const void* ops64, cudaStream_t) = nullptr;
+  cudaError_t (*cells)(const BatchArgs&, const void* ops64, int fast, cudaStream_t) = nullptr;
   cudaError_t (*volume)(const BatchArgs&, const void* ops64, cudaStream_t) = nullptr;
   cudaError_t (*mark)(const BatchArgs&, cudaStream_t) = nullptr;
   cudaError_t (*subcell)(const BatchArgs&, const void* ops64, const FaceConst&, int grid, cudaStream_t) = nullptr;

@@ -211,6 +211,38 @@ int aderdg_get_info(aderdg_ctx* ctx, aderdg_info* info);
 
 const char* aderdg_last_error(aderdg_ctx* ctx); /* ctx may be NULL: last global error */
 
+/* ---- batched simulations ----
+ * Many independent simulations of one (system, N, precision, limiter) stepped
+ * by the same launches, each with its own grid, boundary conditions,
+ * physical parameters, CFL time step and end time (the reference runs one
+ * simulation per process; this is the GB300 form of running many).  The
+ * batch owns a pool of units; a simulation with an IMAX x JMAX grid takes
+ * (IMAX+1)(JMAX+1) consecutive units (first fit).  Simulations are admitted
+ * and released between steps while the others keep running. */
+typedef struct aderdg_batch aderdg_batch;
+
+/* Device bytes per unit of a batch of this kind (admission by HBM footprint). */
+long aderdg_batch_unit_bytes(int system, int N, int precision, int limiter);
+int aderdg_batch_create(int system, int N, int precision, int limiter, long capacity_units, int max_instances,
+                        aderdg_batch** out);
+int aderdg_batch_destroy(aderdg_batch* b);
+/* Admits one simulation (cfg must match the batch; uh and lh_ic as in
+ * aderdg_upload / aderdg_init_limiter, lh_ic nullable) that runs until tend
+ * or max_steps steps (<= 0: no limit).  *slot receives its id.
+ * ADERDG_ENOSPACE when no free range or table entry is left. */
+int aderdg_batch_admit(aderdg_batch* b, const aderdg_config* cfg, const double* uh, const double* lh_ic, double tend,
+                       long max_steps, int* slot);
+int aderdg_batch_release(aderdg_batch* b, int slot);
+/* Enqueues `steps` fused steps of every running simulation and returns
+ * without waiting; aderdg_batch_sync waits, reads the per-simulation state
+ * back and gives the number still running. */
+int aderdg_batch_launch(aderdg_batch* b, int steps);
+int aderdg_batch_sync(aderdg_batch* b, int* n_running);
+int aderdg_batch_query(aderdg_batch* b, int slot, double* time, double* dt, long* steps, int* done);
+int aderdg_batch_download(aderdg_batch* b, int slot, double* uh);
+int aderdg_batch_info(aderdg_batch* b, long* used_units, long* capacity_units, long* device_bytes, int* n_instances);
+const char* aderdg_batch_last_error(aderdg_batch* b);
+
 /* ---- host setup helpers (initial fields; not on the hot path) ---- */
 enum aderdg_ic {
   ADERDG_IC_AD_ZERO = 0,      /* Advection-Diffusion/initialize.f90:148-164 */
