@@ -158,7 +158,7 @@ def load(build_if_missing=False):
         "aderdg_batch_download": (i, [vp, i, dp]),
         "aderdg_batch_info": (i, [vp, ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long),
                                   ctypes.POINTER(ctypes.c_long), ip]),
-        "aderdg_batch_last_error": (ctypes.c_char_p, [vp]),
+        "aderdg_batch_last_error": (ctypes.c_char_p, [vp]), "aderdg_batch_profile": (i, [vp, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -177,7 +177,7 @@ EXPORTED = ("aderdg_create", "aderdg_destroy", "aderdg_upload", "aderdg_init_lim
             "aderdg_operator", "aderdg_step_host", "aderdg_time_steps", "aderdg_profile_step",
             "aderdg_batch_unit_bytes", "aderdg_batch_create", "aderdg_batch_destroy", "aderdg_batch_admit",
             "aderdg_batch_release", "aderdg_batch_launch", "aderdg_batch_sync", "aderdg_batch_query",
-            "aderdg_batch_download", "aderdg_batch_info", "aderdg_batch_last_error")
+            "aderdg_batch_download", "aderdg_batch_info", "aderdg_batch_last_error", "aderdg_batch_profile")
 
 
 def _dp(a):
@@ -458,6 +458,12 @@ class Batch:
         uh = np.empty(cfg.dofs, dtype=np.float64)
         self._ck(self.L.aderdg_batch_download(self.h, slot, _dp(uh)))
         return uh
+
+    def profile(self):
+        """Device milliseconds of each launch of one eager step of the batch."""
+        ms = np.zeros(7, dtype=np.float64)
+        self._ck(self.L.aderdg_batch_profile(self.h, _dp(ms)))
+        return dict(zip(Solver.PHASES, ms))
 
     def info(self):
         u, c, b = ctypes.c_long(0), ctypes.c_long(0), ctypes.c_long(0)

@@ -509,6 +509,43 @@ int aderdg_batch_info(aderdg_batch* b, long* used_units, long* capacity_units, l
   return ADERDG_OK;
 }
 
+int aderdg_batch_profile(aderdg_batch* b, double* phase_ms) {
+  if (!b || !phase_ms) return bfail(b, ADERDG_EINVAL, "null argument");
+  if (b->n_used == 0) {
+    for (int k = 0; k < 7; ++k) phase_ms[k] = 0.0;
+    return ADERDG_OK;
+  }
+  BatchArgs a = b->args;
+  a.ncells = a.nfx = a.nfy = b->hw;
+  a.mode = aderdg::kCellFused;
+  const int fp32 = b->precision ? 1 : 0;
+  cudaEvent_t ev[8];
+  for (auto& e : ev) BK(b, cudaEventCreate(&e));
+  BK(b, cudaEventRecord(ev[0], b->stream));
+  BK(b, bcontrol(b, aderdg::kCtlBegin, -1));
+  BK(b, cudaEventRecord(ev[1], b->stream));
+  BK(b, b->kt->predictor(a, bpred_ops(b), fp32, false, b->stream));
+  BK(b, cudaEventRecord(ev[2], b->stream));
+  BK(b, b->kt->faces(a, b->fc, fp32, b->stream));
+  BK(b, cudaEventRecord(ev[3], b->stream));
+  BK(b, b->kt->cells(a, b->ops64.data(), fp32, b->stream));
+  BK(b, cudaEventRecord(ev[4], b->stream));
+  if (b->limiter) BK(b, b->kt->mark(a, b->stream));
+  BK(b, cudaEventRecord(ev[5], b->stream));
+  if (b->limiter) BK(b, b->kt->subcell(a, b->ops64.data(), b->fc, b->subcell_grid, b->stream));
+  BK(b, cudaEventRecord(ev[6], b->stream));
+  BK(b, bcontrol(b, aderdg::kCtlEnd, -1));
+  BK(b, cudaEventRecord(ev[7], b->stream));
+  BK(b, cudaStreamSynchronize(b->stream));
+  for (int k = 0; k < 7; ++k) {
+    float ms = 0.f;
+    BK(b, cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+    phase_ms[k] = ms;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  return pull_states(b);
+}
+
 const char* aderdg_batch_last_error(aderdg_batch* b) { return b ? b->err.c_str() : ""; }
 
 }  // extern "C"

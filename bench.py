@@ -1,23 +1,39 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 ADER-DG time step.
 
-One "step" is one complete ADER-DG time step (calc_time_step, predictor with
-volume integral, Riemann problems, surface integral + element update + DMP,
-subcell limiter) over the whole grid of the workload.  Default workload: the
-Euler isentropic vortex, N=4, 256x256 periodic cells on [0,10]^2, limiter on,
-FP64.  The metric is DOF-updates per second, one DOF-update being one
-coefficient uh(v,i,j,cell) advanced by one step (nVar (N+1)^2 per cell).
+Metric: DOF-updates per second, one DOF-update being one coefficient
+uh(v,i,j,cell) advanced by one ADER-DG time step (nVar (N+1)^2 per cell), plus
+the p50/p99 time-to-solution of served requests.
+
+Default workload ("mix"): the seeded request mix -- each request draws its
+system uniformly from {advection-diffusion, Euler vortex, Euler 2D Riemann
+problem, Baer-Nunziato cylinder}, N uniformly from {2,3,4,5}, a square grid
+side log-uniformly from [32, 512] and initial-field parameters jittered by
++-10% (workloads.request_mix, seed 0); the first --requests of the 1024
+requests, each advanced --steps steps (fixed K).  One bench "step" is one time
+step of every request.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--workload mix|euler_vortex|euler_rp2d|bn_cylinder|ad_sine]
 
-Ours: `value` is device time (CUDA events on the library's stream, L2 flushed
-before every timed step) with the state resident in HBM; `e2e` is the same
-metric through aderdg_step_host with host buffers (host->device copy of uh,
-one step, device->host copy of uh, wall clock); `roofline` is the FP64-pipe
-roofline of the dominant kernel (the predictor).  The reference arm times the
-FP64 CPU restatement of the reference (oracle/) on this machine's host cores.
-Multi-GPU: requests are independent simulations, so N GPUs run N replicas
-(weak scaling, no collective).
+Ours:
+  value       batched FP32-mixed throughput, all requests resident in HBM in
+              their (system, N) batches, the batches stepping concurrently on
+              their own streams (wall clock between fully synchronised points;
+              the state, ~tens of GB, is far larger than L2);
+  plain_fp64  the plain single-instance FP64 GPU path on the same requests
+              (one simulation at a time, CUDA events per step, L2 flushed);
+  e2e         the served run through the public API: Poisson arrivals at
+              --rate req/s, initial fields projected and copied host->device on
+              admission, results copied device->host on completion; it reports
+              the p50/p99 time-to-solution;
+  roofline    the dominant kernel of the batched step (k_cells, FP64-pipe bound)
+              from its CUDA-event durations measured live;
+  cpu_baseline the FP64 CPU restatement of the reference (oracle/), one thread,
+              on a bounded sample of the same requests.
+The reference arm times the same restatement on the host (the Fortran
+reference cannot be built on these machines).  Multi-GPU: requests are
+independent, so N GPUs serve N replicas of the mix (weak scaling).
 """
 import argparse
 import json
@@ -34,6 +50,7 @@ sys.path.insert(0, os.path.join(REPO, "ader-dg_gb300"))
 
 METRIC = "batched DOF-updates/s vs plain FP64 GPU path on 1 GB300; p50/p99 solve latency"
 UNIT = "DOF-updates/s"
+NVAR = {0: 1, 1: 4, 2: 9}
 
 
 def parse():
@@ -42,40 +59,42 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="euler_vortex")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--workload", default="mix")
+    ap.add_argument("--requests", type=int, default=128)
+    ap.add_argument("--rate", type=float, default=100.0)
+    ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32"])
     ap.add_argument("--side", type=int, default=0)
+    ap.add_argument("--hbm-budget-gb", type=float, default=160.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
     return ap.parse_args()
 
 
-# ---------------------------------------------------------------- flop model
+# ---------------------------------------------------------------- work models
 def predictor_flops_per_cell(system, N):
-    """Floating-point operations the predictor kernel executes per cell
-    (fused multiply-add = 2, division = 1), from the loop structure of
-    predictor.cuh: the first Picard iteration evaluated once (constant in
-    time), N-1 full iterations, the last iteration contracted to the time
-    average, then the volume integral and the face extrapolation."""
-    P = N + 1
-    V = {0: 1, 1: 4, 2: 9}[system]
-    cflux = {0: 6, 1: 19, 2: 60}[system]            # pointwise flux (+ its gradient for AD)
-    extra = {0: 8 * P, 1: 0, 2: 8 * P + 12 + 2 * V}[system]  # AD/BN gradients, BN NCP and its update
-    contract = 4 * P * V                              # one time level: 2P FMAs per variable
+    """Floating-point operations the predictor executes per cell (FMA = 2,
+    division = 1) from the loop structure of predictor.cuh: the first Picard
+    iteration once (constant in time), N-1 full iterations, the last one
+    contracted to the time average, then volume integral and face extrapolation."""
+    P, V = N + 1, NVAR[system]
+    cflux = {0: 6, 1: 19, 2: 60}[system]
+    extra = {0: 8 * P, 1: 0, 2: 8 * P + 12 + 2 * V}[system]
+    contract = 4 * P * V
     it1 = cflux + contract + extra + 3 * P * V
     mid = P * (cflux + contract + extra) + P * V + 2 * P * P * V
     last = P * (cflux + 4 * V + contract + extra) + V + 2 * P * V
     vol = V * (4 * P + 3)
-    per_node = it1 + max(N - 1, 0) * mid + last + vol
-    faces = 4 * P * V * 2 * 2 * P
-    return P * P * per_node + faces
+    return P * P * (it1 + max(N - 1, 0) * mid + last + vol) + 4 * P * V * 2 * 2 * P
 
 
-def predictor_bytes_per_cell(system, N, rbytes):
-    P = N + 1
-    V = {0: 1, 1: 4, 2: 9}[system]
-    bnd = 4 * P * V * rbytes * (3 if system == 0 else 2)
-    return 8 * V * P * P * 2 + bnd  # read uh, write duh, write face states
+def cells_fp64_flops_per_cell(system, N):
+    """FP64 operations of the cell kernel per cell: the sum-factorised subcell
+    and Gauss-Lobatto projections of the DMP (y then x pass, one FMA per term;
+    none for advection-diffusion) and the update uh += dt duh / (w_i w_j)."""
+    P, V, S = N + 1, NVAR[system], 2 * N + 1
+    proj = 0 if system == 0 else 2 * V * P * (S * P + P * P + S * S + P * P)
+    return proj + 3 * V * P * P
 
 
 # ---------------------------------------------------------------- clocks
@@ -85,17 +104,14 @@ class ClockSampler:
              "clocks_event_reasons.sw_power_cap"
 
     def __init__(self, index=0):
-        self.samples = []
-        self.proc = None
-        self.index = index
+        self.samples, self.proc, self.index = [], None, index
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
-            self.t.start()
+            threading.Thread(target=self._read, daemon=True).start()
         except OSError:
             self.proc = None
         return self
@@ -115,16 +131,19 @@ class ClockSampler:
     def summary(self):
         if not self.samples:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
-        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [v for v in (num(s[1]) for s in self.samples) if v is not None]
+        mx = [v for v in (num(s[2]) for s in self.samples) if v is not None]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = set()
-        for s in self.samples:
-            for k, n in enumerate(names):
-                if len(s) > 5 + k and s[5 + k].lower().startswith("active"):
-                    reasons.add(n)
+        reasons = sorted({n for s in self.samples for k, n in enumerate(names)
+                          if len(s) > 5 + k and s[5 + k].lower().startswith("active")})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(self.samples)}
 
 
 # ---------------------------------------------------------------- helpers
@@ -154,100 +173,229 @@ def allmax(dist, x):
     return float(t.item())
 
 
-def setup_solver(aderdg, name, side, prec):
-    cfg, ic, params, tend = aderdg.workloads.make(name, side=side or None, precision=prec)
-    uh, lh = aderdg.project_initial_condition(cfg, ic, params)
-    s = aderdg.Solver(cfg)
-    s.upload(uh)
-    if cfg.limiter:
-        s.init_limiter(lh)
-    return s, cfg, uh, lh, tend
+def mix_specs(n):
+    import aderdg
+    return aderdg.workloads.request_mix(1024, seed=0)[:n]
 
 
-def cpu_oracle_rate(name, side, steps_budget_s=20.0, max_steps=5, threads=1):
-    """FP64 CPU restatement of the reference timed on this host: the first
-    `max_steps` steps of the workload (bounded to ~steps_budget_s)."""
+def spec_config(aderdg, spec, precision):
+    cfg, ic, _, _ = aderdg.workloads.make(spec["name"], side=spec["side"], N=spec["N"], precision=precision)
+    return cfg, ic
+
+
+def oracle_rate(specs, budget_s=20.0, side_cap=48, steps=1):
+    """DOF-updates/s of the FP64 oracle, one thread, over `specs` with grid
+    sides capped at side_cap (same N, system and cell count per side; the
+    cost per DOF does not depend on the number of cells), bounded by budget_s."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import aderdg
     import pyoracle as po
-    cfg, ic, params, tend = aderdg.workloads.make(name, side=side or None)
-    oc = po.make_config(cfg.system, cfg.N, cfg.imax, cfg.jmax, xl=cfg.xl, xr=cfg.xr, bc=cfg.bc, cfl=cfg.cfl,
-                        gamma=cfg.gamma, gamma_s=cfg.gamma_s, gamma_g=cfg.gamma_g, pi_s=cfg.pi_s, pi_g=cfg.pi_g,
-                        cx=cfg.cx, cy=cfg.cy, a=cfg.a, ad_flux_mode=cfg.ad_flux_mode, limiter=cfg.limiter)
-    o = po.Oracle(oc)
-    uh, lh = o.project_ic(ic, params)
-    o.set(po.UH, uh)
-    if cfg.limiter:
-        o.init_limiter(lh)
-    t, done, el = 0.0, 0, 0.0
-    while done < max_steps and el < steps_budget_s:
+    dofs, el, used = 0, 0.0, 0
+    for spec in specs:
+        if el > budget_s:
+            break
+        cfg, ic, _, _ = aderdg.workloads.make(spec["name"], side=min(spec["side"], side_cap), N=spec["N"])
+        oc = po.make_config(cfg.system, cfg.N, cfg.imax, cfg.jmax, xl=cfg.xl, xr=cfg.xr, bc=cfg.bc, cfl=cfg.cfl,
+                            gamma=cfg.gamma, gamma_s=cfg.gamma_s, gamma_g=cfg.gamma_g, pi_s=cfg.pi_s,
+                            pi_g=cfg.pi_g, cx=cfg.cx, cy=cfg.cy, a=cfg.a, ad_flux_mode=cfg.ad_flux_mode,
+                            limiter=cfg.limiter)
+        o = po.Oracle(oc)
+        uh, lh = o.project_ic(ic, spec["params"])
+        o.set(po.UH, uh)
+        if cfg.limiter and cfg.system != 0:
+            o.init_limiter(lh)
+        t = 0.0
         t0 = time.perf_counter()
-        t, _, _ = o.step(t, tend)
+        for _ in range(steps):
+            t, _, _ = o.step(t, spec["tend"])
         el += time.perf_counter() - t0
-        done += 1
-    return cfg.dofs * done / el, done, el, cfg
+        dofs += cfg.dofs * steps
+        used += 1
+    return dofs / el, used, el
 
 
 # ---------------------------------------------------------------- arms
+def _oracle_worker(job):
+    """One process of the reference arm: oracle steps of one request."""
+    spec, side_cap, steps = job
+    rate, _, el = oracle_rate([spec], budget_s=1e9, side_cap=side_cap, steps=steps)
+    return rate
+
+
 def run_reference(args):
+    """The FP64 CPU restatement on all host cores: one process per core, each
+    stepping one request of the mix (requests are independent)."""
+    import multiprocessing as mp
     dist, rank, ws, _ = dist_init()
     if rank != 0:
         return
-    # each step is one full oracle step of a bounded patch of the workload
-    # (same N and cell size; the per-DOF cost does not depend on the grid size)
-    import aderdg
-    cfg, _, _, _ = aderdg.workloads.make(args.workload, side=args.side or None)
-    side = cfg.imax
-    per_dof_s = 1.0 / 2.5e6
-    budget = 150.0
-    while side > 16 and (args.steps + args.warmup) * cfg.nvar * cfg.P ** 2 * side * side * per_dof_s > budget:
-        side //= 2
-    sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import pyoracle as po
-    c2, ic, params, tend = aderdg.workloads.make(args.workload, side=side)
-    scale = side / cfg.imax
-    c2.xr = (c2.xl[0] + (cfg.xr[0] - cfg.xl[0]) * scale, c2.xl[1] + (cfg.xr[1] - cfg.xl[1]) * scale)
-    oc = po.make_config(c2.system, c2.N, c2.imax, c2.jmax, xl=c2.xl, xr=c2.xr, bc=c2.bc, cfl=c2.cfl,
-                        gamma=c2.gamma, gamma_s=c2.gamma_s, gamma_g=c2.gamma_g, pi_s=c2.pi_s, pi_g=c2.pi_g,
-                        cx=c2.cx, cy=c2.cy, a=c2.a, ad_flux_mode=c2.ad_flux_mode, limiter=c2.limiter)
-    o = po.Oracle(oc)
-    uh, lh = o.project_ic(ic, params)
-    o.set(po.UH, uh)
-    if c2.limiter:
-        o.init_limiter(lh)
-    t = 0.0
-    for _ in range(args.warmup):
-        t, _, _ = o.step(t, tend)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        t, _, _ = o.step(t, tend)
-    el = time.perf_counter() - t0
-    val = c2.dofs * args.steps / el
-    sample = "%d steps of a %dx%d patch (cell size of the %dx%d workload), single thread, FP64" % (
-        args.steps, side, side, cfg.imax, cfg.jmax)
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        if args.workload == "mix":
+            specs = mix_specs(args.requests)
+            jobs = lambda k: [(specs[(cores * k + q) % len(specs)], 40, 2) for q in range(cores)]  # noqa: E731
+            sample = ("per step: two oracle steps of each of %d requests of the mix at once (one per core, rotating "
+                      "through the first %d), grid sides capped at 40; FP64" % (cores, args.requests))
+            cfg_desc = {"workload": "mix", "requests": args.requests, "steps_per_request": args.steps}
+        else:
+            import aderdg
+            cfg, ic, params, tend = aderdg.workloads.make(args.workload, side=args.side or None)
+            spec = dict(name=args.workload, N=cfg.N, side=cfg.imax, params=params, tend=tend)
+            jobs = lambda k: [(spec, 64, 2)] * cores  # noqa: E731
+            sample = "per step: two oracle steps of a 64x64 grid of the workload on each of %d cores; FP64" % cores
+            cfg_desc = {"workload": args.workload, "N": cfg.N, "grid": [cfg.imax, cfg.jmax]}
+        for k in range(args.warmup):
+            pool.map(_oracle_worker, [(j[0], 16, 1) for j in jobs(k)])
+        rates = []
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            # cores step their requests at once: the aggregate rate is the sum of theirs
+            rates.append(sum(pool.map(_oracle_worker, jobs(k))))
+        el = time.perf_counter() - t0
+    val = float(np.mean(rates))
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": el / max(args.steps, 1) * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic: projected initial field of the workload (deterministic)",
-            "config": workload_config(cfg, args),
-            "cpu_baseline": {"value": val, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+            "data": "synthetic: projected initial fields of the seeded request mix (deterministic)",
+            "config": cfg_desc,
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def workload_config(cfg, args):
-    names = {0: "advection-diffusion", 1: "euler", 2: "baer-nunziato"}
-    return {"workload": args.workload, "system": names[cfg.system], "N": cfg.N, "grid": [cfg.imax, cfg.jmax],
-            "precision": args.precision, "limiter": bool(cfg.limiter), "global_batch": 1,
-            "l2": "flushed before every timed step", "parallelism": "replicas" if args.gpus > 1 else "single"}
-
-
-def run_ours(args):
-    dist, rank, ws, lr = dist_init()
-    import aderdg
-    aderdg.build()
+def run_mix(args, aderdg, dist, rank, ws, lr):
     prec = aderdg.FP32_MIXED if args.precision == "fp32" else aderdg.FP64
-    s, cfg, uh, lh, tend = setup_solver(aderdg, args.workload, args.side, prec)
+    specs = mix_specs(args.requests)
+    K, W = args.steps, args.warmup
+    # ---- batched, resident: every request admitted into its (system, N) batch
+    groups, members = {}, []
+    need = {}
+    for spec in specs:
+        cfg, ic = spec_config(aderdg, spec, prec)
+        key = (cfg.system, cfg.N)
+        need[key] = need.get(key, 0) + aderdg.Batch.units(cfg)
+        members.append((spec, cfg, ic, key))
+    for key, units in need.items():
+        lim = 0 if key[0] == aderdg.SYS_ADVDIFF else 1
+        groups[key] = aderdg.Batch(key[0], key[1], prec, lim, capacity_units=units + 16,
+                                   max_instances=sum(1 for m in members if m[3] == key) + 1)
+    total_dofs = 0
+    bytes_in = 0
+    slots = []
+    for spec, cfg, ic, key in members:
+        uh, lh = aderdg.project_initial_condition(cfg, ic, spec["params"])
+        lim = cfg.limiter and cfg.system != aderdg.SYS_ADVDIFF
+        slot = groups[key].admit(cfg, uh, lh if lim else None, spec["tend"], W + K + 1)
+        assert slot is not None
+        slots.append((key, slot, cfg.dofs))
+        total_dofs += cfg.dofs
+        bytes_in += uh.nbytes + (lh.nbytes if lim else 0)
+    for g in groups.values():
+        g.launch(W)
+    for g in groups.values():
+        g.sync()
+    steps0 = [groups[key].query(slot)["steps"] for key, slot, _ in slots]
+    barrier(dist)
+    with ClockSampler(lr) as clk:
+        t0 = time.perf_counter()
+        for g in groups.values():
+            g.launch(K)
+        for g in groups.values():
+            g.sync()
+        batched_s = time.perf_counter() - t0
+    batched_s = allmax(dist, batched_s)
+    barrier(dist)
+    # DOF-updates actually done in the timed region (a request that reaches its end time stops early)
+    updates = sum(d * (groups[key].query(slot)["steps"] - s0) for (key, slot, d), s0 in zip(slots, steps0))
+    value = updates * ws / batched_s
+    # dominant kernel: per-launch device times of one more (eager) step of every group
+    phase_tot = {}
+    cells_flops = 0.0
+    for key, g in groups.items():
+        ph = g.profile()
+        for k, v in ph.items():
+            phase_tot[k] = phase_tot.get(k, 0.0) + v
+    for spec, cfg, ic, key in members:
+        cells_flops += cells_fp64_flops_per_cell(cfg.system, cfg.N) * cfg.cells
+    dev_bytes = sum(g.info()["device_bytes"] for g in groups.values())
+    for g in groups.values():
+        g.close()
+    if rank != 0:
+        return None
+    fp64_peak, fp32_peak = aderdg.probe_peaks()
+    cells_ms = phase_tot.get("cells", 0.0)
+    dominant = max((k for k in phase_tot if k not in ("begin", "end")), key=lambda k: phase_tot[k])
+    ach = cells_flops / (cells_ms * 1e-3) / 1e9 if cells_ms > 0 else None
+    roof = {"bound": "fp64", "kernel": "k_cells (all (system, N) groups of the mix)", "achieved": ach,
+            "peak": fp64_peak, "unit": "GFLOP/s", "frac": (ach / fp64_peak) if ach else None,
+            "peak_source": "measured by aderdg_probe_peaks (dependent-FMA microkernel on this GPU); "
+                           "MEASURED_PEAKS.json carries no FP64 non-tensor figure",
+            "flops_per_launch": cells_flops, "launch_ms": cells_ms, "dominant_phase": dominant,
+            "phase_ms_one_step": phase_tot, "traffic": None}
+    try:
+        with open(os.path.join(REPO, "profiles", "traffic.json")) as fh:
+            tr = json.load(fh)
+        per = tr.get("k_cells_fp32mixed_bytes_per_dof")
+        if per:
+            roof["traffic"] = per * total_dofs
+            roof["traffic_note"] = "DRAM bytes per DOF of k_cells from one ncu capture (profiles/), times the mix's DOFs"
+    except (OSError, ValueError):
+        pass
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
+            "ms_per_step": batched_s / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64" if prec == aderdg.FP32_MIXED else "f64",
+            "data": "synthetic: seeded request mix (request_mix seed 0), projected initial fields; no dataset",
+            "config": {"workload": "mix (served/batched request mix)", "requests": len(specs),
+                       "steps_per_request": K, "dofs_per_step": total_dofs,
+                       "dof_updates_timed": updates, "groups": len(groups),
+                       "precision": args.precision, "l2": "state (%.1f GB on device) far larger than L2" %
+                       (dev_bytes / 1e9), "parallelism": "replicas" if ws > 1 else "single",
+                       "arrival_rate_per_s": args.rate},
+            "roofline": roof, "clocks": clk.summary(),
+            "gpu_launches": sum(7 if k[0] != 0 else 5 for k in groups) * K}
+    return line
+
+
+def run_plain_fp64(aderdg, specs, steps):
+    """The plain single-instance FP64 path: one simulation at a time, CUDA
+    events per step, L2 flushed before every timed step."""
+    dofs, ms = 0, 0.0
+    for spec in specs:
+        cfg, ic = spec_config(aderdg, spec, aderdg.FP64)
+        uh, lh = aderdg.project_initial_condition(cfg, ic, spec["params"])
+        s = aderdg.Solver(cfg)
+        s.upload(uh)
+        if cfg.limiter and cfg.system != aderdg.SYS_ADVDIFF:
+            s.init_limiter(lh)
+        t, _, _ = s.step(0.0, spec["tend"])
+        t, st = s.time_steps(t, spec["tend"], steps, flush_l2=True)
+        dofs += cfg.dofs * steps
+        ms += float(st.sum())
+        s.close()
+    return dofs / (ms * 1e-3), ms
+
+
+def run_served(aderdg, args, specs, prec):
+    srv = aderdg.serving.Server(hbm_budget_bytes=args.hbm_budget_gb * 1e9, precision=prec, sync_every=4)
+    rep = srv.run(specs, rate=args.rate, seed=0, max_steps=args.steps)
+    done = rep.pop("requests_done")
+    srv.close()
+    h2d = sum(r.dofs * 8 for r in done)
+    lim_bytes = sum(r.dofs * 8 * ((2 * r.N + 1) ** 2) // ((r.N + 1) ** 2) for r in done
+                    if r.cfg.limiter and r.cfg.system != aderdg.SYS_ADVDIFF)
+    return rep, h2d + lim_bytes, sum(r.dofs * 8 for r in done)
+
+
+def run_single(args, aderdg, dist, rank, ws, lr):
+    """A plain named workload on one simulation (not the headline)."""
+    prec = aderdg.FP32_MIXED if args.precision == "fp32" else aderdg.FP64
+    cfg, ic, params, tend = aderdg.workloads.make(args.workload, side=args.side or None, precision=prec)
+    uh, lh = aderdg.project_initial_condition(cfg, ic, params)
+    s = aderdg.Solver(cfg)
+    s.upload(uh)
+    if cfg.limiter and cfg.system != aderdg.SYS_ADVDIFF:
+        s.init_limiter(lh)
     t = 0.0
     for _ in range(args.warmup):
         t, _, _ = s.step(t, tend)
@@ -255,88 +403,74 @@ def run_ours(args):
     with ClockSampler(lr) as clk:
         t, ms = s.time_steps(t, tend, args.steps, flush_l2=True)
     total_ms = allmax(dist, float(ms.sum()))
-    barrier(dist)
-    dofs_total = cfg.dofs * args.steps * ws
-    value = dofs_total / (total_ms * 1e-3)
-    # per-phase device times of one step (predictor = the dominant kernel)
     t, phases = s.profile_step(t, tend)
-    launches = 7 if cfg.limiter else 5
     if rank != 0:
-        return
-    info = s.info()
-    p50, p99 = float(np.percentile(ms, 50)), float(np.percentile(ms, 99))
+        return None
     fp64_peak, fp32_peak = aderdg.probe_peaks()
     fpeak = fp32_peak if prec == aderdg.FP32_MIXED else fp64_peak
     flops = predictor_flops_per_cell(cfg.system, cfg.N) * cfg.cells
-    pred_ms = phases["predictor"]
-    achieved = flops / (pred_ms * 1e-3) / 1e9
-    peaks = {}
-    try:
-        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
-            peaks = json.load(fh)
-    except OSError:
-        pass
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    rb = 4 if prec == aderdg.FP32_MIXED else 8
-    pbytes = predictor_bytes_per_cell(cfg.system, cfg.N, rb) * cfg.cells
-    roof = {"bound": "fp32" if prec == aderdg.FP32_MIXED else "fp64", "kernel": "k_predictor",
-            "achieved": achieved, "peak": fpeak, "unit": "GFLOP/s", "frac": achieved / fpeak,
-            "peak_source": "measured by aderdg_probe_peaks (dependent-FMA microkernel, this GPU); "
-                           "MEASURED_PEAKS.json carries no FP64/FP32 non-tensor figure",
-            "flops_per_launch": flops, "launch_ms": pred_ms, "traffic": None,
-            "hbm": {"algorithmic_bytes": pbytes, "achieved_gbs": pbytes / (pred_ms * 1e-3) / 1e9,
-                    "peak_gbs": hbm_peak, "frac": pbytes / (pred_ms * 1e-3) / 1e9 / hbm_peak,
-                    "peak_source": "MEASURED_PEAKS.json hbm_gbs"}}
-    try:
-        with open(os.path.join(REPO, "profiles", "traffic.json")) as fh:
-            tr = json.load(fh).get("%s_N%d_%s" % (args.workload, cfg.N, args.precision))
-            if tr:
-                roof["traffic"] = tr["bytes_per_cell"] * cfg.cells
-    except (OSError, ValueError):
-        pass
-    # e2e: the drop-in step with host buffers (pinned via torch when available)
+    ach = flops / (phases["predictor"] * 1e-3) / 1e9
     host = np.empty(cfg.dofs, dtype=np.float64)
-    try:
-        import torch
-        pinned = torch.empty(cfg.dofs, dtype=torch.float64).pin_memory()
-        host = pinned.numpy()
-    except Exception:
-        pass
     s.download_into(host)
-    e2e_steps = max(3, min(args.steps, 10))
+    n_e = max(3, min(args.steps, 10))
     t_e = time.perf_counter()
-    for _ in range(e2e_steps):
+    for _ in range(n_e):
         t, _, _ = s.step_host(host, t, tend)
     e2e_s = time.perf_counter() - t_e
-    e2e = {"value": cfg.dofs * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": cfg.dofs * 8,
-           "d2h_bytes_per_step": cfg.dofs * 8, "steps": e2e_steps, "api": "aderdg_step_host"}
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if prec == aderdg.FP32_MIXED else "f64",
-            "data": "synthetic: projected initial field of the workload (deterministic)",
-            "config": workload_config(cfg, args),
-            "latency_ms": {"p50": p50, "p99": p99, "what": "device time per time step"},
-            "phase_ms": phases, "gpu_launches": launches * args.steps,
-            "roofline": roof, "e2e": e2e, "clocks": clk.summary(),
-            "limited_cells": info["n_limited"], "dt": info["dt"]}
-    if cfg.limiter and tend > 0:
-        line["time_to_solution_s_extrapolated"] = tend / info["dt"] * total_ms / args.steps * 1e-3
-    if not args.no_variants and args.workload == "euler_vortex" and prec == aderdg.FP64:
-        s2, c2, _, _, tend2 = setup_solver(aderdg, args.workload, args.side, aderdg.FP32_MIXED)
-        t2 = 0.0
-        for _ in range(args.warmup):
-            t2, _, _ = s2.step(t2, tend2)
-        t2, ms2 = s2.time_steps(t2, tend2, args.steps, flush_l2=True)
-        line["fp32_mixed"] = {"value": c2.dofs * args.steps / (ms2.sum() * 1e-3), "unit": UNIT,
-                              "ms_per_step": float(ms2.mean()), "speedup_vs_fp64": float(ms.sum() / ms2.sum())}
-        s2.close()
-    if not args.no_cpu_baseline:
-        rate, done, el, _ = cpu_oracle_rate(args.workload, args.side, steps_budget_s=20.0, max_steps=3)
-        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
-                                "sample": "first %d steps of the full %dx%d workload (%.1f s), FP64 oracle, "
-                                          "one thread" % (done, cfg.imax, cfg.jmax, el)}
-    print(json.dumps(line), flush=True)
+    info = s.info()
     s.close()
+    return {"metric": METRIC, "value": cfg.dofs * args.steps * ws / (total_ms * 1e-3), "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64" if prec == aderdg.FP32_MIXED else "f64",
+            "data": "synthetic: projected initial field of the workload (deterministic)",
+            "config": {"workload": args.workload, "N": cfg.N, "grid": [cfg.imax, cfg.jmax],
+                       "precision": args.precision, "l2": "flushed before every timed step"},
+            "latency_ms": {"p50": float(np.percentile(ms, 50)), "p99": float(np.percentile(ms, 99))},
+            "phase_ms": phases, "gpu_launches": (7 if cfg.limiter else 5) * args.steps,
+            "roofline": {"bound": "fp32" if prec == aderdg.FP32_MIXED else "fp64", "kernel": "k_predictor",
+                         "achieved": ach, "peak": fpeak, "unit": "GFLOP/s", "frac": ach / fpeak, "traffic": None,
+                         "peak_source": "aderdg_probe_peaks on this GPU"},
+            "e2e": {"value": cfg.dofs * n_e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": cfg.dofs * 8,
+                    "d2h_bytes_per_step": cfg.dofs * 8, "api": "aderdg_step_host"},
+            "clocks": clk.summary(), "limited_cells": info["n_limited"]}
+
+
+def run_ours(args):
+    dist, rank, ws, lr = dist_init()
+    import aderdg
+    aderdg.build()
+    if args.workload != "mix":
+        line = run_single(args, aderdg, dist, rank, ws, lr)
+        if line:
+            print(json.dumps(line), flush=True)
+        return
+    line = run_mix(args, aderdg, dist, rank, ws, lr)
+    if rank != 0:
+        return
+    prec = aderdg.FP32_MIXED if args.precision == "fp32" else aderdg.FP64
+    specs = mix_specs(args.requests)
+    if not args.no_serve:
+        rep, h2d, d2h = run_served(aderdg, args, specs, prec)
+        line["e2e"] = {"value": rep["dof_updates_per_s"], "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
+                       "d2h_bytes_per_step": d2h / args.steps,
+                       "api": "aderdg_batch_admit / launch / sync / download / release (continuous batching)",
+                       "makespan_s": rep["makespan_s"], "requests": rep["requests"]}
+        line["latency_s"] = {"p50": rep["tts_p50_s"], "p99": rep["tts_p99_s"],
+                             "what": "time to solution, arrival to result on the host, Poisson arrivals at %.0f/s"
+                                     % args.rate}
+    if not args.no_plain:
+        plain_steps = min(args.steps, 10)
+        rate, ms = run_plain_fp64(aderdg, specs, plain_steps)
+        line["plain_fp64"] = {"value": rate, "unit": UNIT, "steps_per_request": plain_steps,
+                              "what": "single-instance FP64 path, one request at a time, same requests"}
+        line["batched_over_plain_fp64"] = line["value"] / rate
+    if not args.no_cpu_baseline:
+        rate, used, el = oracle_rate(specs, budget_s=20.0, side_cap=48)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": "one FP64 oracle step of each of the first %d requests of the mix with grid "
+                                          "sides capped at 48 (%.1f s), one thread" % (used, el)}
+    print(json.dumps(line), flush=True)
 
 
 def main():

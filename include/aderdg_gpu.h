@@ -241,6 +241,9 @@ int aderdg_batch_sync(aderdg_batch* b, int* n_running);
 int aderdg_batch_query(aderdg_batch* b, int slot, double* time, double* dt, long* steps, int* done);
 int aderdg_batch_download(aderdg_batch* b, int slot, double* uh);
 int aderdg_batch_info(aderdg_batch* b, long* used_units, long* capacity_units, long* device_bytes, int* n_instances);
+/* One fused step of the batch, eager, with CUDA events between its launches:
+ * device ms of each in phase_ms[7] (as aderdg_profile_step). */
+int aderdg_batch_profile(aderdg_batch* b, double* phase_ms);
 const char* aderdg_batch_last_error(aderdg_batch* b);
 
 /* ---- host setup helpers (initial fields; not on the hot path) ---- */
