@@ -157,7 +157,7 @@ int launch_step(aderdg_ctx* c) {
   if (r) return r;
   if (c->limiter) {
     CK(c, c->kt->mark(c->args, c->stream));
-    CK(c, c->kt->subcell(c->args, c->ops64.data(), c->fc, c->subcell_grid, c->stream));
+    CK(c, c->kt->subcell(c->args, c->ops64.data(), c->fc, c->subcell_grid, c->fp32, c->stream));
   }
   CK(c, control(c, aderdg::kCtlEnd));
   return ADERDG_OK;
@@ -345,7 +345,7 @@ int aderdg_create(const aderdg_config* cfg, aderdg_ctx** out) {
     c->ops32.assign(kt->ops32_size, 0);
     kt->make_ops32(c->ops, c->ops32.data());
   }
-  if (c->limiter) c->subcell_grid = kt->subcell_grid(c->num_sms);
+  if (c->limiter) c->subcell_grid = kt->subcell_grid(c->num_sms, c->fp32);
   // set kernel attributes now, outside any later stream capture
   {
     BatchArgs z = a;
@@ -537,7 +537,7 @@ int aderdg_limiter(aderdg_ctx* c) {
   if (!c->pending) return fail(c, ADERDG_ESTATE, "run aderdg_element_update first");
   CK(c, cudaMemsetAsync(c->args.list_count, 0, sizeof(int), c->stream));
   CK(c, c->kt->mark(c->args, c->stream));
-  CK(c, c->kt->subcell(c->args, c->ops64.data(), c->fc, c->subcell_grid, c->stream));
+  CK(c, c->kt->subcell(c->args, c->ops64.data(), c->fc, c->subcell_grid, c->fp32, c->stream));
   CK(c, control(c, aderdg::kCtlEnd));
   c->pending = false;
   return pull_state(c);
@@ -670,7 +670,7 @@ int aderdg_profile_step(aderdg_ctx* c, double* time, double tend, double* phase_
   CK(c, cudaEventRecord(ev[4], c->stream));
   if (c->limiter) CK(c, c->kt->mark(c->args, c->stream));
   CK(c, cudaEventRecord(ev[5], c->stream));
-  if (c->limiter) CK(c, c->kt->subcell(c->args, c->ops64.data(), c->fc, c->subcell_grid, c->stream));
+  if (c->limiter) CK(c, c->kt->subcell(c->args, c->ops64.data(), c->fc, c->subcell_grid, c->fp32, c->stream));
   CK(c, cudaEventRecord(ev[6], c->stream));
   CK(c, control(c, aderdg::kCtlEnd));
   CK(c, cudaEventRecord(ev[7], c->stream));
@@ -721,20 +721,20 @@ int aderdg_get_array(aderdg_ctx* c, int which, void* out) {
   const BatchArgs& a = c->args;
   const void* src = nullptr;
   size_t esz = sizeof(double);
-  bool narrow = false;  // FP32 storage widened to double
+  bool narrow = false;  // FP32 storage (the mixed mode's intermediates) widened to double
   switch (which) {
     case ADERDG_A_UH: src = a.uh[par]; break;
-    case ADERDG_A_DUH: src = a.duh; break;
+    case ADERDG_A_DUH: src = a.duh; narrow = c->fp32; break;
     case ADERDG_A_QHI: src = a.qhi; break;
     case ADERDG_A_FHI: src = a.fhi; break;
     case ADERDG_A_SHI: src = a.shi; break;
     case ADERDG_A_QBND: src = a.qbnd; narrow = c->fp32; break;
     case ADERDG_A_FBND:
     case ADERDG_A_GRADQBND: src = a.fbnd; narrow = c->fp32; break;
-    case ADERDG_A_FU: src = a.fu; break;
-    case ADERDG_A_GU: src = a.gu; break;
-    case ADERDG_A_FP: src = a.fp; break;
-    case ADERDG_A_GP: src = a.gp; break;
+    case ADERDG_A_FU: src = a.fu; narrow = c->fp32; break;
+    case ADERDG_A_GU: src = a.gu; narrow = c->fp32; break;
+    case ADERDG_A_FP: src = a.fp; narrow = c->fp32; break;
+    case ADERDG_A_GP: src = a.gp; narrow = c->fp32; break;
     case ADERDG_A_LH: src = a.lh[par]; break;
     case ADERDG_A_RECOMPUTE: src = a.recompute; esz = sizeof(int); break;
     case ADERDG_A_STATUS: src = a.status[par]; esz = sizeof(int); break;
@@ -775,17 +775,17 @@ int aderdg_set_array(aderdg_ctx* c, int which, const void* in) {
   bool narrow = false;
   switch (which) {
     case ADERDG_A_UH: dst = a.uh[par]; break;
-    case ADERDG_A_DUH: dst = a.duh; break;
+    case ADERDG_A_DUH: dst = a.duh; narrow = c->fp32; break;
     case ADERDG_A_QHI: dst = a.qhi; break;
     case ADERDG_A_FHI: dst = a.fhi; break;
     case ADERDG_A_SHI: dst = a.shi; break;
     case ADERDG_A_QBND: dst = a.qbnd; narrow = c->fp32; break;
     case ADERDG_A_FBND:
     case ADERDG_A_GRADQBND: dst = a.fbnd; narrow = c->fp32; break;
-    case ADERDG_A_FU: dst = a.fu; break;
-    case ADERDG_A_GU: dst = a.gu; break;
-    case ADERDG_A_FP: dst = a.fp; break;
-    case ADERDG_A_GP: dst = a.gp; break;
+    case ADERDG_A_FU: dst = a.fu; narrow = c->fp32; break;
+    case ADERDG_A_GU: dst = a.gu; narrow = c->fp32; break;
+    case ADERDG_A_FP: dst = a.fp; narrow = c->fp32; break;
+    case ADERDG_A_GP: dst = a.gp; narrow = c->fp32; break;
     case ADERDG_A_LH: dst = a.lh[par]; break;
     case ADERDG_A_RECOMPUTE: dst = a.recompute; esz = sizeof(int); break;
     case ADERDG_A_STATUS: dst = a.status[par]; esz = sizeof(int); break;

@@ -150,7 +150,7 @@ int blaunch_step(aderdg_batch* b) {
   BK(b, b->kt->cells(a, b->ops64.data(), fp32, b->stream));
   if (b->limiter) {
     BK(b, b->kt->mark(a, b->stream));
-    BK(b, b->kt->subcell(a, b->ops64.data(), b->fc, b->subcell_grid, b->stream));
+    BK(b, b->kt->subcell(a, b->ops64.data(), b->fc, b->subcell_grid, b->precision ? 1 : 0, b->stream));
   }
   BK(b, bcontrol(b, aderdg::kCtlEnd, -1));
   return ADERDG_OK;
@@ -302,7 +302,7 @@ int aderdg_batch_create(int system, int N, int precision, int limiter, long capa
     b->ops32.assign(kt->ops32_size, 0);
     kt->make_ops32(b->ops, b->ops32.data());
   }
-  if (b->limiter) b->subcell_grid = kt->subcell_grid(b->num_sms);
+  if (b->limiter) b->subcell_grid = kt->subcell_grid(b->num_sms, b->precision ? 1 : 0);
   {  // kernel attributes before any capture
     BatchArgs z = a;
     z.ncells = z.nfx = z.nfy = 0;
@@ -532,7 +532,7 @@ int aderdg_batch_profile(aderdg_batch* b, double* phase_ms) {
   BK(b, cudaEventRecord(ev[4], b->stream));
   if (b->limiter) BK(b, b->kt->mark(a, b->stream));
   BK(b, cudaEventRecord(ev[5], b->stream));
-  if (b->limiter) BK(b, b->kt->subcell(a, b->ops64.data(), b->fc, b->subcell_grid, b->stream));
+  if (b->limiter) BK(b, b->kt->subcell(a, b->ops64.data(), b->fc, b->subcell_grid, b->precision ? 1 : 0, b->stream));
   BK(b, cudaEventRecord(ev[6], b->stream));
   BK(b, bcontrol(b, aderdg::kCtlEnd, -1));
   BK(b, cudaEventRecord(ev[7], b->stream));

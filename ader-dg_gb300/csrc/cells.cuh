@@ -39,26 +39,28 @@ __device__ __forceinline__ double okey_inv(long long k) {
 // Subcell / Gauss-Lobatto projections of one cell (get_subcell_data and
 // get_lobatto_data, Euler/limiter.f90:12-68), sum-factorised y then x with
 // the reference's summation order.  A "team" of nr threads with rank r works
-// on one cell; the caller synchronises between the two passes.
-template <int N, int V>
+// on one cell; the caller synchronises between the two passes.  The operators
+// come from shared memory: lim = uh2lim (s,k) at [s + S*k], lob = uh2lob (q,k)
+// at [q + P*k].  T = double: exact-order mul then add, or one fused
+// multiply-add per term (kFast); T = float: fused multiply-adds (FP32-mixed).
+template <int N, int V, class T>
 struct Proj {
   static constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1;
-  // acc + a*b: exact-order mul then add, or one fused multiply-add (kFast)
   template <bool kFast>
-  __device__ __forceinline__ static double madd(double acc, double a, double b) {
+  __device__ __forceinline__ static T madd(T acc, T a, T b) {
     if constexpr (kFast) return fma(a, b, acc);
     else return acc + a * b;
   }
   // y pass: LY[v][s][i] = sum_k U[v][i + P k] uh2lim(s,k); LB[v][s][i] likewise with uh2lob
   template <bool kFast = false>
-  __device__ static void ypass(const double* U, double* LY, double* LB, const DevOps<N, double>& op, int r, int nr) {
+  __device__ static void ypass(const T* U, T* LY, T* LB, const T* lim, const T* lob, int r, int nr) {
     for (int idx = r; idx < P * S; idx += nr) {
       const int ii = idx % P, s = idx / P;
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        double acc = 0.0;
+        T acc = 0;
 #pragma unroll
-        for (int k = 0; k < P; ++k) acc = madd<kFast>(acc, U[v * P2 + ii + P * k], op.uh2lim[s + S * k]);
+        for (int k = 0; k < P; ++k) acc = madd<kFast>(acc, U[v * P2 + ii + P * k], lim[s + S * k]);
         LY[(v * S + s) * P + ii] = acc;
       }
     }
@@ -66,44 +68,44 @@ struct Proj {
       const int ii = idx % P, s = idx / P;
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        double acc = 0.0;
+        T acc = 0;
 #pragma unroll
-        for (int k = 0; k < P; ++k) acc = madd<kFast>(acc, U[v * P2 + ii + P * k], op.uh2lob[s + P * k]);
+        for (int k = 0; k < P; ++k) acc = madd<kFast>(acc, U[v * P2 + ii + P * k], lob[s + P * k]);
         LB[(v * P + s) * P + ii] = acc;
       }
     }
   }
   // subcell value (s1, s2) from the y pass
   template <bool kFast = false>
-  __device__ static void subcell(const double* LY, const DevOps<N, double>& op, int s1, int s2, double* out) {
+  __device__ static void subcell(const T* LY, const T* lim, int s1, int s2, T* out) {
 #pragma unroll
     for (int v = 0; v < V; ++v) {
-      double acc = 0.0;
+      T acc = 0;
 #pragma unroll
-      for (int k = 0; k < P; ++k) acc = madd<kFast>(acc, LY[(v * S + s2) * P + k], op.uh2lim[s1 + S * k]);
+      for (int k = 0; k < P; ++k) acc = madd<kFast>(acc, LY[(v * S + s2) * P + k], lim[s1 + S * k]);
       out[v] = acc;
     }
   }
   template <bool kFast = false>
-  __device__ static void lobatto(const double* LB, const DevOps<N, double>& op, int s1, int s2, double* out) {
+  __device__ static void lobatto(const T* LB, const T* lob, int s1, int s2, T* out) {
 #pragma unroll
     for (int v = 0; v < V; ++v) {
-      double acc = 0.0;
+      T acc = 0;
 #pragma unroll
-      for (int k = 0; k < P; ++k) acc = madd<kFast>(acc, LB[(v * P + s2) * P + k], op.uh2lob[s1 + P * k]);
+      for (int k = 0; k < P; ++k) acc = madd<kFast>(acc, LB[(v * P + s2) * P + k], lob[s1 + P * k]);
       out[v] = acc;
     }
   }
-  // x pass fused with min/max (integer keys) and the positivity test of every subcell
+  // x pass fused with min/max (integer keys) and the positivity test of every subcell (FP64)
   template <class Sys, bool kFast = false>
-  __device__ static void xpass_minmax(const double* U, const double* LY, const double* LB, const DevOps<N, double>& op,
-                                      const Phys& ph, int r, int nr, double* mn, double* mx, bool& posfail) {
-    double val[V];
+  __device__ static void xpass_minmax(const T* U, const T* LY, const T* LB, const T* lim, const T* lob,
+                                      const Phys& ph, int r, int nr, T* mn, T* mx, bool& posfail) {
+    T val[V];
     long long kmn[V], kmx[V];
 #pragma unroll
     for (int v = 0; v < V; ++v) { kmn[v] = okey(mn[v]); kmx[v] = okey(mx[v]); }
     for (int idx = r; idx < S * S; idx += nr) {
-      subcell<kFast>(LY, op, idx % S, idx / S, val);
+      subcell<kFast>(LY, lim, idx % S, idx / S, val);
 #pragma unroll
       for (int v = 0; v < V; ++v) { const long long k = okey(val[v]); kmn[v] = min(kmn[v], k); kmx[v] = max(kmx[v], k); }
       if constexpr (Sys::ID != kSysAD) {
@@ -111,7 +113,7 @@ struct Proj {
       }
     }
     for (int idx = r; idx < P * P; idx += nr) {
-      lobatto<kFast>(LB, op, idx % P, idx / P, val);
+      lobatto<kFast>(LB, lob, idx % P, idx / P, val);
 #pragma unroll
       for (int v = 0; v < V; ++v) { const long long k = okey(val[v]); kmn[v] = min(kmn[v], k); kmx[v] = max(kmx[v], k); }
     }
@@ -126,6 +128,43 @@ struct Proj {
 #pragma unroll
     for (int v = 0; v < V; ++v) { mn[v] = okey_inv(kmn[v]); mx[v] = okey_inv(kmx[v]); }
   }
+  // FP32 x pass fused with min/max and the admissibility test: a subcell whose
+  // FP32 value is not clearly admissible (err = the projection's error bound
+  // per variable) is projected again in FP64 from U64 and tested exactly.
+  template <class Sys>
+  __device__ static void xpass_minmax_f32(const float* LY, const float* LB, const float* lim, const float* lob,
+                                          const double* U64, const DevOps<N, double>& op,
+                                          const typename Sys::FConst& fc, const float* err, const Phys& ph,
+                                          int r, int nr, float* mn, float* mx, bool& posfail) {
+    float val[V];
+    for (int idx = r; idx < S * S; idx += nr) {
+      const int s1 = idx % S, s2 = idx / S;
+      subcell<true>(LY, lim, s1, s2, val);
+#pragma unroll
+      for (int v = 0; v < V; ++v) { mn[v] = fminf(mn[v], val[v]); mx[v] = fmaxf(mx[v], val[v]); }
+      if constexpr (Sys::ID != kSysAD) {
+        if (!Sys::admissible_box_f32(fc, val, err)) {
+          double q[V];
+#pragma unroll
+          for (int v = 0; v < V; ++v) {
+            double acc = 0.0;
+            for (int l = 0; l < P; ++l) {
+              double row = 0.0;
+              for (int k = 0; k < P; ++k) row = fma(U64[v * P2 + k + P * l], op.uh2lim[s1 + S * k], row);
+              acc = fma(row, op.uh2lim[s2 + S * l], acc);
+            }
+            q[v] = acc;
+          }
+          if (!Sys::positive(ph, q)) posfail = true;
+        }
+      }
+    }
+    for (int idx = r; idx < P * P; idx += nr) {
+      lobatto<true>(LB, lob, idx % P, idx / P, val);
+#pragma unroll
+      for (int v = 0; v < V; ++v) { mn[v] = fminf(mn[v], val[v]); mx[v] = fmaxf(mx[v], val[v]); }
+    }
+  }
 };
 
 // Voronoi neighbour index along one axis (Euler/initialize.f90:219-258):
@@ -137,9 +176,8 @@ __device__ __forceinline__ int nb_index(int x, int d, int n, int bc_lo, int bc_h
   return y;
 }
 
-// CFL denominator at one node (calc_time_step.f90: Euler/BN :31-45, AD :37-50);
-// kFast: eigenvalues in FP32 (the FP32-mixed mode), sums and reduction in FP64
-template <class Sys, int N, bool kFast = false>
+// CFL denominator at one node (calc_time_step.f90: Euler/BN :31-45, AD :37-50)
+template <class Sys, int N>
 __device__ __forceinline__ double cfl_denom(const InstDesc& in, const double* Q) {
   if constexpr (Sys::ID == kSysAD) {
     const double factor = (double)(2 * N + 1);
@@ -150,12 +188,23 @@ __device__ __forceinline__ double cfl_denom(const InstDesc& in, const double* Q)
     return denom;
   } else {
     double ex, ey;
-    if constexpr (kFast) Sys::max_eig2_f32(in.ph, Q, ex, ey);
-    else Sys::max_eig2(in.ph, Q, ex, ey);
+    Sys::max_eig2(in.ph, Q, ex, ey);
     double denom = 0.0;
     denom = denom + ex / in.dx;
     denom = denom + ey / in.dy;
     return denom;
+  }
+}
+// FP32-mixed: eigenvalues and the node's denominator in FP32 (the maximum
+// over nodes, and dt, in FP64)
+template <class Sys, int N>
+__device__ __forceinline__ double cfl_denom_f32(const InstDesc& in, const typename Sys::FConst& fc, const float* q) {
+  if constexpr (Sys::ID == kSysAD) {
+    return cfl_denom<Sys, N>(in, nullptr);
+  } else {
+    float ex, ey;
+    Sys::max_eig2_f32(fc, q, ex, ey);
+    return (double)(ex / (float)in.dx + ey / (float)in.dy);
   }
 }
 
@@ -164,9 +213,13 @@ struct CellCfg {
   static constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1, V = Sys::V;
   static constexpr int CPB = (256 / P2) < 1 ? 1 : (256 / P2);
   static constexpr int THREADS = ((CPB * P2 + 31) / 32) * 32;
-  // per cell: U [V][P2], LY [V][S][P], LB [V][P][P], red [2][V][P2]
+  // per cell: U [V][P2], LY [V][S][P], LB [V][P][P], red [2][V][P2] (FP64);
+  // FP32-mixed: U64 [V][P2] then FP32 U [V][P2], LY, LB, red, |U| max [V]
+  // in the same room
   static constexpr int CELL_DBL = V * P2 + V * S * P + V * P * P + 2 * V * P2;
-  static constexpr int SMEM_BYTES = CPB * CELL_DBL * 8 + CPB * 8 /*cell max*/ + CPB * 4 /*flags*/ + 16;
+  static_assert(8 * V * P2 + 4 * (3 * V * P2 + V * S * P + V * P * P + V) <= 8 * CELL_DBL, "FP32 cell layout");
+  static constexpr int OPS_DBL = S * P + P * P;  // uh2lim, uh2lob
+  static constexpr int SMEM_BYTES = CPB * CELL_DBL * 8 + OPS_DBL * 8 + CPB * 8 /*cell max*/ + CPB * 4 /*flags*/ + 16;
 };
 
 template <class Sys, int N, bool kFast>
@@ -175,7 +228,8 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
   constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1, V = Sys::V, CPB = C::CPB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* sm = reinterpret_cast<double*>(smem_raw);
-  unsigned long long* cmax = reinterpret_cast<unsigned long long*>(sm + CPB * C::CELL_DBL);
+  double* opsm = sm + CPB * C::CELL_DBL;
+  unsigned long long* cmax = reinterpret_cast<unsigned long long*>(opsm + C::OPS_DBL);
   int* cflag = reinterpret_cast<int*>(cmax + CPB);
 
   const int mode = a.mode;
@@ -197,16 +251,27 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
   const long long lcell = cell - in.cell_base;
   const int ci = valid ? (int)(lcell % in.imax) : 0, cj = valid ? (int)(lcell / in.imax) : 0;
   const bool limiter = Sys::ID != kSysAD && a.mm[0] != nullptr;
-
   double* U = sm + (size_t)(in_cta ? lc : 0) * C::CELL_DBL;
   double* LY = U + V * P2;
   double* LB = LY + V * S * P;
   double* RED = LB + V * P * P;
+  // FP32-mixed views of the same room
+  float* Uf = reinterpret_cast<float*>(U + V * P2);
+  float* LYf = Uf + V * P2;
+  float* LBf = LYf + V * S * P;
+  float* REDf = LBf + V * P * P;
+  unsigned* amax = reinterpret_cast<unsigned*>(REDf + 2 * V * P2);
 
+  // projection operators into shared memory (lanes index them by subcell)
+  for (int k = t; k < C::OPS_DBL; k += blockDim.x) {
+    if constexpr (kFast) reinterpret_cast<float*>(opsm)[k] = k < S * P ? op.uh2limf[k] : op.uh2lobf[k - S * P];
+    else opsm[k] = k < S * P ? op.uh2lim[k] : op.uh2lob[k - S * P];
+  }
   if (in_cta && node == 0) {
     cmax[lc] = 0ull;
     cflag[lc] = 0;
   }
+  if (kFast && in_cta && node < V) amax[node] = 0u;
   __syncthreads();
 
   // ---------------------------------------------------------------- update
@@ -214,31 +279,58 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
   const size_t off = ((size_t)(valid ? cell : 0) * P2 + node) * V;
   if (act) {
     if (mode == kCellFused || mode == kCellSurface || mode == kCellUpdate) {
-      double d[V];
+      const long long fxl = in.fx_base + ci + (long long)(in.imax + 1) * cj;
+      const long long fyb = in.fy_base + ci + (long long)in.imax * cj;
+      const long long fyt = fyb + in.imax;
+      if constexpr (kFast) {
+        // FP32-mixed: duh and the face fluxes are stored in FP32; the surface
+        // contraction and the scaling by 1/(w_i w_j) in FP32, the update of
+        // the FP64 state in FP64
+        const float* D32 = reinterpret_cast<const float*>(a.duh);
+        const float* XL = reinterpret_cast<const float*>(a.fu);
+        const float* XR = reinterpret_cast<const float*>((Sys::ID == kSysBN) ? a.fp : a.fu);
+        const float* YB = reinterpret_cast<const float*>(a.gu);
+        const float* YT = reinterpret_cast<const float*>((Sys::ID == kSysBN) ? a.gp : a.gu);
+        float d[V];
 #pragma unroll
-      for (int v = 0; v < V; ++v) d[v] = a.duh[off + v];
-      if (mode != kCellUpdate) {
-        // surface_integral.f90:20-35: x faces then y faces
-        const long long fxl = in.fx_base + ci + (long long)(in.imax + 1) * cj;
-        const long long fyb = in.fy_base + ci + (long long)in.imax * cj;
-        const long long fyt = fyb + in.imax;
-        const double* XL = a.fu;
-        const double* XR = (Sys::ID == kSysBN) ? a.fp : a.fu;
-        const double* YB = a.gu;
-        const double* YT = (Sys::ID == kSysBN) ? a.gp : a.gu;
-        const double cx = op.wd[j] / in.dx, cy = op.wd[i] / in.dy;
-        if constexpr (kFast) {
-          // FP32-mixed: the surface contraction in FP32, added to the FP64 update
-          const float cxf = (float)cx, cyf = (float)cy;
+        for (int v = 0; v < V; ++v) d[v] = D32[off + v];
+        if (mode != kCellUpdate) {
+          const float cxf = op.wf[j] / (float)in.dx, cyf = op.wf[i] / (float)in.dy;
 #pragma unroll
           for (int v = 0; v < V; ++v) {
-            const float fl = (float)XL[((size_t)fxl * P + j) * V + v], fr = (float)XR[((size_t)(fxl + 1) * P + j) * V + v];
-            const float gb = (float)YB[((size_t)fyb * P + i) * V + v], gt = (float)YT[((size_t)fyt * P + i) * V + v];
-            const float sx = fr * (float)op.FRd[i] - fl * (float)op.FLd[i];
-            const float sy = gt * (float)op.FRd[j] - gb * (float)op.FLd[j];
-            d[v] = d[v] - (double)(cxf * sx + cyf * sy);
+            const float fl = XL[((size_t)fxl * P + j) * V + v], fr = XR[((size_t)(fxl + 1) * P + j) * V + v];
+            const float gb = YB[((size_t)fyb * P + i) * V + v], gt = YT[((size_t)fyt * P + i) * V + v];
+            const float sx = fr * op.FRf[i] - fl * op.FLf[i];
+            const float sy = gt * op.FRf[j] - gb * op.FLf[j];
+            d[v] = d[v] - (cxf * sx + cyf * sy);
           }
+        }
+        if (mode == kCellSurface) {
+          float* D32w = reinterpret_cast<float*>(a.duh);
+#pragma unroll
+          for (int v = 0; v < V; ++v) D32w[off + v] = d[v];
         } else {
+          const double dt = st.dt;
+          const double* uo = a.uh[par] + off;
+          double* un = a.uh[par ^ 1] + off;
+          const float iw = op.iwwf[i + P * j];
+#pragma unroll
+          for (int v = 0; v < V; ++v) {
+            u[v] = uo[v] + dt * (double)(d[v] * iw);
+            un[v] = u[v];
+          }
+        }
+      } else {
+        double d[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) d[v] = a.duh[off + v];
+        if (mode != kCellUpdate) {
+          // surface_integral.f90:20-35: x faces then y faces
+          const double* XL = a.fu;
+          const double* XR = (Sys::ID == kSysBN) ? a.fp : a.fu;
+          const double* YB = a.gu;
+          const double* YT = (Sys::ID == kSysBN) ? a.gp : a.gu;
+          const double cx = op.wd[j] / in.dx, cy = op.wd[i] / in.dy;
 #pragma unroll
           for (int v = 0; v < V; ++v) {
             const double fl = XL[((size_t)fxl * P + j) * V + v], fr = XR[((size_t)(fxl + 1) * P + j) * V + v];
@@ -250,21 +342,20 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
             d[v] = d[v] - cy * (gt * op.FRd[j] - gb * op.FLd[j]);
           }
         }
-      }
-      if (mode == kCellSurface) {
+        if (mode == kCellSurface) {
 #pragma unroll
-        for (int v = 0; v < V; ++v) a.duh[off + v] = d[v];
-      } else {
-        // element_update.f90:18-26
-        const double dt = st.dt;
-        const double* uo = a.uh[par] + off;
-        double* un = a.uh[par ^ 1] + off;
+          for (int v = 0; v < V; ++v) a.duh[off + v] = d[v];
+        } else {
+          // element_update.f90:18-26
+          const double dt = st.dt;
+          const double* uo = a.uh[par] + off;
+          double* un = a.uh[par ^ 1] + off;
 #pragma unroll
-        for (int v = 0; v < V; ++v) {
-          if constexpr (kFast) d[v] = d[v] * op.iww[i + P * j];
-          else d[v] = d[v] / (op.wd[i] * op.wd[j]);
-          u[v] = uo[v] + dt * d[v];
-          un[v] = u[v];
+          for (int v = 0; v < V; ++v) {
+            d[v] = d[v] / (op.wd[i] * op.wd[j]);
+            u[v] = uo[v] + dt * d[v];
+            un[v] = u[v];
+          }
         }
       }
     } else {
@@ -274,9 +365,21 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
   }
   if (mode == kCellSurface) return;  // uniform per launch: no barrier follows
 
+  // FP32 copy of the node's state (FP32-mixed)
+  float uf[V];
+  if constexpr (kFast) {
+#pragma unroll
+    for (int v = 0; v < V; ++v) uf[v] = act ? (float)u[v] : 0.0f;
+  }
+
   // ------------------------------------------------------------- CFL part
   const bool want_cfl = mode != kCellInitDmp;
-  if (act && want_cfl) atomicMax(&cmax[lc], (unsigned long long)__double_as_longlong(cfl_denom<Sys, N, kFast>(in, u)));
+  if (act && want_cfl) {
+    double dn;
+    if constexpr (kFast) dn = cfl_denom_f32<Sys, N>(in, typename Sys::FConst(in.ph), uf);
+    else dn = cfl_denom<Sys, N>(in, u);
+    atomicMax(&cmax[lc], (unsigned long long)__double_as_longlong(dn));
+  }
 
   // ------------------------------------------------------------- DMP part
   const bool want_dmp = limiter && mode != kCellCfl;
@@ -284,38 +387,91 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
     // Cells whose limiter is active keep their min/max from the subcell data
     // (get_min_max, Euler/limiter.f90:134-139) in the priming pass.
     const bool from_lh = act && mode == kCellPrime && a.status[par][valid ? cell : 0] != 0;
-    if (act) {
+    if constexpr (kFast) {
+      if (act) {
 #pragma unroll
-      for (int v = 0; v < V; ++v) U[v * P2 + node] = u[v];
-    }
-    __syncthreads();
-    if (act && !from_lh) Proj<N, V>::template ypass<kFast>(U, LY, LB, op, node, P2);
-    __syncthreads();
-    double mn[V], mx[V];
-    bool posfail = false;
-#pragma unroll
-    for (int v = 0; v < V; ++v) { mn[v] = kInf; mx[v] = -kInf; }
-    if (act) {
-      if (from_lh) {
-        const double* L = a.lh[par] + (size_t)cell * S * S * V;
-        for (int idx = node; idx < S * S; idx += P2)
-#pragma unroll
-          for (int v = 0; v < V; ++v) { mn[v] = fmin(mn[v], L[idx * V + v]); mx[v] = fmax(mx[v], L[idx * V + v]); }
-      } else {
-        Proj<N, V>::template xpass_minmax<Sys, kFast>(U, LY, LB, op, in.ph, node, P2, mn, mx, posfail);
+        for (int v = 0; v < V; ++v) {
+          U[v * P2 + node] = u[v];
+          Uf[v * P2 + node] = uf[v];
+          atomicMax(&amax[v], __float_as_uint(fabsf(uf[v])));
+        }
       }
+      __syncthreads();
+      const float* lim = reinterpret_cast<const float*>(opsm);
+      const float* lob = lim + S * P;
+      if (act && !from_lh) Proj<N, V, float>::template ypass<true>(Uf, LYf, LBf, lim, lob, node, P2);
+      __syncthreads();
+      float mn[V], mx[V];
+      bool posfail = false;
 #pragma unroll
-      for (int v = 0; v < V; ++v) {
-        RED[v * P2 + node] = mn[v];
-        RED[(V + v) * P2 + node] = mx[v];
+      for (int v = 0; v < V; ++v) { mn[v] = uf[v]; mx[v] = uf[v]; }
+      if (act) {
+        if (from_lh) {
+          const double* L = a.lh[par] + (size_t)cell * S * S * V;
+#pragma unroll
+          for (int v = 0; v < V; ++v) { mn[v] = __int_as_float(0x7f800000); mx[v] = -__int_as_float(0x7f800000); }
+          for (int idx = node; idx < S * S; idx += P2)
+#pragma unroll
+            for (int v = 0; v < V; ++v) { mn[v] = fminf(mn[v], (float)L[idx * V + v]); mx[v] = fmaxf(mx[v], (float)L[idx * V + v]); }
+        } else {
+          float err[V];
+#pragma unroll
+          for (int v = 0; v < V; ++v) err[v] = op.perr * __uint_as_float(amax[v]);
+          Proj<N, V, float>::template xpass_minmax_f32<Sys>(LYf, LBf, lim, lob, U, op, typename Sys::FConst(in.ph),
+                                                            err, in.ph, node, P2, mn, mx, posfail);
+        }
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          REDf[v * P2 + node] = mn[v];
+          REDf[(V + v) * P2 + node] = mx[v];
+        }
+        if (posfail) atomicOr(&cflag[lc], 1);
       }
-      if (posfail) atomicOr(&cflag[lc], 1);
+    } else {
+      if (act) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) U[v * P2 + node] = u[v];
+      }
+      __syncthreads();
+      const double* lim = opsm;
+      const double* lob = opsm + S * P;
+      if (act && !from_lh) Proj<N, V, double>::template ypass<false>(U, LY, LB, lim, lob, node, P2);
+      __syncthreads();
+      double mn[V], mx[V];
+      bool posfail = false;
+#pragma unroll
+      for (int v = 0; v < V; ++v) { mn[v] = kInf; mx[v] = -kInf; }
+      if (act) {
+        if (from_lh) {
+          const double* L = a.lh[par] + (size_t)cell * S * S * V;
+          for (int idx = node; idx < S * S; idx += P2)
+#pragma unroll
+            for (int v = 0; v < V; ++v) { mn[v] = fmin(mn[v], L[idx * V + v]); mx[v] = fmax(mx[v], L[idx * V + v]); }
+        } else {
+          Proj<N, V, double>::template xpass_minmax<Sys, false>(U, LY, LB, lim, lob, in.ph, node, P2, mn, mx, posfail);
+        }
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          RED[v * P2 + node] = mn[v];
+          RED[(V + v) * P2 + node] = mx[v];
+        }
+        if (posfail) atomicOr(&cflag[lc], 1);
+      }
     }
     __syncthreads();
     if (act && node < V) {
       const int v = node;
-      double cmn = RED[v * P2], cmx = RED[(V + v) * P2];
-      for (int k = 1; k < P2; ++k) { cmn = fmin(cmn, RED[v * P2 + k]); cmx = fmax(cmx, RED[(V + v) * P2 + k]); }
+      double cmn, cmx;
+      if constexpr (kFast) {
+        float fmn = REDf[v * P2], fmx = REDf[(V + v) * P2];
+        for (int k = 1; k < P2; ++k) { fmn = fminf(fmn, REDf[v * P2 + k]); fmx = fmaxf(fmx, REDf[(V + v) * P2 + k]); }
+        cmn = (double)fmn;
+        cmx = (double)fmx;
+      } else {
+        cmn = RED[v * P2];
+        cmx = RED[(V + v) * P2];
+        for (int k = 1; k < P2; ++k) { cmn = fmin(cmn, RED[v * P2 + k]); cmx = fmax(cmx, RED[(V + v) * P2 + k]); }
+      }
       if (mode == kCellPrime) {
         a.mm[par][(size_t)cell * 2 * V + v] = cmn;
         a.mm[par][(size_t)cell * 2 * V + V + v] = cmx;

@@ -4,10 +4,11 @@
 //   cells of all instances are numbered globally; instance k owns the cell
 //   range [cell_base, cell_base + imax*jmax), cell = i + imax*j inside it.
 //   uh      [cell][P*P nodes][V]   FP64, exactly the Fortran uh(v,i,j,I,J)
-//   duh     [cell][P*P][V]         FP64
+//   duh     [cell][P*P][V]         FP64 (FP32 in the FP32-mixed mode)
 //   qbnd    [cell][P][4][V]        reference qbnd(v,face,l,I,J)
 //   fbnd    [cell][P][4][V]        (AD: gradQbnd [cell][P][4][2][V])
 //   fu/gu   x faces [fx_base + i + (imax+1)*j][P][V], y faces [fy_base + i + imax*j][P][V]
+//           (FP32 in the FP32-mixed mode)
 //   lh      [cell][S*S][V]         subcell state of limited cells
 //   mm      [cell][2][V]           per-cell min/max for the DMP neighbourhood
 #pragma once
@@ -78,11 +79,17 @@ struct DevOps {
   R wg;              // sum_l' w(l') g(l')
   R FL[P], FR[P];
   double wd[P], FLd[P], FRd[P];
-  double iww[P * P];     // 1 / (w_i w_j) at [i + P*j]
+  float wf[P], FLf[P], FRf[P];  // FP32-mixed surface integral and update
+  float iwwf[P * P];            // 1 / (w_i w_j) at [i + P*j]
   double xid[P];
   double uh2lim[S * P];  // (s,k) at [s + S*k]
   double lim2uh[P * S];  // (k,s) at [k + P*s]
   double uh2lob[P * P];  // (q,k) at [q + P*k]
+  // FP32-mixed DMP: the projections in FP32, and a bound on their error:
+  // |FP32 projection - exact projection| <= perr * max over the cell's nodes |uh|
+  float uh2limf[S * P];
+  float uh2lobf[P * P];
+  float perr;
 };
 
 // Arguments shared by all kernels of one (system, N) batch.  The state that
@@ -98,10 +105,10 @@ struct BatchArgs {
   long long ncells;
   long long nfx, nfy;                // total x / y faces
   double* uh[2];                     // uh [cell][P*P][V]
-  double* duh;
+  double* duh;                       // FP32 storage in the FP32-mixed mode
   void* qbnd;                        // R precision (predictor output)
   void* fbnd;                        // R precision; AD: gradQbnd
-  double* fu;                        // BN: Fm
+  double* fu;                        // BN: Fm; fu..gp FP32 storage in the FP32-mixed mode
   double* gu;                        // BN: Gm
   double* fp;                        // BN only: Fp
   double* gp;                        // BN only: Gp

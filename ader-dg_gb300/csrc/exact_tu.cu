@@ -98,26 +98,35 @@ cudaError_t mark(const BatchArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-int subcell_grid(int num_sms) {
-  using C = SubCfg<Sys, N>;
+template <class T>
+int subcell_grid_t(int num_sms) {
+  using C = SubCfg<Sys, N, T>;
   int per_sm = 0;
-  cudaFuncSetAttribute(k_subcell<Sys, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_subcell<Sys, N>, C::THREADS, C::SMEM_BYTES) != cudaSuccess)
+  cudaFuncSetAttribute(k_subcell<Sys, N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_subcell<Sys, N, T>, C::THREADS, C::SMEM_BYTES) !=
+      cudaSuccess)
     per_sm = 1;
   if (per_sm < 1) per_sm = 1;
   return per_sm * num_sms;
 }
 
-cudaError_t subcell(const BatchArgs& a, const void* ops, const FaceConst& fc, int grid, cudaStream_t s) {
-  using C = SubCfg<Sys, N>;
+int subcell_grid(int num_sms, int fp32) { return fp32 ? subcell_grid_t<float>(num_sms) : subcell_grid_t<double>(num_sms); }
+
+template <class T>
+cudaError_t subcell_t(const BatchArgs& a, const void* ops, const FaceConst& fc, int grid, cudaStream_t s) {
+  using C = SubCfg<Sys, N, T>;
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_subcell<Sys, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
+    cudaError_t e = cudaFuncSetAttribute(k_subcell<Sys, N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  k_subcell<Sys, N><<<grid, C::THREADS, C::SMEM_BYTES, s>>>(a, *reinterpret_cast<const DevOps<N, double>*>(ops), fc);
+  k_subcell<Sys, N, T><<<grid, C::THREADS, C::SMEM_BYTES, s>>>(a, *reinterpret_cast<const DevOps<N, double>*>(ops), fc);
   return cudaGetLastError();
+}
+
+cudaError_t subcell(const BatchArgs& a, const void* ops, const FaceConst& fc, int grid, int fp32, cudaStream_t s) {
+  return fp32 ? subcell_t<float>(a, ops, fc, grid, s) : subcell_t<double>(a, ops, fc, grid, s);
 }
 #endif
 

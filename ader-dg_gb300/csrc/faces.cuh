@@ -7,8 +7,12 @@
 // Advection-Diffusion/riemann_problem.f90:8-113 (viscous LLF).  One thread per
 // (face, point); the x faces of all instances come first, then the y faces.
 // Compiled with --fmad=false: every value agrees bit for bit with the
-// reference expression evaluated in FP64 from the same face states.
+// reference expression evaluated in FP64 from the same face states.  In the
+// FP32-mixed mode (R = float) the fluxes are stored in FP32, and the Euler
+// and Baer-Nunziato fluxes are computed in FP32.
 #pragma once
+
+#include <type_traits>
 
 #include "common.cuh"
 #include "physics.cuh"
@@ -37,22 +41,24 @@ __device__ __forceinline__ int find_inst_fy(const InstDesc* inst, int n, long lo
   return lo;
 }
 
-template <int V, class R>
-__device__ __forceinline__ void load_face_state(const R* qb, const R* fb, long long cell, int P, int l, int f, double* Q, double* F) {
+template <int V, class R, class T>
+__device__ __forceinline__ void load_face_state(const R* qb, const R* fb, long long cell, int P, int l, int f, T* Q, T* F) {
   const size_t o = (((size_t)cell * P + l) * 4 + f) * V;
 #pragma unroll
   for (int v = 0; v < V; ++v) {
-    Q[v] = (double)qb[o + v];
-    if (F) F[v] = (double)fb[o + v];
+    Q[v] = (T)qb[o + v];
+    if (F) F[v] = (T)fb[o + v];
   }
 }
 
 // Euler double Mach reflection boundary state: Q = prim2cons(Vp), F = flux(Q)
 // along axis d (matmul(Fbc, nv) of Euler/riemann_problem.f90:43-46).
-__device__ __forceinline__ void dmr_state(const Phys& ph, const double* Vp, int d, double* Q, double* F) {
-  double Fb[8];
-  EulerSys::prim2cons(ph, Vp, Q);
-  EulerSys::flux(ph, Q, Fb);
+template <class T>
+__device__ __forceinline__ void dmr_state(const PhysC<T>& pc, const double* Vpd, int d, T* Q, T* F) {
+  T Fb[8], Vp[4];
+  for (int v = 0; v < 4; ++v) Vp[v] = (T)Vpd[v];
+  EulerSys::prim2cons(pc, Vp, Q);
+  EulerSys::flux(pc, Q, Fb);
   for (int v = 0; v < 4; ++v) F[v] = Fb[d * 4 + v];
 }
 
@@ -136,9 +142,9 @@ __device__ void faces_euler_fp32(const BatchArgs& a, const FaceConst& fc, const 
     load(cR, fl, QR, FR);
   }
   const float smax = fmaxf(euler_max_eig_t<float>(gamma, QL, d), euler_max_eig_t<float>(gamma, QR, d));
-  double* dst = (xdir ? a.fu : a.gu) + ((size_t)face * P + l) * V;
+  float* dst = reinterpret_cast<float*>(xdir ? a.fu : a.gu) + ((size_t)face * P + l) * V;
 #pragma unroll
-  for (int v = 0; v < V; ++v) dst[v] = (double)(0.5f * (FL[v] + FR[v]) - 0.5f * smax * (QR[v] - QL[v]));
+  for (int v = 0; v < V; ++v) dst[v] = 0.5f * (FL[v] + FR[v]) - 0.5f * smax * (QR[v] - QL[v]);
 }
 
 template <class Sys, int N, class R>
@@ -234,17 +240,20 @@ __global__ void __launch_bounds__(256) k_faces(BatchArgs a, FaceConst fc) {
     const double smax = smax_c + 2.0 * eta * smax_v;
     const double FL0 = ph.cx * QL[0] + -ph.a * gL[0], FL1 = ph.cy * QL[0] + -ph.a * gL[1];
     const double FR0 = ph.cx * QR[0] + -ph.a * gR[0], FR1 = ph.cy * QR[0] + -ph.a * gR[1];
-    double* dst = xdir ? a.fu : a.gu;
-    dst[out] = 0.5 * ((FL0 + FR0) * nv0 + (FL1 + FR1) * nv1) - 0.5 * smax * (QR[0] - QL[0]);
+    R* dst = reinterpret_cast<R*>(xdir ? a.fu : a.gu);
+    dst[out] = (R)(0.5 * ((FL0 + FR0) * nv0 + (FL1 + FR1) * nv1) - 0.5 * smax * (QR[0] - QL[0]));
   } else {
-    double QL[V], QR[V], FL[V], FR[V];
+    // compute type: FP64 (reference order), FP32 for Baer-Nunziato in the mixed mode
+    using CT = typename std::conditional<sizeof(R) == 4, float, double>::type;
+    const PhysC<CT> pc(ph);
+    CT QL[V], QR[V], FL[V], FR[V];
     const bool is_dmr = (Sys::ID == kSysEuler) && in.bc_mode == 1;
     const long long cL = xdir ? cid(i - 1, j) : cid(i, j - 1);
     const long long cR = cid(i, j);
     if (pos == 0) {
       if (is_dmr) {
         if (xdir) {  // inflow, Euler/riemann_problem.f90:41-48
-          dmr_state(ph, fc.Va, 0, QL, FL);
+          dmr_state(pc, fc.Va, 0, QL, FL);
           load_face_state<V, R>(qb, fb, cR, P, l, fl, QR, FR);
         } else {     // transmissive / reflective wall, :76-86
           load_face_state<V, R>(qb, fb, cR, P, l, fl, QL, FL);
@@ -268,7 +277,7 @@ __global__ void __launch_bounds__(256) k_faces(BatchArgs a, FaceConst fc) {
       load_face_state<V, R>(qb, fb, cLast, P, l, fr, QL, FL);
       if (is_dmr && !xdir) {  // time-dependent top boundary, :88-100
         const double x_sw = fc.xsw0 + fc.xsw1 * a.st[k].time;
-        dmr_state(ph, ((double)(i + 1) * in.dx <= x_sw) ? fc.Va : fc.Vb, 1, QR, FR);
+        dmr_state(pc, ((double)(i + 1) * in.dx <= x_sw) ? fc.Va : fc.Vb, 1, QR, FR);
       } else if (!is_dmr && bcr == 3) {
         load_face_state<V, R>(qb, fb, xdir ? cid(0, j) : cid(i, 0), P, l, fl, QR, FR);
       } else {
@@ -279,23 +288,23 @@ __global__ void __launch_bounds__(256) k_faces(BatchArgs a, FaceConst fc) {
       load_face_state<V, R>(qb, fb, cR, P, l, fl, QR, FR);
     }
     // Rusanov: smax from both sides' eigenvalues (Euler/pde.f90:97-114)
-    const double smax = fmax(Sys::max_eig(ph, QL, d), Sys::max_eig(ph, QR, d));
+    const CT smax = tmax(Sys::max_eig(pc, QL, d), Sys::max_eig(pc, QR, d));
     if constexpr (Sys::ID == kSysBN) {
       // path-conservative fluctuations, Baer-Nunziato/pde.f90:326-353
-      double D[9];
-      BNSys::roe_times_jump(ph, QL, QR, d, D);
-      double* dm = xdir ? a.fu : a.gu;
-      double* dp = xdir ? a.fp : a.gp;
+      CT D[9];
+      BNSys::roe_times_jump(pc, QL, QR, d, D);
+      R* dm = reinterpret_cast<R*>(xdir ? a.fu : a.gu);
+      R* dp = reinterpret_cast<R*>(xdir ? a.fp : a.gp);
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        const double base = 0.5 * (FL[v] + FR[v]) - 0.5 * smax * (QR[v] - QL[v]);
-        dm[out + v] = base - 0.5 * D[v];
-        dp[out + v] = base + 0.5 * D[v];
+        const CT base = CT(0.5) * (FL[v] + FR[v]) - CT(0.5) * smax * (QR[v] - QL[v]);
+        dm[out + v] = (R)(base - CT(0.5) * D[v]);
+        dp[out + v] = (R)(base + CT(0.5) * D[v]);
       }
     } else {
-      double* dst = xdir ? a.fu : a.gu;
+      R* dst = reinterpret_cast<R*>(xdir ? a.fu : a.gu);
 #pragma unroll
-      for (int v = 0; v < V; ++v) dst[out + v] = 0.5 * (FL[v] + FR[v]) - 0.5 * smax * (QR[v] - QL[v]);
+      for (int v = 0; v < V; ++v) dst[out + v] = (R)(CT(0.5) * (FL[v] + FR[v]) - CT(0.5) * smax * (QR[v] - QL[v]));
     }
   }
 }

@@ -8,7 +8,8 @@
 //     cell, persistent over the list; then put_subcell_data, the DMP of
 //     recompute = 2 cells, the next step's min/max and CFL contribution.
 //     update_limiter (Lh = NewLh) is the parity flip of the Lh buffers.
-// Compiled with --fmad=false, reference operation order throughout.
+// Compiled with --fmad=false, reference operation order throughout; the
+// FP32-mixed mode runs the subcell re-solve (K4b) in FP32.
 #pragma once
 
 #include "cells.cuh"
@@ -64,65 +65,98 @@ __global__ void __launch_bounds__(256) k_mark(BatchArgs a) {
   }
 }
 
-template <class Sys, int N>
+template <class Sys, int N, class T>
 struct SubCfg {
   static constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1, V = Sys::V;
   static constexpr int R = S + 4;  // gathered region: subcells -1 .. S+2 (1-based)
   static constexpr int H = S + 2;  // reconstructed region: 0 .. S+1
   static constexpr int THREADS = 128;
-  // doubles: sub0 [V][R*R], slopes x/y/t + wLx wRx wLy wRy [7][V][H*H], edge fluxes [2][V][(S+1)*S],
-  // subuh1 [V][S*S], put_subcell_data / DMP scratch
-  static constexpr int SCRATCH = V * S * P + V * P2 + V * S * P + V * P * P;
-  static constexpr int DBL = V * R * R + 7 * V * H * H + 2 * V * (S + 1) * S + V * S * S + SCRATCH + 2 * V * THREADS;
-  static constexpr int SMEM_BYTES = DBL * 8 + 64;
+  static constexpr int NE = (S + 1) * S;               // x edges (and y edges) of the subgrid
+  static constexpr int NEF = (Sys::ID == kSysBN ? 4 : 2) * V * NE;  // edge fluxes (+ BN fluctuations)
+  // compute-type (T) elements: sub0 [V][R*R], slopes x/y/t and wLx wRx wLy wRy
+  // [7][V][H*H], edge fluxes, subuh1 [V][S*S], luhy [V][P][S], and the
+  // operators uh2lim [S*P], lim2uh [P*S] in T.  The gather stages the 3x3
+  // neighbourhood's uh [9][V][P2] and its y pass [9][V][P][S] in the room of
+  // the slopes, which are formed after it.
+  static constexpr int TSLOPE = 7 * V * H * H;
+  static_assert(9 * V * P2 + 9 * V * P * S <= TSLOPE, "gather staging room");
+  static constexpr int TEL = V * R * R + TSLOPE + NEF + V * S * S + V * S * P + 2 * S * P;
+  static constexpr int TBYTES = ((TEL * (int)sizeof(T) + 15) / 16) * 16;
+  // FP64 elements: new polynomial UN [V][P2], DMP y pass LY [V][S][P], LB
+  // [V][P][P], reduction [2][V][THREADS], operators uh2lim, uh2lob (FP64)
+  static constexpr int OPS_DBL = S * P + P * P;
+  static constexpr int DEL = V * P2 + V * S * P + V * P * P + 2 * V * THREADS + OPS_DBL;
+  // misc: flags, CFL max, neighbour cells and their status
+  static constexpr int MISC = 16 + 9 * 8 + 9 * 4 + 12;
+  static constexpr int SMEM_BYTES = TBYTES + DEL * 8 + MISC;
 };
 
 // minmod, Euler/limiter.f90:384-405
-__device__ __forceinline__ double minmod(double a, double b) {
-  if (a * b <= 0.0) return 0.0;
-  return (fabs(a) < fabs(b)) ? a : b;
+template <class T>
+__device__ __forceinline__ T minmod(T a, T b) {
+  if (a * b <= T(0)) return T(0);
+  return (tabs(a) < tabs(b)) ? a : b;
 }
 
 // Subgrid Rusanov flux (Euler/limiter.f90:361-378; BN :359-383 adds D = B~ dQ)
-template <class Sys>
-__device__ __forceinline__ void rusanov_s(const Phys& ph, const double* QL, const double* QR, int d, double* F, double* D) {
+template <class Sys, class T>
+__device__ __forceinline__ void rusanov_s(const PhysC<T>& pc, const T* QL, const T* QR, int d, T* F, T* D) {
   constexpr int V = Sys::V;
-  const double smax = fmax(Sys::max_eig(ph, QL, d), Sys::max_eig(ph, QR, d));
-  double FLf[2 * V], FRf[2 * V];
-  Sys::flux(ph, QL, FLf);
-  Sys::flux(ph, QR, FRf);
-  const double nv0 = d == 0 ? 1.0 : 0.0, nv1 = d == 0 ? 0.0 : 1.0;
+  const T smax = tmax(Sys::max_eig(pc, QL, d), Sys::max_eig(pc, QR, d));
+  T FLf[2 * V], FRf[2 * V];
+  Sys::flux(pc, QL, FLf);
+  Sys::flux(pc, QR, FRf);
+  const T nv0 = d == 0 ? T(1) : T(0), nv1 = d == 0 ? T(0) : T(1);
 #pragma unroll
   for (int v = 0; v < V; ++v)
-    F[v] = 0.5 * ((FLf[v] + FRf[v]) * nv0 + (FLf[V + v] + FRf[V + v]) * nv1) - 0.5 * smax * (QR[v] - QL[v]);
-  if constexpr (Sys::ID == kSysBN) BNSys::roe_times_jump(ph, QL, QR, d, D);
+    F[v] = T(0.5) * ((FLf[v] + FRf[v]) * nv0 + (FLf[V + v] + FRf[V + v]) * nv1) - T(0.5) * smax * (QR[v] - QL[v]);
+  if constexpr (Sys::ID == kSysBN) BNSys::roe_times_jump(pc, QL, QR, d, D);
 }
 
-template <class Sys, int N>
-__global__ void __launch_bounds__(SubCfg<Sys, N>::THREADS) k_subcell(BatchArgs a, DevOps<N, double> op, FaceConst fc) {
-  using C = SubCfg<Sys, N>;
-  constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1, V = Sys::V, R = C::R, H = C::H, NT = C::THREADS;
+// T = double: the reference's FP64 arithmetic in its order (bit for bit).
+// T = float: the FP32-mixed mode; the subcell re-solve in FP32, the state,
+// Lh, the DMP of the new polynomial and its CFL contribution in FP64.
+template <class Sys, int N, class T>
+__global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS) k_subcell(BatchArgs a, DevOps<N, double> op, FaceConst fc) {
+  using C = SubCfg<Sys, N, T>;
+  constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1, V = Sys::V, R = C::R, H = C::H, NT = C::THREADS, NE = C::NE;
   constexpr bool BN = Sys::ID == kSysBN;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  double* sub0 = reinterpret_cast<double*>(smem_raw);
-  double* slx = sub0 + V * R * R;
-  double* sly = slx + V * H * H;
-  double* slt = sly + V * H * H;
-  double* wLx = slt + V * H * H;
-  double* wRx = wLx + V * H * H;
-  double* wLy = wRx + V * H * H;
-  double* wRy = wLy + V * H * H;
-  double* Fx = wRy + V * H * H;
-  double* Fy = Fx + V * (S + 1) * S;
-  double* sub1 = Fy + V * (S + 1) * S;
-  double* scr = sub1 + V * S * S;
-  double* red = scr + C::SCRATCH;
-  int* flag = reinterpret_cast<int*>(red + 2 * V * NT);
-  unsigned long long* cmaxp = reinterpret_cast<unsigned long long*>(flag + 2);
+  T* sub0 = reinterpret_cast<T*>(smem_raw);
+  T* slx = sub0 + V * R * R;
+  T* sly = slx + V * H * H;
+  T* slt = sly + V * H * H;
+  T* wLx = slt + V * H * H;
+  T* wRx = wLx + V * H * H;
+  T* wLy = wRx + V * H * H;
+  T* wRy = wLy + V * H * H;
+  T* EF = slx + C::TSLOPE;           // x edges: F [V][NE] (BN: then D [V][NE]); then the y edges
+  T* sub1 = EF + C::NEF;
+  T* LUY = sub1 + V * S * S;         // [V][P][S]: luhy(v, iii, s) at (v*P + s)*S + iii
+  T* limT = LUY + V * S * P;         // uh2lim (s,k) at [s + S*k]
+  T* l2uT = limT + S * P;            // lim2uh (k,s) at [k + P*s]
+  T* NB = slx;                       // gather staging: [9][V][P2]
+  T* LYN = NB + 9 * V * P2;          // [9][V][P][S]: sum_m uh(k, m) uh2lim(s, m) at ((n*V + v)*P + k)*S + s
+  double* UN = reinterpret_cast<double*>(smem_raw + C::TBYTES);  // [V][P2]
+  double* LY = UN + V * P2;          // DMP y pass [V][S][P]
+  double* LB = LY + V * S * P;       // [V][P][P]
+  double* red = LB + V * P * P;      // [2][V][NT]
+  double* opsm = red + 2 * V * NT;   // uh2lim, uh2lob (FP64)
+  unsigned char* misc = reinterpret_cast<unsigned char*>(opsm + C::OPS_DBL);
+  int* flag = reinterpret_cast<int*>(misc);
+  unsigned long long* cmaxp = reinterpret_cast<unsigned long long*>(misc + 8);
+  long long* nbc = reinterpret_cast<long long*>(misc + 16);  // 3x3 neighbour cells, n = (bi+1) + 3 (bj+1)
+  int* nbs = reinterpret_cast<int*>(misc + 16 + 9 * 8);     // their status (0: project olduh)
 
   const int t = threadIdx.x;
-  auto SU = [&](int v, int ii, int jj) -> double& { return sub0[v * R * R + (ii + 1) + R * (jj + 1)]; };  // ii,jj in -1..S+2
-  auto hx = [&](int v, int ii, int jj) { return v * H * H + ii + H * jj; };                              // ii,jj in 0..S+1
+  for (int k = t; k < C::OPS_DBL; k += NT) opsm[k] = k < S * P ? op.uh2lim[k] : op.uh2lob[k - S * P];
+  for (int k = t; k < S * P; k += NT) {
+    limT[k] = (T)op.uh2lim[k];
+    l2uT[k] = (T)op.lim2uh[k];
+  }
+  __syncthreads();
+  auto SU = [&](int v, int ii, int jj) -> T& { return sub0[v * R * R + (ii + 1) + R * (jj + 1)]; };  // ii,jj in -1..S+2
+  auto hx = [&](int v, int ii, int jj) { return v * H * H + ii + H * jj; };                         // ii,jj in 0..S+1
 
   const int count = *a.list_count;
   for (int li = blockIdx.x; li < count; li += gridDim.x) {
@@ -131,55 +165,84 @@ __global__ void __launch_bounds__(SubCfg<Sys, N>::THREADS) k_subcell(BatchArgs a
     const InstDesc& in = a.inst[k];
     const InstState& st = a.st[k];
     const Phys ph = in.ph;
+    const PhysC<T> pc(ph);
     const int par = parity(st);
     const long long lc = c - in.cell_base;
     const int ci = (int)(lc % in.imax), cj = (int)(lc / in.imax);
     const int rec = a.recompute[c];
-    const double dt = st.dt;
-    const double ldx0 = in.dx / (double)S, ldx1 = in.dy / (double)S;
+    const T dt = (T)st.dt;
+    const T ldx0 = (T)(in.dx / (double)S), ldx1 = (T)(in.dy / (double)S);
     const bool dmr = (Sys::ID == kSysEuler) && in.bc_mode == 1;
 
     // ---- gather the subcell data of the 3x3 neighbourhood (only the strip
-    // the reconstruction reads): olduh projections or Lh of limited cells
+    // the reconstruction reads): get_subcell_data of olduh (sum-factorised:
+    // the y contraction of each neighbour once, then x; the reference's
+    // summation order) or Lh of limited cells
+    if (t < 9) {
+      const int bi = t % 3 - 1, bj = t / 3 - 1;
+      const int in_ = nb_index(ci, bi, in.imax, in.bc[0], in.bc[1]);
+      const int jn_ = nb_index(cj, bj, in.jmax, in.bc[2], in.bc[3]);
+      const long long nc = in.cell_base + in_ + (long long)in.imax * jn_;
+      nbc[t] = nc;
+      nbs[t] = a.status[par][nc];
+    }
+    if (t == 0) {
+      flag[0] = 0;
+      *cmaxp = 0ull;
+    }
+    __syncthreads();
+    for (int p = t; p < 9 * P2 * V; p += NT) {
+      const int n = p / (P2 * V), r = p - n * (P2 * V);
+      const int node = r / V, v = r - node * V;
+      if (nbs[n] == 0) NB[(n * V + v) * P2 + node] = (T)a.uh[par][(size_t)nbc[n] * P2 * V + r];
+    }
+    __syncthreads();
+    for (int p = t; p < 9 * V * P * S; p += NT) {
+      const int n = p / (V * P * S);
+      if (nbs[n] != 0) continue;
+      const int r = p - n * (V * P * S);
+      const int v = r / (P * S), kk = (r / S) % P, sb = r % S;
+      const T* u = NB + (n * V + v) * P2;
+      T ly = T(0);
+#pragma unroll
+      for (int m = 0; m < P; ++m) ly = ly + u[kk + P * m] * limT[sb + S * m];
+      LYN[p] = ly;
+    }
+    __syncthreads();
     for (int p = t; p < R * R; p += NT) {
       const int ii = p % R - 1, jj = p / R - 1;
       const int bi = ii < 1 ? -1 : (ii > S ? 1 : 0), bj = jj < 1 ? -1 : (jj > S ? 1 : 0);
       const int sa = ii - 1 - bi * S, sb = jj - 1 - bj * S;
-      const int in_ = nb_index(ci, bi, in.imax, in.bc[0], in.bc[1]);
-      const int jn_ = nb_index(cj, bj, in.jmax, in.bc[2], in.bc[3]);
-      const long long nc = in.cell_base + in_ + (long long)in.imax * jn_;
-      double val[V];
-      if (a.status[par][nc] == 0) {
-        // get_subcell_data of olduh at subcell (sa, sb): y contraction then x
-        const double* uo = a.uh[par] + (size_t)nc * P2 * V;
+      const int n = (bi + 1) + 3 * (bj + 1);
+      T val[V];
+      if (nbs[n] == 0) {
 #pragma unroll
         for (int v = 0; v < V; ++v) {
-          double acc = 0.0;
+          const T* ly = LYN + (size_t)(n * V + v) * P * S + sb;
+          T acc = T(0);
 #pragma unroll
-          for (int kk = 0; kk < P; ++kk) {
-            double ly = 0.0;
-#pragma unroll
-            for (int m = 0; m < P; ++m) ly = ly + uo[(kk + P * m) * V + v] * op.uh2lim[sb + S * m];
-            acc = acc + ly * op.uh2lim[sa + S * kk];
-          }
+          for (int kk = 0; kk < P; ++kk) acc = acc + ly[kk * S] * limT[sa + S * kk];
           val[v] = acc;
         }
       } else {
-        const double* L = a.lh[par] + ((size_t)nc * S * S + sa + S * sb) * V;
+        const double* L = a.lh[par] + ((size_t)nbc[n] * S * S + sa + S * sb) * V;
 #pragma unroll
-        for (int v = 0; v < V; ++v) val[v] = L[v];
+        for (int v = 0; v < V; ++v) val[v] = (T)L[v];
       }
       if constexpr (Sys::ID == kSysEuler) {
         if (dmr) {  // Euler/limiter.f90:487-522, applied in the reference's order
-          double Qbc[4];
+          T Qbc[4], Vb[4];
           if (ci == 0 && ii <= 0) {
-            EulerSys::prim2cons(ph, fc.Va, Qbc);
+            for (int v = 0; v < 4; ++v) Vb[v] = (T)fc.Va[v];
+            EulerSys::prim2cons(pc, Vb, Qbc);
             for (int v = 0; v < 4; ++v) val[v] = Qbc[v];
           }
           if (cj == 0 && jj <= 0 && (double)(ci + 1) * in.dx > 1.0 / 6.0) val[2] = -val[2];
           if (cj == in.jmax - 1 && jj >= S + 1) {
             const double x_sw = fc.xsw0 + fc.xsw1 * st.time;
-            EulerSys::prim2cons(ph, ((double)(ci + 1) * in.dx <= x_sw) ? fc.Va : fc.Vb, Qbc);
+            const double* src = ((double)(ci + 1) * in.dx <= x_sw) ? fc.Va : fc.Vb;
+            for (int v = 0; v < 4; ++v) Vb[v] = (T)src[v];
+            EulerSys::prim2cons(pc, Vb, Qbc);
             for (int v = 0; v < 4; ++v) val[v] = Qbc[v];
           }
         }
@@ -187,22 +250,18 @@ __global__ void __launch_bounds__(SubCfg<Sys, N>::THREADS) k_subcell(BatchArgs a
 #pragma unroll
       for (int v = 0; v < V; ++v) SU(v, ii, jj) = val[v];
     }
-    if (t == 0) {
-      flag[0] = 0;
-      *cmaxp = 0ull;
-    }
     __syncthreads();
 
     // ---- MUSCL-Hancock reconstruction on subcells 0..S+1
     for (int p = t; p < H * H; p += NT) {
       const int ii = p % H, jj = p / H;
-      double Qt[V], FLx[2 * V], FRx[2 * V], FLy[2 * V], FRy[2 * V];
+      T Qt[V], FLx[2 * V], FRx[2 * V], FLy[2 * V], FRy[2 * V];
       const bool interior = ii >= 1 && ii <= S && jj >= 1 && jj <= S;
       // Euler computes slopes for interior subcells only (halo slopes stay 0,
       // Euler/limiter.f90:529-536); BN also on the halo (BN :486-492)
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        double sx = 0.0, sy = 0.0;
+        T sx = T(0), sy = T(0);
         if (BN || interior) {
           sx = minmod(SU(v, ii + 1, jj) - SU(v, ii, jj), SU(v, ii, jj) - SU(v, ii - 1, jj));
           sy = minmod(SU(v, ii, jj + 1) - SU(v, ii, jj), SU(v, ii, jj) - SU(v, ii, jj - 1));
@@ -210,21 +269,21 @@ __global__ void __launch_bounds__(SubCfg<Sys, N>::THREADS) k_subcell(BatchArgs a
         slx[hx(v, ii, jj)] = sx;
         sly[hx(v, ii, jj)] = sy;
       }
-      double q0[V], wl[V], wr[V];
+      T q0[V], wl[V], wr[V];
 #pragma unroll
       for (int v = 0; v < V; ++v) q0[v] = SU(v, ii, jj);
-      double src[V];
+      T src[V];
       if constexpr (BN) {
         // Baer-Nunziato/limiter.f90:494-497
-        BNSys::src_ncp(ph, q0, slx[hx(8, ii, jj)] / ldx0, sly[hx(8, ii, jj)] / ldx1, src);
+        BNSys::src_ncp(pc, q0, slx[hx(8, ii, jj)] / ldx0, sly[hx(8, ii, jj)] / ldx1, src);
       }
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        wl[v] = q0[v] - 0.5 * slx[hx(v, ii, jj)];
-        wr[v] = q0[v] + 0.5 * slx[hx(v, ii, jj)];
+        wl[v] = q0[v] - T(0.5) * slx[hx(v, ii, jj)];
+        wr[v] = q0[v] + T(0.5) * slx[hx(v, ii, jj)];
       }
-      Sys::flux(ph, wl, FLx);
-      Sys::flux(ph, wr, FRx);
+      Sys::flux(pc, wl, FLx);
+      Sys::flux(pc, wr, FRx);
 #pragma unroll
       for (int v = 0; v < V; ++v) {
         if constexpr (BN) Qt[v] = src[v] - (FRx[v] - FLx[v]) / ldx0;
@@ -234,29 +293,33 @@ __global__ void __launch_bounds__(SubCfg<Sys, N>::THREADS) k_subcell(BatchArgs a
       }
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        wl[v] = q0[v] - 0.5 * sly[hx(v, ii, jj)];
-        wr[v] = q0[v] + 0.5 * sly[hx(v, ii, jj)];
+        wl[v] = q0[v] - T(0.5) * sly[hx(v, ii, jj)];
+        wr[v] = q0[v] + T(0.5) * sly[hx(v, ii, jj)];
       }
-      Sys::flux(ph, wl, FLy);
-      Sys::flux(ph, wr, FRy);
+      Sys::flux(pc, wl, FLy);
+      Sys::flux(pc, wr, FRy);
 #pragma unroll
       for (int v = 0; v < V; ++v) {
         Qt[v] = Qt[v] - (FRy[V + v] - FLy[V + v]) / ldx1;
         slt[hx(v, ii, jj)] = Qt[v];
-        wLx[hx(v, ii, jj)] = wLx[hx(v, ii, jj)] + 0.5 * dt * Qt[v];
-        wRx[hx(v, ii, jj)] = wRx[hx(v, ii, jj)] + 0.5 * dt * Qt[v];
-        wLy[hx(v, ii, jj)] = wl[v] + 0.5 * dt * Qt[v];
-        wRy[hx(v, ii, jj)] = wr[v] + 0.5 * dt * Qt[v];
+        wLx[hx(v, ii, jj)] = wLx[hx(v, ii, jj)] + T(0.5) * dt * Qt[v];
+        wRx[hx(v, ii, jj)] = wRx[hx(v, ii, jj)] + T(0.5) * dt * Qt[v];
+        wLy[hx(v, ii, jj)] = wl[v] + T(0.5) * dt * Qt[v];
+        wRy[hx(v, ii, jj)] = wr[v] + T(0.5) * dt * Qt[v];
       }
     }
     __syncthreads();
 
-    if constexpr (!BN) {
-      // edge fluxes Fx(1..S+1, 1..S), Fy(1..S, 1..S+1), Euler/limiter.f90:571-588
-      for (int p = t; p < 2 * (S + 1) * S; p += NT) {
-        const bool xd = p < (S + 1) * S;
-        const int q = xd ? p : p - (S + 1) * S;
-        double QL[V], QR[V], F[V], Dd[V];
+    // ---- edge fluxes Fx(1..S+1, 1..S), Fy(1..S, 1..S+1) (Euler/limiter.f90:571-588);
+    // BN's four Rusanov fluxes per subcell (Baer-Nunziato/limiter.f90:526-545)
+    // are those of its edges, each formed once here from the same states
+    {
+      T* EX = EF;
+      T* EY = EF + (BN ? 2 : 1) * V * NE;
+      for (int p = t; p < 2 * NE; p += NT) {
+        const bool xd = p < NE;
+        const int q = xd ? p : p - NE;
+        T QL[V], QR[V], F[V], Dd[V];
         int ii, jj;
         if (xd) { ii = q % (S + 1) + 1; jj = q / (S + 1) + 1; }
         else { ii = q % S + 1; jj = q / S + 1; }
@@ -265,63 +328,50 @@ __global__ void __launch_bounds__(SubCfg<Sys, N>::THREADS) k_subcell(BatchArgs a
           QL[v] = xd ? wRx[hx(v, ii - 1, jj)] : wRy[hx(v, ii, jj - 1)];
           QR[v] = xd ? wLx[hx(v, ii, jj)] : wLy[hx(v, ii, jj)];
         }
-        rusanov_s<Sys>(ph, QL, QR, xd ? 0 : 1, F, Dd);
-        double* dst = xd ? Fx : Fy;
+        rusanov_s<Sys>(pc, QL, QR, xd ? 0 : 1, F, Dd);
+        T* dst = xd ? EX : EY;
 #pragma unroll
-        for (int v = 0; v < V; ++v) dst[v * (S + 1) * S + q] = F[v];
-      }
-      __syncthreads();
-      // first-order FV update, Euler/limiter.f90:592-597
-      for (int p = t; p < S * S; p += NT) {
-        const int ii = p % S + 1, jj = p / S + 1;
+        for (int v = 0; v < V; ++v) dst[v * NE + q] = F[v];
+        if constexpr (BN) {
 #pragma unroll
-        for (int v = 0; v < V; ++v) {
-          const double fxp = Fx[v * (S + 1) * S + ii + (S + 1) * (jj - 1)];
-          const double fxm = Fx[v * (S + 1) * S + (ii - 1) + (S + 1) * (jj - 1)];
-          const double fyp = Fy[v * (S + 1) * S + (ii - 1) + S * jj];
-          const double fym = Fy[v * (S + 1) * S + (ii - 1) + S * (jj - 1)];
-          sub1[v * S * S + p] = SU(v, ii, jj) - dt / ldx0 * (fxp - fxm) - dt / ldx1 * (fyp - fym);
+          for (int v = 0; v < V; ++v) dst[(V + v) * NE + q] = Dd[v];
         }
       }
-    } else {
-      // Baer-Nunziato/limiter.f90:526-545: four fluxes per subcell
+      __syncthreads();
       for (int p = t; p < S * S; p += NT) {
         const int ii = p % S + 1, jj = p / S + 1;
-        double qh[V], src[V], fpl[V], fmi[V], gpl[V], gmi[V], Dpx[V], Dmx[V], Dpy[V], Dmy[V], QL[V], QR[V];
+        const int xp = ii + (S + 1) * (jj - 1), xm = (ii - 1) + (S + 1) * (jj - 1);
+        const int yp = (ii - 1) + S * jj, ym = (ii - 1) + S * (jj - 1);
+        if constexpr (!BN) {
+          // first-order FV update, Euler/limiter.f90:592-597
 #pragma unroll
-        for (int v = 0; v < V; ++v) qh[v] = SU(v, ii, jj) + 0.5 * dt * slt[hx(v, ii, jj)];
-        BNSys::src_ncp(ph, qh, slx[hx(8, ii, jj)] / ldx0, sly[hx(8, ii, jj)] / ldx1, src);
+          for (int v = 0; v < V; ++v)
+            sub1[v * S * S + p] = SU(v, ii, jj) - dt / ldx0 * (EX[v * NE + xp] - EX[v * NE + xm]) -
+                                  dt / ldx1 * (EY[v * NE + yp] - EY[v * NE + ym]);
+        } else {
+          T qh[V], src[V];
 #pragma unroll
-        for (int v = 0; v < V; ++v) { QL[v] = wRx[hx(v, ii, jj)]; QR[v] = wLx[hx(v, ii + 1, jj)]; }
-        rusanov_s<Sys>(ph, QL, QR, 0, fpl, Dpx);
+          for (int v = 0; v < V; ++v) qh[v] = SU(v, ii, jj) + T(0.5) * dt * slt[hx(v, ii, jj)];
+          BNSys::src_ncp(pc, qh, slx[hx(8, ii, jj)] / ldx0, sly[hx(8, ii, jj)] / ldx1, src);
 #pragma unroll
-        for (int v = 0; v < V; ++v) { QL[v] = wRx[hx(v, ii - 1, jj)]; QR[v] = wLx[hx(v, ii, jj)]; }
-        rusanov_s<Sys>(ph, QL, QR, 0, fmi, Dmx);
-#pragma unroll
-        for (int v = 0; v < V; ++v) { QL[v] = wRy[hx(v, ii, jj)]; QR[v] = wLy[hx(v, ii, jj + 1)]; }
-        rusanov_s<Sys>(ph, QL, QR, 1, gpl, Dpy);
-#pragma unroll
-        for (int v = 0; v < V; ++v) { QL[v] = wRy[hx(v, ii, jj - 1)]; QR[v] = wLy[hx(v, ii, jj)]; }
-        rusanov_s<Sys>(ph, QL, QR, 1, gmi, Dmy);
-#pragma unroll
-        for (int v = 0; v < V; ++v)
-          sub1[v * S * S + p] = SU(v, ii, jj) - dt / ldx0 * (fpl[v] - fmi[v]) - dt / ldx1 * (gpl[v] - gmi[v]) -
-                                dt / ldx0 * 0.5 * (Dpx[v] + Dmx[v]) - dt / ldx1 * 0.5 * (Dpy[v] + Dmy[v]) + dt * src[v];
+          for (int v = 0; v < V; ++v)
+            sub1[v * S * S + p] = SU(v, ii, jj) - dt / ldx0 * (EX[v * NE + xp] - EX[v * NE + xm]) -
+                                  dt / ldx1 * (EY[v * NE + yp] - EY[v * NE + ym]) -
+                                  dt / ldx0 * T(0.5) * (EX[(V + v) * NE + xp] + EX[(V + v) * NE + xm]) -
+                                  dt / ldx1 * T(0.5) * (EY[(V + v) * NE + yp] + EY[(V + v) * NE + ym]) +
+                                  dt * src[v];
+        }
       }
     }
     __syncthreads();
 
     // ---- put_subcell_data (Euler/limiter.f90:74-98): luhy then luh
-    double* LUY = scr;                 // [V][P][S]: luhy(v, iii, s) at (v*P + s)*S + iii
-    double* UN = scr + V * S * P;      // [V][P2]
-    double* LY = UN + V * P2;          // DMP y pass [V][S][P]
-    double* LB = LY + V * S * P;       // [V][P][P]
     for (int p = t; p < S * P; p += NT) {
       const int iii = p % S, s = p / S;
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        double acc = 0.0;
-        for (int kk = 0; kk < S; ++kk) acc = acc + sub1[v * S * S + iii + S * kk] * op.lim2uh[s + P * kk];
+        T acc = T(0);
+        for (int kk = 0; kk < S; ++kk) acc = acc + sub1[v * S * S + iii + S * kk] * l2uT[s + P * kk];
         LUY[(v * P + s) * S + iii] = acc;
       }
     }
@@ -331,22 +381,21 @@ __global__ void __launch_bounds__(SubCfg<Sys, N>::THREADS) k_subcell(BatchArgs a
       const int s1 = p % P, jjj = p / P;
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        double acc = 0.0;
-        for (int kk = 0; kk < S; ++kk) acc = acc + LUY[(v * P + jjj) * S + kk] * op.lim2uh[s1 + P * kk];
-        UN[v * P2 + p] = acc;
-        uout[p * V + v] = acc;
+        T acc = T(0);
+        for (int kk = 0; kk < S; ++kk) acc = acc + LUY[(v * P + jjj) * S + kk] * l2uT[s1 + P * kk];
+        UN[v * P2 + p] = (double)acc;
+        uout[p * V + v] = (double)acc;
       }
     }
     __syncthreads();
-
     // ---- DMP of the new polynomial (recompute = 2) and the next min/max
-    Proj<N, V>::ypass(UN, LY, LB, op, t, NT);
+    Proj<N, V, double>::ypass(UN, LY, LB, opsm, opsm + S * P, t, NT);
     __syncthreads();
     double mn[V], mx[V];
     bool posfail = false;
 #pragma unroll
     for (int v = 0; v < V; ++v) { mn[v] = kInf; mx[v] = -kInf; }
-    Proj<N, V>::template xpass_minmax<Sys>(UN, LY, LB, op, ph, t, NT, mn, mx, posfail);
+    Proj<N, V, double>::template xpass_minmax<Sys>(UN, LY, LB, opsm, opsm + S * P, ph, t, NT, mn, mx, posfail);
 #pragma unroll
     for (int v = 0; v < V; ++v) { red[v * NT + t] = mn[v]; red[(V + v) * NT + t] = mx[v]; }
     if (posfail) atomicOr(&flag[0], 1);
@@ -387,12 +436,16 @@ __global__ void __launch_bounds__(SubCfg<Sys, N>::THREADS) k_subcell(BatchArgs a
       double* nl = a.lh[par ^ 1] + (size_t)c * S * S * V;
       for (int p = t; p < S * S; p += NT)
 #pragma unroll
-        for (int v = 0; v < V; ++v) nl[p * V + v] = sub1[v * S * S + p];
+        for (int v = 0; v < V; ++v) nl[p * V + v] = (double)sub1[v * S * S + p];
       // min/max over the new subcell data (get_min_max of the next step)
       for (int v = 0; v < V; ++v) { mn[v] = kInf; mx[v] = -kInf; }
       for (int p = t; p < S * S; p += NT)
 #pragma unroll
-        for (int v = 0; v < V; ++v) { mn[v] = fmin(mn[v], sub1[v * S * S + p]); mx[v] = fmax(mx[v], sub1[v * S * S + p]); }
+        for (int v = 0; v < V; ++v) {
+          const double x = (double)sub1[v * S * S + p];
+          mn[v] = fmin(mn[v], x);
+          mx[v] = fmax(mx[v], x);
+        }
     }
     __syncthreads();
     if (limited) {

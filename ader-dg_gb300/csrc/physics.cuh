@@ -17,15 +17,38 @@
 
 namespace aderdg {
 
+// Physical constants in the compute type T, formed once from Phys with the
+// same FP64 expressions the reference writes inline (gamma - 1, gamma_s *
+// pi_s, ...): for T = double every function below rounds exactly like the
+// reference expression; T = float serves the FP32-mixed subcell re-solve.
+template <class T>
+struct PhysC {
+  T gamma, gm1;                    // Euler
+  T gs, gg, ps, pg, gs1, gg1, gsps, ggpg;  // Baer-Nunziato
+  __device__ explicit PhysC(const Phys& ph)
+      : gamma(T(ph.gamma)), gm1(T(ph.gamma - 1.0)), gs(T(ph.gs)), gg(T(ph.gg)), ps(T(ph.ps)), pg(T(ph.pg)),
+        gs1(T(ph.gs - 1.0)), gg1(T(ph.gg - 1.0)), gsps(T(ph.gs * ph.ps)), ggpg(T(ph.gg * ph.pg)) {}
+};
+template <class T> __device__ __forceinline__ T tabs(T x) {
+  if constexpr (sizeof(T) == 4) return fabsf(x); else return fabs(x);
+}
+template <class T> __device__ __forceinline__ T tmax(T a, T b) {
+  if constexpr (sizeof(T) == 4) return fmaxf(a, b); else return fmax(a, b);
+}
+template <class T> __device__ __forceinline__ T tsqrt(T x) {
+  if constexpr (sizeof(T) == 4) return sqrtf(x); else return sqrt(x);
+}
+
 // ---------------------------------------------------------------------------
 struct EulerSys {
   static constexpr int V = 4;
   static constexpr int ID = kSysEuler;
 
   // Euler/pde.f90:46-69; F[d*V + v]
-  __device__ static void flux(const Phys& ph, const double* Q, double* F) {
-    double irho = 1.0 / Q[0];
-    double p = (ph.gamma - 1.0) * (Q[3] - 0.5 * (Q[1] * Q[1] + Q[2] * Q[2]) * irho);
+  template <class T>
+  __device__ static void flux(const PhysC<T>& pc, const T* Q, T* F) {
+    T irho = T(1) / Q[0];
+    T p = pc.gm1 * (Q[3] - T(0.5) * (Q[1] * Q[1] + Q[2] * Q[2]) * irho);
     F[0] = Q[1];
     F[1] = irho * Q[1] * Q[1] + p;
     F[2] = irho * Q[1] * Q[2];
@@ -35,13 +58,16 @@ struct EulerSys {
     F[6] = irho * Q[2] * Q[2] + p;
     F[7] = irho * Q[2] * (Q[3] + p);
   }
+  __device__ static void flux(const Phys& ph, const double* Q, double* F) { flux<double>(PhysC<double>(ph), Q, F); }
   // maxval(abs(Lambda)) of Euler/pde.f90:75-91 for the unit normal of axis d
-  __device__ static double max_eig(const Phys& ph, const double* Q, int d) {
-    double u = (d == 0 ? Q[1] : Q[2]) / Q[0];
-    double p = (ph.gamma - 1.0) * (Q[3] - 0.5 * (Q[1] * Q[1] + Q[2] * Q[2]) / Q[0]);
-    double c = sqrt(ph.gamma * p / Q[0]);
-    return fmax(fmax(fabs(u - c), fabs(u)), fabs(u + c));
+  template <class T>
+  __device__ static T max_eig(const PhysC<T>& pc, const T* Q, int d) {
+    T u = (d == 0 ? Q[1] : Q[2]) / Q[0];
+    T p = pc.gm1 * (Q[3] - T(0.5) * (Q[1] * Q[1] + Q[2] * Q[2]) / Q[0]);
+    T c = tsqrt(pc.gamma * p / Q[0]);
+    return tmax(tmax(tabs(u - c), tabs(u)), tabs(u + c));
   }
+  __device__ static double max_eig(const Phys& ph, const double* Q, int d) { return max_eig<double>(PhysC<double>(ph), Q, d); }
   // both axes at once: the pressure and sound speed do not depend on the
   // normal, so they are formed once (same expressions, same rounding)
   __device__ static void max_eig2(const Phys& ph, const double* Q, double& ex, double& ey) {
@@ -51,23 +77,41 @@ struct EulerSys {
     ex = fmax(fmax(fabs(u - c), fabs(u)), fabs(u + c));
     ey = fmax(fmax(fabs(v - c), fabs(v)), fabs(v + c));
   }
-  // FP32 eigenvalues for the mixed-precision CFL (the max reduction stays FP64)
-  __device__ static void max_eig2_f32(const Phys& ph, const double* Qd, double& ex, double& ey) {
-    const float q0 = (float)Qd[0], q1 = (float)Qd[1], q2 = (float)Qd[2], q3 = (float)Qd[3];
-    const float iq = 1.0f / q0;
-    const float p = (float)(ph.gamma - 1.0) * (q3 - 0.5f * (q1 * q1 + q2 * q2) * iq);
-    const float c = sqrtf((float)ph.gamma * p * iq);
-    const float u = q1 * iq, v = q2 * iq;
-    ex = (double)(fabsf(u) + c);
-    ey = (double)(fabsf(v) + c);
+  // Constants of the FP32-mixed cell kernel (CFL eigenvalues, admissibility pre-test).
+  struct FConst {
+    float gm1, gamma;
+    __device__ explicit FConst(const Phys& ph) : gm1((float)(ph.gamma - 1.0)), gamma((float)ph.gamma) {}
+  };
+  // FP32 eigenvalues for the mixed-precision CFL
+  __device__ static void max_eig2_f32(const FConst& fc, const float* q, float& ex, float& ey) {
+    const float iq = 1.0f / q[0];
+    const float p = fc.gm1 * (q[3] - 0.5f * (q[1] * q[1] + q[2] * q[2]) * iq);
+    const float c = sqrtf(fc.gamma * p * iq);
+    ex = fabsf(q[1] * iq) + c;
+    ey = fabsf(q[2] * iq) + c;
+  }
+  // True when every state within e (componentwise) of the FP32 state q passes
+  // positive()'s test, with a margin for this evaluation's own rounding.  False
+  // means "not settled": the caller re-evaluates the state in FP64.
+  __device__ static bool admissible_box_f32(const FConst& fc, const float* q, const float* e) {
+    const float r_lo = q[0] - e[0];
+    if (!(r_lo > 2.0e-12f) || !(fc.gm1 > 0.0f)) return false;
+    const float m1 = fabsf(q[1]) + e[1], m2 = fabsf(q[2]) + e[2];
+    const float ke_hi = 0.5f * (m1 * m1 + m2 * m2) / r_lo;
+    const float x_lo = (q[3] - e[3]) - ke_hi;
+    const float margin = 1.0e-5f * (fabsf(q[3]) + e[3] + ke_hi);
+    const float p_lo = fc.gm1 * (x_lo - margin);
+    return p_lo > 2.0e-12f && margin < 1.0e30f;
   }
   // Euler/pde.f90:29-40
-  __device__ static void prim2cons(const Phys& ph, const double* Vp, double* Q) {
+  template <class T>
+  __device__ static void prim2cons(const PhysC<T>& pc, const T* Vp, T* Q) {
     Q[0] = Vp[0];
     Q[1] = Vp[0] * Vp[1];
     Q[2] = Vp[0] * Vp[2];
-    Q[3] = Vp[3] / (ph.gamma - 1) + 0.5 * Vp[0] * (Vp[1] * Vp[1] + Vp[2] * Vp[2]);
+    Q[3] = Vp[3] / pc.gm1 + T(0.5) * Vp[0] * (Vp[1] * Vp[1] + Vp[2] * Vp[2]);
   }
+  __device__ static void prim2cons(const Phys& ph, const double* Vp, double* Q) { prim2cons<double>(PhysC<double>(ph), Vp, Q); }
   // Euler/pde.f90:120-145: true when admissible
   __device__ static bool positive(const Phys& ph, const double* Q) {
     double irho = 1.0 / Q[0];
@@ -118,26 +162,29 @@ struct BNSys {
   static constexpr int ID = kSysBN;
 
   // Baer-Nunziato/pde.f90:8-43
-  __device__ static void cons2prim(const Phys& ph, const double* Q, double* Vp) {
-    double phi_s = Q[8], phi_g = 1.0 - Q[8];
-    double rho_s = Q[0] / phi_s, rho_g = Q[4] / phi_g;
-    double u_s = Q[1] / Q[0], v_s = Q[2] / Q[0];
-    double u_g = Q[5] / Q[4], v_g = Q[6] / Q[4];
-    double E_s = Q[3] / phi_s, E_g = Q[7] / phi_g;
-    double p_s = (ph.gs - 1.0) * (E_s - 0.5 * rho_s * (u_s * u_s + v_s * v_s)) - ph.gs * ph.ps;
-    double p_g = (ph.gg - 1.0) * (E_g - 0.5 * rho_g * (u_g * u_g + v_g * v_g)) - ph.gg * ph.pg;
+  template <class T>
+  __device__ static void cons2prim(const PhysC<T>& pc, const T* Q, T* Vp) {
+    T phi_s = Q[8], phi_g = T(1) - Q[8];
+    T rho_s = Q[0] / phi_s, rho_g = Q[4] / phi_g;
+    T u_s = Q[1] / Q[0], v_s = Q[2] / Q[0];
+    T u_g = Q[5] / Q[4], v_g = Q[6] / Q[4];
+    T E_s = Q[3] / phi_s, E_g = Q[7] / phi_g;
+    T p_s = pc.gs1 * (E_s - T(0.5) * rho_s * (u_s * u_s + v_s * v_s)) - pc.gsps;
+    T p_g = pc.gg1 * (E_g - T(0.5) * rho_g * (u_g * u_g + v_g * v_g)) - pc.ggpg;
     Vp[0] = rho_s; Vp[1] = u_s; Vp[2] = v_s; Vp[3] = p_s;
     Vp[4] = rho_g; Vp[5] = u_g; Vp[6] = v_g; Vp[7] = p_g; Vp[8] = phi_s;
   }
+  __device__ static void cons2prim(const Phys& ph, const double* Q, double* Vp) { cons2prim<double>(PhysC<double>(ph), Q, Vp); }
   // Baer-Nunziato/pde.f90:74-119
-  __device__ static void flux(const Phys& ph, const double* Q, double* F) {
-    double phi_s = Q[8], phi_g = 1.0 - Q[8];
-    double rho_s = Q[0] / phi_s, rho_g = Q[4] / phi_g;
-    double u_s = Q[1] / Q[0], v_s = Q[2] / Q[0];
-    double u_g = Q[5] / Q[4], v_g = Q[6] / Q[4];
-    double E_s = Q[3] / phi_s, E_g = Q[7] / phi_g;
-    double p_s = (ph.gs - 1.0) * (E_s - 0.5 * rho_s * (u_s * u_s + v_s * v_s)) - ph.gs * ph.ps;
-    double p_g = (ph.gg - 1.0) * (E_g - 0.5 * rho_g * (u_g * u_g + v_g * v_g)) - ph.gg * ph.pg;
+  template <class T>
+  __device__ static void flux(const PhysC<T>& pc, const T* Q, T* F) {
+    T phi_s = Q[8], phi_g = T(1) - Q[8];
+    T rho_s = Q[0] / phi_s, rho_g = Q[4] / phi_g;
+    T u_s = Q[1] / Q[0], v_s = Q[2] / Q[0];
+    T u_g = Q[5] / Q[4], v_g = Q[6] / Q[4];
+    T E_s = Q[3] / phi_s, E_g = Q[7] / phi_g;
+    T p_s = pc.gs1 * (E_s - T(0.5) * rho_s * (u_s * u_s + v_s * v_s)) - pc.gsps;
+    T p_g = pc.gg1 * (E_g - T(0.5) * rho_g * (u_g * u_g + v_g * v_g)) - pc.ggpg;
     F[0] = phi_s * rho_s * u_s;
     F[1] = phi_s * (rho_s * u_s * u_s + p_s);
     F[2] = phi_s * rho_s * u_s * v_s;
@@ -146,7 +193,7 @@ struct BNSys {
     F[5] = phi_g * (rho_g * u_g * u_g + p_g);
     F[6] = phi_g * rho_g * u_g * v_g;
     F[7] = phi_g * u_g * (E_g + p_g);
-    F[8] = 0.0;
+    F[8] = T(0);
     F[9] = phi_s * rho_s * v_s;
     F[10] = phi_s * rho_s * u_s * v_s;
     F[11] = phi_s * (rho_s * v_s * v_s + p_s);
@@ -155,24 +202,27 @@ struct BNSys {
     F[14] = phi_g * rho_g * u_g * v_g;
     F[15] = phi_g * (rho_g * v_g * v_g + p_g);
     F[16] = phi_g * v_g * (E_g + p_g);
-    F[17] = 0.0;
+    F[17] = T(0);
   }
+  __device__ static void flux(const Phys& ph, const double* Q, double* F) { flux<double>(PhysC<double>(ph), Q, F); }
   // Baer-Nunziato/pde.f90:125-144
-  __device__ static double max_eig(const Phys& ph, const double* Q, int d) {
-    double Vp[9];
-    cons2prim(ph, Q, Vp);
-    double u_s = (d == 0) ? Vp[1] * 1.0 + Vp[2] * 0.0 : Vp[1] * 0.0 + Vp[2] * 1.0;
-    double u_g = (d == 0) ? Vp[5] * 1.0 + Vp[6] * 0.0 : Vp[5] * 0.0 + Vp[6] * 1.0;
-    double a_s = sqrt(ph.gs * (Vp[3] + ph.ps) / Vp[0]);
-    double a_g = sqrt(ph.gg * (Vp[7] + ph.pg) / Vp[4]);
-    double m = fabs(u_g - a_g);
-    m = fmax(m, fabs(u_g + a_g));
-    m = fmax(m, fabs(u_s - a_s));
-    m = fmax(m, fabs(u_s + a_s));
-    m = fmax(m, fabs(u_g));
-    m = fmax(m, fabs(u_s));
+  template <class T>
+  __device__ static T max_eig(const PhysC<T>& pc, const T* Q, int d) {
+    T Vp[9];
+    cons2prim(pc, Q, Vp);
+    T u_s = (d == 0) ? Vp[1] * T(1) + Vp[2] * T(0) : Vp[1] * T(0) + Vp[2] * T(1);
+    T u_g = (d == 0) ? Vp[5] * T(1) + Vp[6] * T(0) : Vp[5] * T(0) + Vp[6] * T(1);
+    T a_s = tsqrt(pc.gs * (Vp[3] + pc.ps) / Vp[0]);
+    T a_g = tsqrt(pc.gg * (Vp[7] + pc.pg) / Vp[4]);
+    T m = tabs(u_g - a_g);
+    m = tmax(m, tabs(u_g + a_g));
+    m = tmax(m, tabs(u_s - a_s));
+    m = tmax(m, tabs(u_s + a_s));
+    m = tmax(m, tabs(u_g));
+    m = tmax(m, tabs(u_s));
     return m;
   }
+  __device__ static double max_eig(const Phys& ph, const double* Q, int d) { return max_eig<double>(PhysC<double>(ph), Q, d); }
   __device__ static void max_eig2(const Phys& ph, const double* Q, double& ex, double& ey) {
     double Vp[9];
     cons2prim(ph, Q, Vp);
@@ -190,34 +240,60 @@ struct BNSys {
       (d == 0 ? ex : ey) = m;
     }
   }
-  __device__ static void max_eig2_f32(const Phys& ph, const double* Qd, double& ex, double& ey) {
-    float q[9];
-    for (int v = 0; v < 9; ++v) q[v] = (float)Qd[v];
+  struct FConst {
+    float gs, gg, gs1, gg1, gsps, ggpg, ps, pg;
+    __device__ explicit FConst(const Phys& ph)
+        : gs((float)ph.gs), gg((float)ph.gg), gs1((float)(ph.gs - 1.0)), gg1((float)(ph.gg - 1.0)),
+          gsps((float)(ph.gs * ph.ps)), ggpg((float)(ph.gg * ph.pg)), ps((float)ph.ps), pg((float)ph.pg) {}
+  };
+  __device__ static void max_eig2_f32(const FConst& fc, const float* q, float& ex, float& ey) {
     const float a = q[8], b = 1.0f - q[8];
     const float irs = 1.0f / q[0], irg = 1.0f / q[4];
     const float us = q[1] * irs, vs = q[2] * irs, ug = q[5] * irg, vg = q[6] * irg;
     const float rs = q[0] / a, rg = q[4] / b;
-    const float ps = (float)(ph.gs - 1.0) * (q[3] / a - 0.5f * rs * (us * us + vs * vs)) - (float)(ph.gs * ph.ps);
-    const float pg = (float)(ph.gg - 1.0) * (q[7] / b - 0.5f * rg * (ug * ug + vg * vg)) - (float)(ph.gg * ph.pg);
-    const float as = sqrtf((float)ph.gs * (ps + (float)ph.ps) / rs), ag = sqrtf((float)ph.gg * (pg + (float)ph.pg) / rg);
-    ex = (double)fmaxf(fabsf(ug) + ag, fabsf(us) + as);
-    ey = (double)fmaxf(fabsf(vg) + ag, fabsf(vs) + as);
+    const float ps = fc.gs1 * (q[3] / a - 0.5f * rs * (us * us + vs * vs)) - fc.gsps;
+    const float pg = fc.gg1 * (q[7] / b - 0.5f * rg * (ug * ug + vg * vg)) - fc.ggpg;
+    const float as = sqrtf(fc.gs * (ps + fc.ps) / rs), ag = sqrtf(fc.gg * (pg + fc.pg) / rg);
+    ex = fmaxf(fabsf(ug) + ag, fabsf(us) + as);
+    ey = fmaxf(fabsf(vg) + ag, fabsf(vs) + as);
+  }
+  // True when every state within e (componentwise) of the FP32 state q passes
+  // positive()'s test (rho_s, rho_g, p_s + pi_s, p_g + pi_g above 1e-12 and
+  // 0 < phi_s < 1), with a margin for this evaluation's own rounding.  With
+  // phi in [a_lo, a_hi]: p_s + pi_s = (gamma_s - 1) ((Q3 - ke_s) / phi - pi_s),
+  // ke_s = (Q1^2 + Q2^2) / (2 Q0), smallest at the X_lo / a end that makes it
+  // smallest.  False means "not settled": the caller re-evaluates in FP64.
+  __device__ static bool admissible_box_f32(const FConst& fc, const float* q, const float* e) {
+    const float a_lo = q[8] - e[8], a_hi = q[8] + e[8];
+    const float b_lo = 1.0f - a_hi, b_hi = 1.0f - a_lo;
+    if (!(a_lo > 1.0e-2f) || !(b_lo > 1.0e-2f) || !(fc.gs1 > 0.0f) || !(fc.gg1 > 0.0f)) return false;
+    const float q0 = q[0] - e[0], q4 = q[4] - e[4];
+    if (!(q0 > 0.0f) || !(q4 > 0.0f) || !(q0 > 4.0e-12f * a_hi) || !(q4 > 4.0e-12f * b_hi)) return false;
+    const float s1 = fabsf(q[1]) + e[1], s2 = fabsf(q[2]) + e[2];
+    const float g1 = fabsf(q[5]) + e[5], g2 = fabsf(q[6]) + e[6];
+    const float kes = 0.5f * (s1 * s1 + s2 * s2) / q0, keg = 0.5f * (g1 * g1 + g2 * g2) / q4;
+    const float xs = (q[3] - e[3]) - kes, xg = (q[7] - e[7]) - keg;
+    const float ys = xs / (xs >= 0.0f ? a_hi : a_lo) - fc.ps, yg = xg / (xg >= 0.0f ? b_hi : b_lo) - fc.pg;
+    const float ms = 1.0e-5f * ((fabsf(q[3]) + e[3] + kes) / a_lo + fabsf(fc.ps));
+    const float mg = 1.0e-5f * ((fabsf(q[7]) + e[7] + keg) / b_lo + fabsf(fc.pg));
+    return fc.gs1 * (ys - ms) > 2.0e-12f && fc.gg1 * (yg - mg) > 2.0e-12f && ms < 1.0e30f && mg < 1.0e30f;
   }
   // column 9 of PDEMatrixB (Baer-Nunziato/pde.f90:150-186); the other columns are zero
-  __device__ static void matrixB_col9(const Phys& ph, const double* Q, int d, double* b) {
-    const double nv0 = d == 0 ? 1.0 : 0.0, nv1 = d == 0 ? 0.0 : 1.0;
-    double phi_g = 1.0 - Q[8];
-    double rho_g = Q[4] / phi_g;
-    double u_s = Q[1] / Q[0], v_s = Q[2] / Q[0];
-    double u_n = nv0 * u_s + nv1 * v_s;
-    double u_g = Q[5] / Q[4], v_g = Q[6] / Q[4];
-    double E_g = Q[7] / phi_g;
-    double p_g = (ph.gg - 1.0) * (E_g - 0.5 * rho_g * (u_g * u_g + v_g * v_g)) - ph.gg * ph.pg;
-    b[0] = 0.0;
+  template <class T>
+  __device__ static void matrixB_col9(const PhysC<T>& pc, const T* Q, int d, T* b) {
+    const T nv0 = d == 0 ? T(1) : T(0), nv1 = d == 0 ? T(0) : T(1);
+    T phi_g = T(1) - Q[8];
+    T rho_g = Q[4] / phi_g;
+    T u_s = Q[1] / Q[0], v_s = Q[2] / Q[0];
+    T u_n = nv0 * u_s + nv1 * v_s;
+    T u_g = Q[5] / Q[4], v_g = Q[6] / Q[4];
+    T E_g = Q[7] / phi_g;
+    T p_g = pc.gg1 * (E_g - T(0.5) * rho_g * (u_g * u_g + v_g * v_g)) - pc.ggpg;
+    b[0] = T(0);
     b[1] = -(nv0 * p_g);
     b[2] = -(nv1 * p_g);
     b[3] = -(p_g * u_n);
-    b[4] = 0.0;
+    b[4] = T(0);
     b[5] = nv0 * p_g;
     b[6] = nv1 * p_g;
     b[7] = p_g * u_n;
@@ -225,51 +301,61 @@ struct BNSys {
   }
   // D = RoeMatrix(QL,QR) * (QR - QL): 3-point Gauss-Legendre path integral,
   // Baer-Nunziato/pde.f90:296-320 and the matmul of :348
-  __device__ static void roe_times_jump(const Phys& ph, const double* QL, const double* QR, int d, double* D) {
+  template <class T>
+  __device__ static void roe_times_jump(const PhysC<T>& pc, const T* QL, const T* QR, int d, T* D) {
     const double sq = sqrt(15.0) / 10.;
-    const double sGP[3] = {0.5 - sq, 0.5, 0.5 + sq};
-    const double wGP[3] = {5. / 18.0, 8. / 18., 5. / 18.};
-    double broe[9], b[9], Q[9];
-    for (int v = 0; v < 9; ++v) broe[v] = 0.0;
+    const T sGP[3] = {T(0.5 - sq), T(0.5), T(0.5 + sq)};
+    const T wGP[3] = {T(5. / 18.0), T(8. / 18.), T(5. / 18.)};
+    T broe[9], b[9], Q[9];
+    for (int v = 0; v < 9; ++v) broe[v] = T(0);
     for (int g = 0; g < 3; ++g) {
       for (int v = 0; v < 9; ++v) Q[v] = QL[v] + sGP[g] * (QR[v] - QL[v]);
-      matrixB_col9(ph, Q, d, b);
+      matrixB_col9(pc, Q, d, b);
       for (int v = 0; v < 9; ++v) broe[v] = broe[v] + wGP[g] * b[v];
     }
-    const double dq9 = QR[8] - QL[8];
+    const T dq9 = QR[8] - QL[8];
     for (int v = 0; v < 9; ++v) D[v] = broe[v] * dq9;
   }
+  __device__ static void roe_times_jump(const Phys& ph, const double* QL, const double* QR, int d, double* D) {
+    roe_times_jump<double>(PhysC<double>(ph), QL, QR, d, D);
+  }
   // -NCP, Baer-Nunziato/pde.f90:192-231 and :277-290; only the volume-fraction gradient enters
-  __device__ static void src_ncp(const Phys& ph, const double* Q, double ax, double ay, double* S) {
-    double phi_g = 1.0 - Q[8];
-    double rho_g = Q[4] / phi_g;
-    double u_s = Q[1] / Q[0], v_s = Q[2] / Q[0];
-    double u_g = Q[5] / Q[4], v_g = Q[6] / Q[4];
-    double E_g = Q[7] / phi_g;
-    double p_g = (ph.gg - 1.0) * (E_g - 0.5 * rho_g * (u_g * u_g + v_g * v_g)) - ph.gg * ph.pg;
-    double un = u_s * ax + v_s * ay;
-    S[0] = -0.0;
+  template <class T>
+  __device__ static void src_ncp(const PhysC<T>& pc, const T* Q, T ax, T ay, T* S) {
+    T phi_g = T(1) - Q[8];
+    T rho_g = Q[4] / phi_g;
+    T u_s = Q[1] / Q[0], v_s = Q[2] / Q[0];
+    T u_g = Q[5] / Q[4], v_g = Q[6] / Q[4];
+    T E_g = Q[7] / phi_g;
+    T p_g = pc.gg1 * (E_g - T(0.5) * rho_g * (u_g * u_g + v_g * v_g)) - pc.ggpg;
+    T un = u_s * ax + v_s * ay;
+    S[0] = -T(0);
     S[1] = -(-p_g * ax);
     S[2] = -(-p_g * ay);
     S[3] = -(-p_g * un);
-    S[4] = -0.0;
+    S[4] = -T(0);
     S[5] = -(p_g * ax);
     S[6] = -(p_g * ay);
     S[7] = -(p_g * un);
     S[8] = -un;
   }
+  __device__ static void src_ncp(const Phys& ph, const double* Q, double ax, double ay, double* S) {
+    src_ncp<double>(PhysC<double>(ph), Q, ax, ay, S);
+  }
   // Baer-Nunziato/pde.f90:49-68
-  __device__ static void prim2cons(const Phys& ph, const double* Vp, double* Q) {
+  template <class T>
+  __device__ static void prim2cons(const PhysC<T>& pc, const T* Vp, T* Q) {
     Q[0] = Vp[8] * Vp[0];
     Q[1] = Q[0] * Vp[1];
     Q[2] = Q[0] * Vp[2];
-    Q[3] = Q[0] * (0.5 * (Vp[1] * Vp[1] + Vp[2] * Vp[2]) + (Vp[3] + ph.gs * ph.ps) / (Vp[0] * (ph.gs - 1.0)));
-    Q[4] = (1.0 - Vp[8]) * Vp[4];
+    Q[3] = Q[0] * (T(0.5) * (Vp[1] * Vp[1] + Vp[2] * Vp[2]) + (Vp[3] + pc.gsps) / (Vp[0] * pc.gs1));
+    Q[4] = (T(1) - Vp[8]) * Vp[4];
     Q[5] = Q[4] * Vp[5];
     Q[6] = Q[4] * Vp[6];
-    Q[7] = Q[4] * (0.5 * (Vp[5] * Vp[5] + Vp[6] * Vp[6]) + (Vp[7] + ph.gg * ph.pg) / (Vp[4] * (ph.gg - 1.0)));
+    Q[7] = Q[4] * (T(0.5) * (Vp[5] * Vp[5] + Vp[6] * Vp[6]) + (Vp[7] + pc.ggpg) / (Vp[4] * pc.gg1));
     Q[8] = Vp[8];
   }
+  __device__ static void prim2cons(const Phys& ph, const double* Vp, double* Q) { prim2cons<double>(PhysC<double>(ph), Vp, Q); }
   // Baer-Nunziato/pde.f90:237-266
   __device__ static bool positive(const Phys& ph, const double* Q) {
     double Vp[9];
@@ -365,6 +451,9 @@ struct ADSys {
   template <class R>
   struct PConst {
     __device__ explicit PConst(const Phys&) {}
+  };
+  struct FConst {
+    __device__ explicit FConst(const Phys&) {}
   };
   // Advection-Diffusion/pde.f90:70-80 (|cx nv1 + cy nv2|)
   __device__ static double max_eig_c(const Phys& ph, int d) {

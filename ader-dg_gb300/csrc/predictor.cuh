@@ -380,8 +380,9 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
     }
   } else {
     // volume integral: duh = (w_j/dx) sum_k Kxi(i,k) Fhi_x(k,j) + (w_i/dy) sum_k Kxi(j,k) Fhi_y(i,k) [+ w_i w_j Shi]
+    // duh is stored in the compute precision R (FP32 in the mixed mode)
     const R vx = op.w[j] / R(in.dx), vy = op.w[i] / R(in.dy);
-    double* dst = a.duh + ((size_t)cell * P2 + node) * V;
+    R* dst = reinterpret_cast<R*>(a.duh) + ((size_t)cell * P2 + node) * V;
 #pragma unroll
     for (int v = 0; v < V; ++v) {
       R sxv = R(0), syv = R(0);
@@ -392,7 +393,7 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
       }
       R d = sxv * vx + syv * vy;
       if constexpr (Sys::ID == kSysBN) d = fma(op.w[i] * op.w[j], Sh[v], d);
-      dst[v] = (double)d;
+      dst[v] = d;
     }
   }
 

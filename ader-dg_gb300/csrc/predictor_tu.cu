@@ -39,8 +39,13 @@ void make_ops(const HostOps& h, void* out) {
     o.FRd[a] = h.FR[a];
     o.xid[a] = h.xi[a];
   }
+  for (int a = 0; a < P; ++a) {
+    o.wf[a] = (float)h.w[a];
+    o.FLf[a] = (float)h.FL[a];
+    o.FRf[a] = (float)h.FR[a];
+  }
   for (int j = 0; j < P; ++j)
-    for (int i = 0; i < P; ++i) o.iww[i + P * j] = 1.0 / (h.w[i] * h.w[j]);
+    for (int i = 0; i < P; ++i) o.iwwf[i + P * j] = (float)(1.0 / (h.w[i] * h.w[j]));
   for (int k = 0; k < P * P; ++k) {
     o.Kxi[k] = (R)h.Kxi[k];
     o.dudx[k] = (R)h.dudx[k];
@@ -72,6 +77,24 @@ void make_ops(const HostOps& h, void* out) {
     o.lim2uh[k] = h.lim2uh[k];
   }
   for (int k = 0; k < P * P; ++k) o.uh2lob[k] = h.uh2lob[k];
+  for (int k = 0; k < S * P; ++k) o.uh2limf[k] = (float)h.uh2lim[k];
+  for (int k = 0; k < P * P; ++k) o.uh2lobf[k] = (float)h.uh2lob[k];
+  // Error of a two-pass FP32 projection (inputs and operators rounded to
+  // FP32, P-term accumulations in each pass): at most (2P + 4) u Lambda^2 max|uh|,
+  // u = 2^-24, Lambda = the larger of the operators' max row sums of |entries|;
+  // taken with a factor 4 of safety.
+  double lam = 0.0;
+  for (int s = 0; s < S; ++s) {
+    double r = 0.0;
+    for (int k = 0; k < P; ++k) r += std::fabs(h.uh2lim[s + S * k]);
+    lam = r > lam ? r : lam;
+  }
+  for (int q = 0; q < P; ++q) {
+    double r = 0.0;
+    for (int k = 0; k < P; ++k) r += std::fabs(h.uh2lob[q + P * k]);
+    lam = r > lam ? r : lam;
+  }
+  o.perr = (float)(4.0 * (2 * P + 4) * std::ldexp(1.0, -24) * lam * lam);
   *reinterpret_cast<DevOps<N, R>*>(out) = o;
 }
 

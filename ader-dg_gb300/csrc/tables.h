@@ -28,8 +28,8 @@ struct KernelTable {
   cudaError_t (*cells)(const BatchArgs&, const void* ops64, int fast, cudaStream_t) = nullptr;
   cudaError_t (*volume)(const BatchArgs&, const void* ops64, cudaStream_t) = nullptr;
   cudaError_t (*mark)(const BatchArgs&, cudaStream_t) = nullptr;
-  cudaError_t (*subcell)(const BatchArgs&, const void* ops64, const FaceConst&, int grid, cudaStream_t) = nullptr;
-  int (*subcell_grid)(int num_sms) = nullptr;
+  cudaError_t (*subcell)(const BatchArgs&, const void* ops64, const FaceConst&, int grid, int fp32, cudaStream_t) = nullptr;
+  int (*subcell_grid)(int num_sms, int fp32) = nullptr;
 };
 
 // Returns the table for (sys, N) or nullptr when that pair was not built.
