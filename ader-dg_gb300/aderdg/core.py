@@ -159,6 +159,7 @@ def load(build_if_missing=False):
         "aderdg_batch_info": (i, [vp, ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long),
                                   ctypes.POINTER(ctypes.c_long), ip]),
         "aderdg_batch_last_error": (ctypes.c_char_p, [vp]), "aderdg_batch_profile": (i, [vp, dp]),
+        "aderdg_batch_run_timed": (i, [ctypes.POINTER(vp), i, i, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -177,7 +178,8 @@ EXPORTED = ("aderdg_create", "aderdg_destroy", "aderdg_upload", "aderdg_init_lim
             "aderdg_operator", "aderdg_step_host", "aderdg_time_steps", "aderdg_profile_step",
             "aderdg_batch_unit_bytes", "aderdg_batch_create", "aderdg_batch_destroy", "aderdg_batch_admit",
             "aderdg_batch_release", "aderdg_batch_launch", "aderdg_batch_sync", "aderdg_batch_query",
-            "aderdg_batch_download", "aderdg_batch_info", "aderdg_batch_last_error", "aderdg_batch_profile")
+            "aderdg_batch_download", "aderdg_batch_info", "aderdg_batch_last_error", "aderdg_batch_profile",
+            "aderdg_batch_run_timed")
 
 
 def _dp(a):
@@ -464,6 +466,18 @@ class Batch:
         ms = np.zeros(7, dtype=np.float64)
         self._ck(self.L.aderdg_batch_profile(self.h, _dp(ms)))
         return dict(zip(Solver.PHASES, ms))
+
+    @staticmethod
+    def run_timed(batches, steps):
+        """Device milliseconds of `steps` steps of all `batches` run concurrently
+        (CUDA events bracketing every batch's stream)."""
+        L = load()
+        arr = (ctypes.c_void_p * len(batches))(*[b.h for b in batches])
+        ms = ctypes.c_double(0)
+        r = L.aderdg_batch_run_timed(arr, len(batches), int(steps), ctypes.byref(ms))
+        if r:
+            raise AderdgError(r, L.aderdg_last_error(None).decode())
+        return ms.value
 
     def info(self):
         u, c, b = ctypes.c_long(0), ctypes.c_long(0), ctypes.c_long(0)

@@ -207,6 +207,33 @@ int ensure_phase_buffers(aderdg_ctx* c) {
 namespace aderdg {
 void set_last_error(const std::string& msg) { g_err = msg; }
 int validate_config(const aderdg_config* c, std::string* why) { return validate(c, why); }
+// Instance description of a configuration (cell and face bases 0).
+InstDesc make_inst_desc(const aderdg_config* cfg) {
+  InstDesc in{};
+  in.imax = cfg->imax;
+  in.jmax = cfg->jmax;
+  in.cell_base = in.fx_base = in.fy_base = 0;
+  in.dx = (cfg->xr[0] - cfg->xl[0]) / cfg->imax;  // dx = (xR-xL)/VMAX, Euler/initialize.f90:45-46
+  in.dy = (cfg->xr[1] - cfg->xl[1]) / cfg->jmax;
+  in.idxf = (float)(1.0 / in.dx);
+  in.idyf = (float)(1.0 / in.dy);
+  in.xl0 = cfg->xl[0];
+  in.xl1 = cfg->xl[1];
+  for (int s = 0; s < 4; ++s) in.bc[s] = cfg->bc[s];
+  in.bc_mode = cfg->bc_mode;
+  in.cfl_pnpm = cfg->cfl * pnpm_cfl(cfg->N);
+  in.ph.gamma = cfg->gamma;
+  in.ph.gs = cfg->gamma_s;
+  in.ph.gg = cfg->gamma_g;
+  in.ph.ps = cfg->pi_s;
+  in.ph.pg = cfg->pi_g;
+  in.ph.cx = cfg->cx;
+  in.ph.cy = cfg->cy;
+  in.ph.a = cfg->a;
+  in.ph.ad_fused = cfg->ad_flux_mode;
+  return in;
+}
+
 FaceConst make_face_const(const HostOps& ops) {
   const double pi = 4.0 * std::atan(1.0);
   FaceConst fc{};
@@ -313,27 +340,7 @@ int aderdg_create(const aderdg_config* cfg, aderdg_ctx** out) {
   a.nfy = c->nfy;
 
   InstDesc& in = c->h_inst;
-  in.imax = cfg->imax;
-  in.jmax = cfg->jmax;
-  in.cell_base = 0;
-  in.fx_base = 0;
-  in.fy_base = 0;
-  in.dx = (cfg->xr[0] - cfg->xl[0]) / cfg->imax;  // dx = (xR-xL)/VMAX, Euler/initialize.f90:45-46
-  in.dy = (cfg->xr[1] - cfg->xl[1]) / cfg->jmax;
-  in.xl0 = cfg->xl[0];
-  in.xl1 = cfg->xl[1];
-  for (int s = 0; s < 4; ++s) in.bc[s] = cfg->bc[s];
-  in.bc_mode = cfg->bc_mode;
-  in.cfl_pnpm = cfg->cfl * aderdg::pnpm_cfl(cfg->N);
-  in.ph.gamma = cfg->gamma;
-  in.ph.gs = cfg->gamma_s;
-  in.ph.gg = cfg->gamma_g;
-  in.ph.ps = cfg->pi_s;
-  in.ph.pg = cfg->pi_g;
-  in.ph.cx = cfg->cx;
-  in.ph.cy = cfg->cy;
-  in.ph.a = cfg->a;
-  in.ph.ad_fused = cfg->ad_flux_mode;
+  in = aderdg::make_inst_desc(cfg);
   e = cudaMemcpy(c->d_inst, &in, sizeof(InstDesc), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return bail(fail_cuda(nullptr, "cudaMemcpy inst", e));
 

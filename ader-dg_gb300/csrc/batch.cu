@@ -30,6 +30,7 @@ namespace aderdg {
 void set_last_error(const std::string& msg);
 int validate_config(const aderdg_config* c, std::string* why);
 FaceConst make_face_const(const HostOps& ops);
+InstDesc make_inst_desc(const aderdg_config* cfg);
 }  // namespace aderdg
 
 using aderdg::BatchArgs;
@@ -361,26 +362,8 @@ int aderdg_batch_admit(aderdg_batch* b, const aderdg_config* cfg, const double* 
   b->pos_of[s] = pos;
   ++b->n_used;
   InstDesc& in = b->h_inst[pos];
-  in = InstDesc{};
-  in.imax = cfg->imax;
-  in.jmax = cfg->jmax;
+  in = aderdg::make_inst_desc(cfg);
   in.cell_base = in.fx_base = in.fy_base = base;
-  in.dx = (cfg->xr[0] - cfg->xl[0]) / cfg->imax;
-  in.dy = (cfg->xr[1] - cfg->xl[1]) / cfg->jmax;
-  in.xl0 = cfg->xl[0];
-  in.xl1 = cfg->xl[1];
-  for (int k = 0; k < 4; ++k) in.bc[k] = cfg->bc[k];
-  in.bc_mode = cfg->bc_mode;
-  in.cfl_pnpm = cfg->cfl * aderdg::pnpm_cfl(cfg->N);
-  in.ph.gamma = cfg->gamma;
-  in.ph.gs = cfg->gamma_s;
-  in.ph.gg = cfg->gamma_g;
-  in.ph.ps = cfg->pi_s;
-  in.ph.pg = cfg->pi_g;
-  in.ph.cx = cfg->cx;
-  in.ph.cy = cfg->cy;
-  in.ph.a = cfg->a;
-  in.ph.ad_fused = cfg->ad_flux_mode;
   InstState& st = b->h_st[pos];
   std::memset(&st, 0, sizeof(st));
   st.time = 0.0;
@@ -456,6 +439,46 @@ int aderdg_batch_launch(aderdg_batch* b, int steps) {
   int r = bensure_graph(b);
   if (r) return r;
   for (int s = 0; s < steps; ++s) BK(b, cudaGraphLaunch(b->gexec, b->stream));
+  return ADERDG_OK;
+}
+
+int aderdg_batch_run_timed(aderdg_batch* const* batches, int n, int steps, double* ms) {
+  if (!batches || n <= 0 || !ms) return bfail(nullptr, ADERDG_EINVAL, "null argument");
+  for (int k = 0; k < n; ++k)
+    if (!batches[k]) return bfail(nullptr, ADERDG_EINVAL, "null batch");
+  aderdg_batch* b0 = batches[0];
+  for (int k = 0; k < n; ++k) {
+    if (batches[k]->n_used == 0) continue;
+    int r = bensure_graph(batches[k]);
+    if (r) return r;
+  }
+  cudaStream_t ts = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  std::vector<cudaEvent_t> done((size_t)n, nullptr);
+  cudaError_t e = cudaStreamCreateWithFlags(&ts, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  for (int k = 0; k < n && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming);
+  // every batch stream starts after e0 on the timing stream; e1 follows all of them
+  if (e == cudaSuccess) e = cudaEventRecord(e0, ts);
+  for (int k = 0; k < n && e == cudaSuccess; ++k) {
+    aderdg_batch* b = batches[k];
+    e = cudaStreamWaitEvent(b->stream, e0, 0);
+    for (int s = 0; s < steps && e == cudaSuccess && b->n_used > 0; ++s) e = cudaGraphLaunch(b->gexec, b->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(done[k], b->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ts, done[k], 0);
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(e1, ts);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float f = 0.0f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&f, e0, e1);
+  for (auto d : done)
+    if (d) cudaEventDestroy(d);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (ts) cudaStreamDestroy(ts);
+  if (e != cudaSuccess) return bcuda(b0, "aderdg_batch_run_timed", e);
+  *ms = (double)f;
   return ADERDG_OK;
 }
 

@@ -128,22 +128,30 @@ struct Proj {
 #pragma unroll
     for (int v = 0; v < V; ++v) { mn[v] = okey_inv(kmn[v]); mx[v] = okey_inv(kmx[v]); }
   }
-  // FP32 x pass fused with min/max and the admissibility test: a subcell whose
-  // FP32 value is not clearly admissible (err = the projection's error bound
-  // per variable) is projected again in FP64 from U64 and tested exactly.
+  // FP32 x pass fused with min/max and the admissibility test.  The y pass
+  // ran on the deviations d = uh - ubar from a reference state ubar of the
+  // cell (the projections reproduce constants, so proj(uh) = ubar + proj(d));
+  // min/max are of the projected deviations.  A subcell whose FP32 value
+  // ubar + proj(d) is not clearly admissible (err = the error bound of
+  // proj(d), plus the rounding of ubar to FP32) is projected again in FP64
+  // from U64 and tested exactly.
   template <class Sys>
   __device__ static void xpass_minmax_f32(const float* LY, const float* LB, const float* lim, const float* lob,
                                           const double* U64, const DevOps<N, double>& op,
-                                          const typename Sys::FConst& fc, const float* err, const Phys& ph,
-                                          int r, int nr, float* mn, float* mx, bool& posfail) {
-    float val[V];
+                                          const typename Sys::FConst& fc, const float* err, const float* ubf,
+                                          const Phys& ph, int r, int nr, float* mn, float* mx, bool& posfail) {
+    float val[V], q[V], e[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) e[v] = err[v] + 2.5e-7f * fabsf(ubf[v]);
     for (int idx = r; idx < S * S; idx += nr) {
       const int s1 = idx % S, s2 = idx / S;
       subcell<true>(LY, lim, s1, s2, val);
 #pragma unroll
       for (int v = 0; v < V; ++v) { mn[v] = fminf(mn[v], val[v]); mx[v] = fmaxf(mx[v], val[v]); }
       if constexpr (Sys::ID != kSysAD) {
-        if (!Sys::admissible_box_f32(fc, val, err)) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) q[v] = ubf[v] + val[v];
+        if (!Sys::admissible_box_f32(fc, q, e)) {
           double q[V];
 #pragma unroll
           for (int v = 0; v < V; ++v) {
@@ -204,7 +212,7 @@ __device__ __forceinline__ double cfl_denom_f32(const InstDesc& in, const typena
   } else {
     float ex, ey;
     Sys::max_eig2_f32(fc, q, ex, ey);
-    return (double)(ex / (float)in.dx + ey / (float)in.dy);
+    return (double)(ex * in.idxf + ey * in.idyf);
   }
 }
 
@@ -217,9 +225,10 @@ struct CellCfg {
   // FP32-mixed: U64 [V][P2] then FP32 U [V][P2], LY, LB, red, |U| max [V]
   // in the same room
   static constexpr int CELL_DBL = V * P2 + V * S * P + V * P * P + 2 * V * P2;
-  static_assert(8 * V * P2 + 4 * (3 * V * P2 + V * S * P + V * P * P + V) <= 8 * CELL_DBL, "FP32 cell layout");
-  static constexpr int OPS_DBL = S * P + P * P;  // uh2lim, uh2lob
-  static constexpr int SMEM_BYTES = CPB * CELL_DBL * 8 + OPS_DBL * 8 + CPB * 8 /*cell max*/ + CPB * 4 /*flags*/ + 16;
+  static_assert(8 * V * P2 + 4 * (3 * V * P2 + V * S * P + V * P * P) <= 8 * CELL_DBL, "FP32 cell layout");
+  static constexpr int OPS_DBL = S * P + P * P;  // uh2lim, uh2lob (FP64, then FP32 in the mixed mode)
+  static constexpr int SMEM_BYTES = CPB * CELL_DBL * 8 + OPS_DBL * 12 + CPB * 8 /*cell max*/ + CPB * 4 /*flags*/ +
+                                    CPB * V * 4 /*|U| max*/ + 16;
 };
 
 template <class Sys, int N, bool kFast>
@@ -229,8 +238,10 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* sm = reinterpret_cast<double*>(smem_raw);
   double* opsm = sm + CPB * C::CELL_DBL;
-  unsigned long long* cmax = reinterpret_cast<unsigned long long*>(opsm + C::OPS_DBL);
+  float* opsf = reinterpret_cast<float*>(opsm + C::OPS_DBL);
+  unsigned long long* cmax = reinterpret_cast<unsigned long long*>(opsf + C::OPS_DBL + (C::OPS_DBL & 1));
   int* cflag = reinterpret_cast<int*>(cmax + CPB);
+  unsigned* amax_all = reinterpret_cast<unsigned*>(cflag + CPB);  // [CPB][V]
 
   const int mode = a.mode;
   const int t = threadIdx.x;
@@ -260,12 +271,12 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
   float* LYf = Uf + V * P2;
   float* LBf = LYf + V * S * P;
   float* REDf = LBf + V * P * P;
-  unsigned* amax = reinterpret_cast<unsigned*>(REDf + 2 * V * P2);
+  unsigned* amax = amax_all + (in_cta ? lc : 0) * V;
 
   // projection operators into shared memory (lanes index them by subcell)
   for (int k = t; k < C::OPS_DBL; k += blockDim.x) {
-    if constexpr (kFast) reinterpret_cast<float*>(opsm)[k] = k < S * P ? op.uh2limf[k] : op.uh2lobf[k - S * P];
-    else opsm[k] = k < S * P ? op.uh2lim[k] : op.uh2lob[k - S * P];
+    opsm[k] = k < S * P ? op.uh2lim[k] : op.uh2lob[k - S * P];
+    if constexpr (kFast) opsf[k] = k < S * P ? op.uh2limf[k] : op.uh2lobf[k - S * P];
   }
   if (in_cta && node == 0) {
     cmax[lc] = 0ull;
@@ -295,7 +306,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
 #pragma unroll
         for (int v = 0; v < V; ++v) d[v] = D32[off + v];
         if (mode != kCellUpdate) {
-          const float cxf = op.wf[j] / (float)in.dx, cyf = op.wf[i] / (float)in.dy;
+          const float cxf = op.wf[j] * in.idxf, cyf = op.wf[i] * in.idyf;
 #pragma unroll
           for (int v = 0; v < V; ++v) {
             const float fl = XL[((size_t)fxl * P + j) * V + v], fr = XR[((size_t)(fxl + 1) * P + j) * V + v];
@@ -316,7 +327,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
           const float iw = op.iwwf[i + P * j];
 #pragma unroll
           for (int v = 0; v < V; ++v) {
-            u[v] = uo[v] + dt * (double)(d[v] * iw);
+            u[v] = fma(dt, (double)(d[v] * iw), uo[v]);
             un[v] = u[v];
           }
         }
@@ -365,11 +376,17 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
   }
   if (mode == kCellSurface) return;  // uniform per launch: no barrier follows
 
-  // FP32 copy of the node's state (FP32-mixed)
-  float uf[V];
+  // FP32-mixed: the node's state in FP32, and its deviation from the cell's
+  // reference state ubar (the start-of-step state at node 0) in FP32
+  float uf[V], du[V], ubf[V];
   if constexpr (kFast) {
+    const double* ub = a.uh[par] + (size_t)(valid ? cell : 0) * P2 * V;
 #pragma unroll
-    for (int v = 0; v < V; ++v) uf[v] = act ? (float)u[v] : 0.0f;
+    for (int v = 0; v < V; ++v) {
+      uf[v] = act ? (float)u[v] : 0.0f;
+      du[v] = act ? (float)(u[v] - ub[v]) : 0.0f;
+      ubf[v] = uf[v] - du[v];
+    }
   }
 
   // ------------------------------------------------------------- CFL part
@@ -387,46 +404,74 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
     // Cells whose limiter is active keep their min/max from the subcell data
     // (get_min_max, Euler/limiter.f90:134-139) in the priming pass.
     const bool from_lh = act && mode == kCellPrime && a.status[par][valid ? cell : 0] != 0;
+    bool f32red = false;  // the cell's partial min/max are in REDf (FP32)
     if constexpr (kFast) {
       if (act) {
 #pragma unroll
         for (int v = 0; v < V; ++v) {
           U[v * P2 + node] = u[v];
-          Uf[v * P2 + node] = uf[v];
-          atomicMax(&amax[v], __float_as_uint(fabsf(uf[v])));
+          Uf[v * P2 + node] = du[v];
+          atomicMax(&amax[v], __float_as_uint(fabsf(du[v])));
         }
       }
       __syncthreads();
-      const float* lim = reinterpret_cast<const float*>(opsm);
-      const float* lob = lim + S * P;
-      if (act && !from_lh) Proj<N, V, float>::template ypass<true>(Uf, LYf, LBf, lim, lob, node, P2);
-      __syncthreads();
-      float mn[V], mx[V];
-      bool posfail = false;
+      // FP32 projections of the deviations when their error bound stays a
+      // tenth of the DMP's absolute tolerance (1e-4) for every variable
+      // (smooth cells); otherwise this cell takes the FP64 projections.
+      float err[V];
+      bool f32ok = true;
 #pragma unroll
-      for (int v = 0; v < V; ++v) { mn[v] = uf[v]; mx[v] = uf[v]; }
+      for (int v = 0; v < V; ++v) {
+        err[v] = op.perr * __uint_as_float(amax[v]);
+        f32ok = f32ok && err[v] <= 1.0e-5f;
+      }
+      if (act && !from_lh) {
+        if (f32ok) Proj<N, V, float>::template ypass<true>(Uf, LYf, LBf, opsf, opsf + S * P, node, P2);
+        else Proj<N, V, double>::template ypass<true>(U, LY, LB, opsm, opsm + S * P, node, P2);
+      }
+      __syncthreads();
+      bool posfail = false;
       if (act) {
         if (from_lh) {
-          const double* L = a.lh[par] + (size_t)cell * S * S * V;
+          double mn[V], mx[V];
 #pragma unroll
-          for (int v = 0; v < V; ++v) { mn[v] = __int_as_float(0x7f800000); mx[v] = -__int_as_float(0x7f800000); }
+          for (int v = 0; v < V; ++v) { mn[v] = kInf; mx[v] = -kInf; }
+          const double* L = a.lh[par] + (size_t)cell * S * S * V;
           for (int idx = node; idx < S * S; idx += P2)
 #pragma unroll
-            for (int v = 0; v < V; ++v) { mn[v] = fminf(mn[v], (float)L[idx * V + v]); mx[v] = fmaxf(mx[v], (float)L[idx * V + v]); }
+            for (int v = 0; v < V; ++v) { mn[v] = fmin(mn[v], L[idx * V + v]); mx[v] = fmax(mx[v], L[idx * V + v]); }
+#pragma unroll
+          for (int v = 0; v < V; ++v) {
+            RED[v * P2 + node] = mn[v];
+            RED[(V + v) * P2 + node] = mx[v];
+          }
+        } else if (f32ok) {
+          float mn[V], mx[V];
+#pragma unroll
+          for (int v = 0; v < V; ++v) { mn[v] = du[v]; mx[v] = du[v]; }
+          Proj<N, V, float>::template xpass_minmax_f32<Sys>(LYf, LBf, opsf, opsf + S * P, U, op,
+                                                            typename Sys::FConst(in.ph), err, ubf, in.ph, node, P2,
+                                                            mn, mx, posfail);
+#pragma unroll
+          for (int v = 0; v < V; ++v) {
+            REDf[v * P2 + node] = mn[v];
+            REDf[(V + v) * P2 + node] = mx[v];
+          }
         } else {
-          float err[V];
+          double mn[V], mx[V];
 #pragma unroll
-          for (int v = 0; v < V; ++v) err[v] = op.perr * __uint_as_float(amax[v]);
-          Proj<N, V, float>::template xpass_minmax_f32<Sys>(LYf, LBf, lim, lob, U, op, typename Sys::FConst(in.ph),
-                                                            err, in.ph, node, P2, mn, mx, posfail);
-        }
+          for (int v = 0; v < V; ++v) { mn[v] = kInf; mx[v] = -kInf; }
+          Proj<N, V, double>::template xpass_minmax<Sys, true>(U, LY, LB, opsm, opsm + S * P, in.ph, node, P2, mn, mx,
+                                                               posfail);
 #pragma unroll
-        for (int v = 0; v < V; ++v) {
-          REDf[v * P2 + node] = mn[v];
-          REDf[(V + v) * P2 + node] = mx[v];
+          for (int v = 0; v < V; ++v) {
+            RED[v * P2 + node] = mn[v];
+            RED[(V + v) * P2 + node] = mx[v];
+          }
         }
         if (posfail) atomicOr(&cflag[lc], 1);
       }
+      f32red = f32ok && !from_lh;
     } else {
       if (act) {
 #pragma unroll
@@ -462,11 +507,12 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
     if (act && node < V) {
       const int v = node;
       double cmn, cmx;
-      if constexpr (kFast) {
+      if (f32red) {
         float fmn = REDf[v * P2], fmx = REDf[(V + v) * P2];
         for (int k = 1; k < P2; ++k) { fmn = fminf(fmn, REDf[v * P2 + k]); fmx = fmaxf(fmx, REDf[(V + v) * P2 + k]); }
-        cmn = (double)fmn;
-        cmx = (double)fmx;
+        const double ubar = a.uh[par][(size_t)cell * P2 * V + v];
+        cmn = ubar + (double)fmn;
+        cmx = ubar + (double)fmx;
       } else {
         cmn = RED[v * P2];
         cmx = RED[(V + v) * P2];
@@ -489,14 +535,29 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
           const long long base = in.cell_base;
           lmin = mmi[(size_t)cell * 2 * V + v];
           lmax = mmi[(size_t)cell * 2 * V + V + v];
-          for (int jj = -1; jj <= 1; ++jj)
-            for (int ii = -1; ii <= 1; ++ii) {
-              const int in_ = nb_index(ci, ii, in.imax, in.bc[0], in.bc[1]);
-              const int jn_ = nb_index(cj, jj, in.jmax, in.bc[2], in.bc[3]);
-              const long long nc = base + in_ + (long long)in.imax * jn_;
-              lmin = fmin(lmin, mmi[(size_t)nc * 2 * V + v]);
-              lmax = fmax(lmax, mmi[(size_t)nc * 2 * V + V + v]);
-            }
+          if constexpr (kFast) {
+            // integer-key min/max (the integer pipe, not FP64)
+            long long kmn = okey(lmin), kmx = okey(lmax);
+            for (int jj = -1; jj <= 1; ++jj)
+              for (int ii = -1; ii <= 1; ++ii) {
+                const int in_ = nb_index(ci, ii, in.imax, in.bc[0], in.bc[1]);
+                const int jn_ = nb_index(cj, jj, in.jmax, in.bc[2], in.bc[3]);
+                const long long nc = base + in_ + (long long)in.imax * jn_;
+                kmn = min(kmn, okey(mmi[(size_t)nc * 2 * V + v]));
+                kmx = max(kmx, okey(mmi[(size_t)nc * 2 * V + V + v]));
+              }
+            lmin = okey_inv(kmn);
+            lmax = okey_inv(kmx);
+          } else {
+            for (int jj = -1; jj <= 1; ++jj)
+              for (int ii = -1; ii <= 1; ++ii) {
+                const int in_ = nb_index(ci, ii, in.imax, in.bc[0], in.bc[1]);
+                const int jn_ = nb_index(cj, jj, in.jmax, in.bc[2], in.bc[3]);
+                const long long nc = base + in_ + (long long)in.imax * jn_;
+                lmin = fmin(lmin, mmi[(size_t)nc * 2 * V + v]);
+                lmax = fmax(lmax, mmi[(size_t)nc * 2 * V + V + v]);
+              }
+          }
           argmax = 0.0;
           if (a.lminmax) {
             a.lminmax[(size_t)cell * 2 * V + v] = lmin;

@@ -36,6 +36,7 @@ struct InstDesc {
   long long cell_base;
   long long fx_base, fy_base;  // first x face / y face
   double dx, dy;
+  float idxf, idyf;            // 1/dx, 1/dy in FP32 (FP32-mixed CFL)
   double xl0, xl1;
   int bc[4];
   int bc_mode;

@@ -80,14 +80,16 @@ struct SubCfg {
   // the slopes, which are formed after it.
   static constexpr int TSLOPE = 7 * V * H * H;
   static_assert(9 * V * P2 + 9 * V * P * S <= TSLOPE, "gather staging room");
-  static constexpr int TEL = V * R * R + TSLOPE + NEF + V * S * S + V * S * P + 2 * S * P;
+  static constexpr int TEL = V * R * R + TSLOPE + NEF + V * S * S + V * S * P + 2 * S * P + P * P;
+  // FP32-mixed DMP of the new polynomial, in the room of the slopes: UN, LY, LB
+  static_assert(V * P2 + V * S * P + V * P * P <= TSLOPE, "FP32 DMP room");
   static constexpr int TBYTES = ((TEL * (int)sizeof(T) + 15) / 16) * 16;
   // FP64 elements: new polynomial UN [V][P2], DMP y pass LY [V][S][P], LB
   // [V][P][P], reduction [2][V][THREADS], operators uh2lim, uh2lob (FP64)
   static constexpr int OPS_DBL = S * P + P * P;
   static constexpr int DEL = V * P2 + V * S * P + V * P * P + 2 * V * THREADS + OPS_DBL;
   // misc: flags, CFL max, neighbour cells and their status
-  static constexpr int MISC = 16 + 9 * 8 + 9 * 4 + 12;
+  static constexpr int MISC = 16 + 9 * 8 + 9 * 4 + 4 * V + 12;
   static constexpr int SMEM_BYTES = TBYTES + DEL * 8 + MISC;
 };
 
@@ -114,8 +116,9 @@ __device__ __forceinline__ void rusanov_s(const PhysC<T>& pc, const T* QL, const
 }
 
 // T = double: the reference's FP64 arithmetic in its order (bit for bit).
-// T = float: the FP32-mixed mode; the subcell re-solve in FP32, the state,
-// Lh, the DMP of the new polynomial and its CFL contribution in FP64.
+// T = float: the FP32-mixed mode; the subcell re-solve, the DMP projections
+// of the new polynomial (while their error bound allows) and its CFL
+// eigenvalues in FP32; the state, Lh and min/max in FP64.
 template <class Sys, int N, class T>
 __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS) k_subcell(BatchArgs a, DevOps<N, double> op, FaceConst fc) {
   using C = SubCfg<Sys, N, T>;
@@ -135,6 +138,7 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS) k_subcell(BatchArg
   T* LUY = sub1 + V * S * S;         // [V][P][S]: luhy(v, iii, s) at (v*P + s)*S + iii
   T* limT = LUY + V * S * P;         // uh2lim (s,k) at [s + S*k]
   T* l2uT = limT + S * P;            // lim2uh (k,s) at [k + P*s]
+  T* lobT = l2uT + S * P;            // uh2lob (q,k) at [q + P*k]
   T* NB = slx;                       // gather staging: [9][V][P2]
   T* LYN = NB + 9 * V * P2;          // [9][V][P][S]: sum_m uh(k, m) uh2lim(s, m) at ((n*V + v)*P + k)*S + s
   double* UN = reinterpret_cast<double*>(smem_raw + C::TBYTES);  // [V][P2]
@@ -147,6 +151,11 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS) k_subcell(BatchArg
   unsigned long long* cmaxp = reinterpret_cast<unsigned long long*>(misc + 8);
   long long* nbc = reinterpret_cast<long long*>(misc + 16);  // 3x3 neighbour cells, n = (bi+1) + 3 (bj+1)
   int* nbs = reinterpret_cast<int*>(misc + 16 + 9 * 8);     // their status (0: project olduh)
+  unsigned* amax = reinterpret_cast<unsigned*>(nbs + 9);     // FP32-mixed: max |UN| per variable
+  float* UNf = reinterpret_cast<float*>(slx);                // FP32-mixed DMP (after the re-solve)
+  float* LYf = UNf + V * P2;
+  float* LBf = LYf + V * S * P;
+  float* redf = reinterpret_cast<float*>(red);              // [2][V][NT]
 
   const int t = threadIdx.x;
   for (int k = t; k < C::OPS_DBL; k += NT) opsm[k] = k < S * P ? op.uh2lim[k] : op.uh2lob[k - S * P];
@@ -154,6 +163,7 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS) k_subcell(BatchArg
     limT[k] = (T)op.uh2lim[k];
     l2uT[k] = (T)op.lim2uh[k];
   }
+  for (int k = t; k < P * P; k += NT) lobT[k] = (T)op.uh2lob[k];
   __syncthreads();
   auto SU = [&](int v, int ii, int jj) -> T& { return sub0[v * R * R + (ii + 1) + R * (jj + 1)]; };  // ii,jj in -1..S+2
   auto hx = [&](int v, int ii, int jj) { return v * H * H + ii + H * jj; };                         // ii,jj in 0..S+1
@@ -190,6 +200,7 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS) k_subcell(BatchArg
       flag[0] = 0;
       *cmaxp = 0ull;
     }
+    if (t < V) amax[t] = 0u;
     __syncthreads();
     for (int p = t; p < 9 * P2 * V; p += NT) {
       const int n = p / (P2 * V), r = p - n * (P2 * V);
@@ -388,32 +399,93 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS) k_subcell(BatchArg
       }
     }
     __syncthreads();
-    // ---- DMP of the new polynomial (recompute = 2) and the next min/max
-    Proj<N, V, double>::ypass(UN, LY, LB, opsm, opsm + S * P, t, NT);
+    if constexpr (sizeof(T) == 4) {
+      // FP32-mixed DMP: deviations from the new polynomial's node-0 state
+      for (int p = t; p < P2; p += NT)
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          const float d = (float)(UN[v * P2 + p] - UN[v * P2]);
+          UNf[v * P2 + p] = d;
+          atomicMax(&amax[v], __float_as_uint(fabsf(d)));
+        }
+      __syncthreads();
+    }
+    // ---- DMP of the new polynomial (recompute = 2) and the next min/max.
+    // FP32-mixed: FP32 projections when their error bound stays a tenth of the
+    // DMP's absolute tolerance, else FP64 (as in the cell kernel).
+    float err[V];
+    bool f32 = false;
+    if constexpr (sizeof(T) == 4) {
+      f32 = true;
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        err[v] = op.perr * __uint_as_float(amax[v]);
+        f32 = f32 && err[v] <= 1.0e-5f;
+      }
+    }
+    if constexpr (sizeof(T) == 4) {
+      if (f32) Proj<N, V, float>::template ypass<true>(UNf, LYf, LBf, limT, lobT, t, NT);
+    }
+    if (!f32) Proj<N, V, double>::ypass(UN, LY, LB, opsm, opsm + S * P, t, NT);
     __syncthreads();
     double mn[V], mx[V];
     bool posfail = false;
+    if (f32) {
+      float fmn[V], fmx[V];
 #pragma unroll
-    for (int v = 0; v < V; ++v) { mn[v] = kInf; mx[v] = -kInf; }
-    Proj<N, V, double>::template xpass_minmax<Sys>(UN, LY, LB, opsm, opsm + S * P, ph, t, NT, mn, mx, posfail);
+      for (int v = 0; v < V; ++v) { fmn[v] = __int_as_float(0x7f800000); fmx[v] = -__int_as_float(0x7f800000); }
+      for (int p = t; p < P2; p += NT)
 #pragma unroll
-    for (int v = 0; v < V; ++v) { red[v * NT + t] = mn[v]; red[(V + v) * NT + t] = mx[v]; }
-    if (posfail) atomicOr(&flag[0], 1);
-    // CFL denominator of the new polynomial
-    for (int p = t; p < P2; p += NT) {
-      double Q[V];
+        for (int v = 0; v < V; ++v) { fmn[v] = fminf(fmn[v], UNf[v * P2 + p]); fmx[v] = fmaxf(fmx[v], UNf[v * P2 + p]); }
+      if constexpr (sizeof(T) == 4) {
+        float ubf[V];
 #pragma unroll
-      for (int v = 0; v < V; ++v) Q[v] = UN[v * P2 + p];
-      atomicMax(cmaxp, (unsigned long long)__double_as_longlong(cfl_denom<Sys, N>(in, Q)));
+        for (int v = 0; v < V; ++v) ubf[v] = (float)UN[v * P2];
+        Proj<N, V, float>::template xpass_minmax_f32<Sys>(LYf, LBf, limT, lobT, UN, op, typename Sys::FConst(ph), err,
+                                                          ubf, ph, t, NT, fmn, fmx, posfail);
+      }
+#pragma unroll
+      for (int v = 0; v < V; ++v) { redf[v * NT + t] = fmn[v]; redf[(V + v) * NT + t] = fmx[v]; }
+      // CFL denominator of the new polynomial (FP32 eigenvalues)
+      for (int p = t; p < P2; p += NT) {
+        float q[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) q[v] = (float)UN[v * P2 + p];
+        atomicMax(cmaxp, (unsigned long long)__double_as_longlong(cfl_denom_f32<Sys, N>(in, typename Sys::FConst(ph), q)));
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < V; ++v) { mn[v] = kInf; mx[v] = -kInf; }
+      Proj<N, V, double>::template xpass_minmax<Sys>(UN, LY, LB, opsm, opsm + S * P, ph, t, NT, mn, mx, posfail);
+#pragma unroll
+      for (int v = 0; v < V; ++v) { red[v * NT + t] = mn[v]; red[(V + v) * NT + t] = mx[v]; }
+      // CFL denominator of the new polynomial
+      for (int p = t; p < P2; p += NT) {
+        double Q[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) Q[v] = UN[v * P2 + p];
+        atomicMax(cmaxp, (unsigned long long)__double_as_longlong(cfl_denom<Sys, N>(in, Q)));
+      }
     }
+    if (posfail) atomicOr(&flag[0], 1);
     __syncthreads();
     double* mmo = a.mm[par ^ 1] + (size_t)c * 2 * V;
+    double dmn = 0.0, dmx = 0.0;  // thread v < V: min/max of the new polynomial's variable v
     if (t < V) {
       const int v = t;
-      double cmn = red[v * NT], cmx = red[(V + v) * NT];
-      for (int q = 1; q < NT; ++q) { cmn = fmin(cmn, red[v * NT + q]); cmx = fmax(cmx, red[(V + v) * NT + q]); }
-      red[v * NT] = cmn;
-      red[(V + v) * NT] = cmx;
+      double cmn, cmx;
+      if (f32) {
+        float fmn = redf[v * NT], fmx = redf[(V + v) * NT];
+        for (int q = 1; q < NT; ++q) { fmn = fminf(fmn, redf[v * NT + q]); fmx = fmaxf(fmx, redf[(V + v) * NT + q]); }
+        cmn = UN[v * P2] + (double)fmn;
+        cmx = UN[v * P2] + (double)fmx;
+      } else {
+        cmn = red[v * NT];
+        cmx = red[(V + v) * NT];
+        for (int q = 1; q < NT; ++q) { cmn = fmin(cmn, red[v * NT + q]); cmx = fmax(cmx, red[(V + v) * NT + q]); }
+      }
+      dmn = cmn;
+      dmx = cmx;
       if (rec == 2) {
         const double* mmi = a.mm[par];
         double lmin = mmi[(size_t)c * 2 * V + v], lmax = mmi[(size_t)c * 2 * V + V + v];
@@ -455,9 +527,12 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS) k_subcell(BatchArg
     __syncthreads();
     if (t < V) {
       const int v = t;
-      double cmn = red[v * NT], cmx = red[(V + v) * NT];
-      if (limited)
+      double cmn = dmn, cmx = dmx;
+      if (limited) {
+        cmn = red[v * NT];
+        cmx = red[(V + v) * NT];
         for (int q = 1; q < NT; ++q) { cmn = fmin(cmn, red[v * NT + q]); cmx = fmax(cmx, red[(V + v) * NT + q]); }
+      }
       mmo[v] = cmn;
       mmo[V + v] = cmx;
     }

@@ -34,6 +34,7 @@
 
 namespace aderdg {
 void set_last_error(const std::string& msg);
+InstDesc make_inst_desc(const aderdg_config* cfg);
 }
 
 namespace {
@@ -162,20 +163,7 @@ extern "C" int aderdg_calc_time_step_noalloc(const aderdg_config* cfg, const dou
   unsigned long long* scratch = nullptr;
   int r = scratch_address(&scratch);
   if (r) return r;
-  aderdg::InstDesc in{};
-  in.imax = cfg->imax;
-  in.jmax = cfg->jmax;
-  in.dx = (cfg->xr[0] - cfg->xl[0]) / cfg->imax;
-  in.dy = (cfg->xr[1] - cfg->xl[1]) / cfg->jmax;
-  in.cfl_pnpm = cfg->cfl * aderdg::pnpm_cfl(cfg->N);
-  in.ph.gamma = cfg->gamma;
-  in.ph.gs = cfg->gamma_s;
-  in.ph.gg = cfg->gamma_g;
-  in.ph.ps = cfg->pi_s;
-  in.ph.pg = cfg->pi_g;
-  in.ph.cx = cfg->cx;
-  in.ph.cy = cfg->cy;
-  in.ph.a = cfg->a;
+  const aderdg::InstDesc in = aderdg::make_inst_desc(cfg);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   cudaError_t e = cudaMemsetAsync(scratch + kMaxBlocks, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) {

@@ -76,6 +76,35 @@ __device__ __forceinline__ void vload(const R* __restrict__ p, R* out) {
   }
 }
 
+// Stores V variables of one node as VP (padded) values with 16-byte vector
+// stores where VP allows (one vector per 4 floats / 2 doubles: no bank
+// conflicts between the lanes of a warp).
+template <class R, int V, int VP>
+__device__ __forceinline__ void vstore(R* __restrict__ p, const R* in) {
+  if constexpr (VP % (16 / sizeof(R)) != 0) {
+#pragma unroll
+    for (int q = 0; q < V; ++q) p[q] = in[q];
+  } else if constexpr (sizeof(R) == 4) {
+#pragma unroll
+    for (int q = 0; q < VP / 4; ++q) {
+      float4 t;
+      t.x = 4 * q + 0 < V ? in[4 * q + 0] : 0.0f;
+      t.y = 4 * q + 1 < V ? in[4 * q + 1] : 0.0f;
+      t.z = 4 * q + 2 < V ? in[4 * q + 2] : 0.0f;
+      t.w = 4 * q + 3 < V ? in[4 * q + 3] : 0.0f;
+      reinterpret_cast<float4*>(p)[q] = t;
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < VP / 2; ++q) {
+      double2 t;
+      t.x = 2 * q + 0 < V ? in[2 * q + 0] : 0.0;
+      t.y = 2 * q + 1 < V ? in[2 * q + 1] : 0.0;
+      reinterpret_cast<double2*>(p)[q] = t;
+    }
+  }
+}
+
 // Flux-derivative contraction of time level l into b[v]; flux buffer [P][2][P2][VP].
 template <int V, int VP, int P, class R>
 __device__ __forceinline__ void contract(const R* __restrict__ cs, int l, int i, int j, const R* Dx, const R* Dy, R* b) {
@@ -130,15 +159,32 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
   // per-thread contraction rows: Dx(i,k) = Kxi(k,i) dt/(dx w_i), Dy(j,k) likewise
   R Dx[P], Dy[P], Gx[P], Gy[P];
   {
-    const R cxw = R(dt / in.dx) / op.w[i];
-    const R cyw = R(dt / in.dy) / op.w[j];
+    // FP32: the reciprocals 1/dx, 1/dy held in FP32 (no FP64 divisions per thread)
+    R idx, idy, cxw, cyw;
+    if constexpr (sizeof(R) == 4) {
+      idx = in.idxf;
+      idy = in.idyf;
+      const R dtf = R(dt);
+      cxw = dtf * idx / op.w[i];
+      cyw = dtf * idy / op.w[j];
+    } else {
+      idx = R(1) / R(in.dx);
+      idy = R(1) / R(in.dy);
+      cxw = R(dt / in.dx) / op.w[i];
+      cyw = R(dt / in.dy) / op.w[j];
+    }
 #pragma unroll
     for (int k = 0; k < P; ++k) {
       Dx[k] = op.Kxi[k + P * i] * cxw;
       Dy[k] = op.Kxi[k + P * j] * cyw;
       // gradient rows dudx(i,k)/dx (BN volume fraction, AD state)
-      Gx[k] = op.dudx[i + P * k] / R(in.dx);
-      Gy[k] = op.dudx[j + P * k] / R(in.dy);
+      if constexpr (sizeof(R) == 4) {
+        Gx[k] = op.dudx[i + P * k] * idx;
+        Gy[k] = op.dudx[j + P * k] * idy;
+      } else {
+        Gx[k] = op.dudx[i + P * k] / R(in.dx);
+        Gy[k] = op.dudx[j + P * k] / R(in.dy);
+      }
     }
   }
 
@@ -255,11 +301,8 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
       } else {
         Sys::template pflux<R>(pc, u, Fx, Fy);
       }
-#pragma unroll
-      for (int v = 0; v < V; ++v) {
-        cs[fidx(0, 0, v)] = Fx[v];
-        cs[fidx(0, 1, v)] = Fy[v];
-      }
+      vstore<R, V, VP>(cs + fidx(0, 0, 0), Fx);
+      vstore<R, V, VP>(cs + fidx(0, 1, 0), Fy);
       __syncthreads();
       R b[V];
       contract<V, VP, P>(cs, 0, i, j, Dx, Dy, b);
@@ -297,11 +340,11 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
         } else {
           Sys::template pflux<R>(pc, q[l], Fx, Fy);
         }
+        vstore<R, V, VP>(cs + fidx(l, 0, 0), Fx);
+        vstore<R, V, VP>(cs + fidx(l, 1, 0), Fy);
+        if (last) {
 #pragma unroll
-        for (int v = 0; v < V; ++v) {
-          cs[fidx(l, 0, v)] = Fx[v];
-          cs[fidx(l, 1, v)] = Fy[v];
-          if (last) {
+          for (int v = 0; v < V; ++v) {
             Fh[0][v] = fma(op.w[l], Fx[v], Fh[0][v]);
             Fh[1][v] = fma(op.w[l], Fy[v], Fh[1][v]);
           }
@@ -381,7 +424,14 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
   } else {
     // volume integral: duh = (w_j/dx) sum_k Kxi(i,k) Fhi_x(k,j) + (w_i/dy) sum_k Kxi(j,k) Fhi_y(i,k) [+ w_i w_j Shi]
     // duh is stored in the compute precision R (FP32 in the mixed mode)
-    const R vx = op.w[j] / R(in.dx), vy = op.w[i] / R(in.dy);
+    R vx, vy;
+    if constexpr (sizeof(R) == 4) {
+      vx = op.w[j] * R(in.idxf);
+      vy = op.w[i] * R(in.idyf);
+    } else {
+      vx = op.w[j] / R(in.dx);
+      vy = op.w[i] / R(in.dy);
+    }
     R* dst = reinterpret_cast<R*>(a.duh) + ((size_t)cell * P2 + node) * V;
 #pragma unroll
     for (int v = 0; v < V; ++v) {

@@ -9,6 +9,7 @@
 // column pivoting for the inverses, and the constrained least-squares
 // reconstruction for the subcell-to-DG map.
 #include "setup.h"
+#include "ic_eval.h"
 
 #include <cmath>
 
@@ -140,6 +141,8 @@ bool invert(const Mat& A, Mat& inv) {
 
 }  // namespace
 
+double pi_value() { return kPi; }
+
 double pnpm_cfl(int N) {
   static const double t[10] = {1.0, 0.33, 0.17, 0.1, 0.069, 0.045, 0.038, 0.03, 0.02, 0.015};
   return (N >= 0 && N <= 9) ? t[N] : 0.0;
@@ -249,117 +252,8 @@ bool build_ops(int N, HostOps& o, std::string* err) {
 }  // namespace aderdg
 
 // ---------------------------------------------------------------------------
-// Initial fields.  The double Mach reflection (Euler/initialize.f90:311-341),
-// the Baer-Nunziato shock tubes (Baer-Nunziato/initialize.f90:302-407) and the
-// zero advection-diffusion field (Advection-Diffusion/initialize.f90:148-164)
-// are the reference's; the isentropic vortex, the 2D four-quadrant Riemann
-// problem, the two-phase cylinder and the sine wave are set-up extensions
-// with the parameters listed in aderdg_gpu.h.
-namespace {
-
-using aderdg::kPi;
-
-void euler_prim2cons(double g, const double* V, double* Q) {  // Euler/pde.f90:29-40
-  Q[0] = V[0];
-  Q[1] = V[0] * V[1];
-  Q[2] = V[0] * V[2];
-  Q[3] = V[3] / (g - 1) + 0.5 * V[0] * (V[1] * V[1] + V[2] * V[2]);
-}
-
-void bn_prim2cons(const aderdg_config& c, const double* V, double* Q) {  // Baer-Nunziato/pde.f90:49-68
-  const double gs = c.gamma_s, gg = c.gamma_g, ps = c.pi_s, pg = c.pi_g;
-  Q[0] = V[8] * V[0];
-  Q[1] = Q[0] * V[1];
-  Q[2] = Q[0] * V[2];
-  Q[3] = Q[0] * (0.5 * (V[1] * V[1] + V[2] * V[2]) + (V[3] + gs * ps) / (V[0] * (gs - 1.0)));
-  Q[4] = (1.0 - V[8]) * V[4];
-  Q[5] = Q[4] * V[5];
-  Q[6] = Q[4] * V[6];
-  Q[7] = Q[4] * (0.5 * (V[5] * V[5] + V[6] * V[6]) + (V[7] + gg * pg) / (V[4] * (gg - 1.0)));
-  Q[8] = V[8];
-}
-
-int eval_ic(const aderdg_config& c, int ic, const double* p, double x, double y, double* u) {
-  double V[9];
-  switch (ic) {
-    case ADERDG_IC_AD_ZERO:
-      u[0] = 0.0;
-      return 0;
-    case ADERDG_IC_AD_SINE:
-      u[0] = p[0] * std::sin(2.0 * kPi * x) * std::sin(2.0 * kPi * y);
-      return 0;
-    case ADERDG_IC_EULER_DMR:
-      if (x <= 1.0 / 6.0 + y / std::tan(kPi / 3.0)) {
-        V[0] = 8.0;
-        V[1] = 8.25 * std::cos(kPi / 6.0);
-        V[2] = -8.25 * std::sin(kPi / 6.0);
-        V[3] = 116.5;
-      } else {
-        V[0] = 1.4;
-        V[1] = 0.0;
-        V[2] = 0.0;
-        V[3] = 1.0;
-      }
-      euler_prim2cons(c.gamma, V, u);
-      return 0;
-    case ADERDG_IC_EULER_VORTEX: {
-      const double g = c.gamma, eps = p[0];
-      const double dx = x - p[1], dy = y - p[2], r2 = dx * dx + dy * dy;
-      const double amp = eps / (2.0 * kPi) * std::exp(0.5 * (1.0 - r2));
-      const double T0 = p[6] / p[3];
-      const double T = T0 + -(g - 1.0) * eps * eps / (8.0 * g * kPi * kPi) * std::exp(1.0 - r2);
-      const double rho = p[3] * std::pow(T / T0, 1.0 / (g - 1.0));
-      V[0] = rho;
-      V[1] = p[4] - amp * dy;
-      V[2] = p[5] + amp * dx;
-      V[3] = rho * T;
-      euler_prim2cons(g, V, u);
-      return 0;
-    }
-    case ADERDG_IC_EULER_RP2D: {
-      const int q = (y >= p[1]) ? (x >= p[0] ? 0 : 1) : (x < p[0] ? 2 : 3);
-      for (int k = 0; k < 4; ++k) V[k] = p[2 + 4 * q + k];
-      euler_prim2cons(c.gamma, V, u);
-      return 0;
-    }
-    case ADERDG_IC_BN_RP1D: {
-      static const double left[4][9] = {{1.0, 0.0, 0.0, 1.0, 0.5, 0.0, 0.0, 1.0, 0.4},
-                                        {800.0, 0.0, 0.0, 500.0, 1.5, 0.0, 0.0, 2.0, 0.4},
-                                        {1.0, 0.9, 0.0, 2.5, 1.0, 0.0, 0.0, 1.0, 0.9},
-                                        {800.0, 1.0, 0.0, 1.0, 2.0, 1.0, 0.0, 1.0, 0.99}};
-      static const double right[4][9] = {{2.0, 0.0, 0.0, 2.0, 1.5, 0.0, 0.0, 2.0, 0.8},
-                                         {1000.0, 0.0, 0.0, 600.0, 1.0, 0.0, 0.0, 1.0, 0.3},
-                                         {1.0, 0.0, 0.0, 1.0, 1.2, 1.0, 0.0, 2.0, 0.2},
-                                         {1000.0, 1.0, 0.0, 1.0, 1.0, 1.0, 0.0, 1.0, 0.01}};
-      const int t = (int)p[0];
-      const int row = t == 1 ? 0 : t == 2 ? 1 : t == 3 ? 2 : t == 7 ? 3 : -1;
-      if (row < 0) return -1;
-      const double* s = (x <= p[1]) ? left[row] : right[row];
-      for (int k = 0; k < 9; ++k) V[k] = s[k];
-      bn_prim2cons(c, V, u);
-      return 0;
-    }
-    case ADERDG_IC_BN_CYLINDER: {
-      const double dx = x - p[0], dy = y - p[1];
-      const double* s = (dx * dx + dy * dy < p[2] * p[2]) ? p + 3 : p + 8;
-      V[0] = s[1];
-      V[1] = 0.0;
-      V[2] = 0.0;
-      V[3] = s[2];
-      V[4] = s[3];
-      V[5] = 0.0;
-      V[6] = 0.0;
-      V[7] = s[4];
-      V[8] = s[0];
-      bn_prim2cons(c, V, u);
-      return 0;
-    }
-  }
-  return -1;
-}
-
-}  // namespace
-
+// Initial fields (ic_eval.h) at the Gauss-Legendre nodes of every cell and at
+// the subcell barycentres (Euler/initialize.f90:262-307).
 extern "C" int aderdg_project_initial_condition(const aderdg_config* cfg, int ic, const double* params, double* uh,
                                                 double* lh_ic) {
   if (!cfg || !uh || cfg->imax < 1 || cfg->jmax < 1) return ADERDG_EINVAL;
@@ -379,13 +273,15 @@ extern "C" int aderdg_project_initial_condition(const aderdg_config* cfg, int ic
       const long cell = (long)i + (long)I * j;
       for (int l = 0; l < P; ++l)
         for (int k = 0; k < P; ++k) {
-          if (eval_ic(*cfg, ic, p, x0 + ops.xi[k] * dx, y0 + ops.xi[l] * dy, u)) return ADERDG_EINVAL;
+          if (aderdg::eval_ic(*cfg, ic, p, aderdg::kPi, x0 + ops.xi[k] * dx, y0 + ops.xi[l] * dy, u))
+            return ADERDG_EINVAL;
           for (int v = 0; v < V; ++v) uh[v + V * (k + P * (l + P * cell))] = u[v];
         }
       if (lh_ic)
         for (int b = 0; b < S; ++b)
           for (int a = 0; a < S; ++a) {
-            if (eval_ic(*cfg, ic, p, x0 + ops.xilimbary[a] * dx, y0 + ops.xilimbary[b] * dy, u)) return ADERDG_EINVAL;
+            if (aderdg::eval_ic(*cfg, ic, p, aderdg::kPi, x0 + ops.xilimbary[a] * dx, y0 + ops.xilimbary[b] * dy, u))
+              return ADERDG_EINVAL;
             for (int v = 0; v < V; ++v) lh_ic[v + V * (a + S * (b + S * cell))] = u[v];
           }
     }

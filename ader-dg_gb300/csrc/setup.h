@@ -28,4 +28,8 @@ bool build_ops(int N, HostOps& ops, std::string* err);
 // Maximum CFL numbers of the PNPM schemes, Euler/ader_dg.f90:28.
 double pnpm_cfl(int N);
 
+// pi = 4 atan(1) as the host computes it (the initial fields use this value
+// on the host and on the device alike).
+double pi_value();
+
 }  // namespace aderdg

@@ -88,15 +88,6 @@ def predictor_flops_per_cell(system, N):
     return P * P * (it1 + max(N - 1, 0) * mid + last + vol) + 4 * P * V * 2 * 2 * P
 
 
-def cells_fp64_flops_per_cell(system, N):
-    """FP64 operations of the cell kernel per cell: the sum-factorised subcell
-    and Gauss-Lobatto projections of the DMP (y then x pass, one FMA per term;
-    none for advection-diffusion) and the update uh += dt duh / (w_i w_j)."""
-    P, V, S = N + 1, NVAR[system], 2 * N + 1
-    proj = 0 if system == 0 else 2 * V * P * (S * P + P * P + S * S + P * P)
-    return proj + 3 * V * P * P
-
-
 # ---------------------------------------------------------------- clocks
 class ClockSampler:
     FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
@@ -298,12 +289,11 @@ def run_mix(args, aderdg, dist, rank, ws, lr):
     steps0 = [groups[key].query(slot)["steps"] for key, slot, _ in slots]
     barrier(dist)
     with ClockSampler(lr) as clk:
-        t0 = time.perf_counter()
-        for g in groups.values():
-            g.launch(K)
-        for g in groups.values():
-            g.sync()
-        batched_s = time.perf_counter() - t0
+        # CUDA events on a timing stream that every group's stream waits for
+        # and that waits for all of them (the groups run concurrently)
+        batched_s = aderdg.Batch.run_timed(list(groups.values()), K) * 1e-3
+    for g in groups.values():
+        g.sync()
     batched_s = allmax(dist, batched_s)
     barrier(dist)
     # DOF-updates actually done in the timed region (a request that reaches its end time stops early)
@@ -311,35 +301,41 @@ def run_mix(args, aderdg, dist, rank, ws, lr):
     value = updates * ws / batched_s
     # dominant kernel: per-launch device times of one more (eager) step of every group
     phase_tot = {}
-    cells_flops = 0.0
+    pred_flops = 0.0
     for key, g in groups.items():
         ph = g.profile()
         for k, v in ph.items():
             phase_tot[k] = phase_tot.get(k, 0.0) + v
     for spec, cfg, ic, key in members:
-        cells_flops += cells_fp64_flops_per_cell(cfg.system, cfg.N) * cfg.cells
+        pred_flops += predictor_flops_per_cell(cfg.system, cfg.N) * cfg.cells
     dev_bytes = sum(g.info()["device_bytes"] for g in groups.values())
     for g in groups.values():
         g.close()
     if rank != 0:
         return None
     fp64_peak, fp32_peak = aderdg.probe_peaks()
-    cells_ms = phase_tot.get("cells", 0.0)
-    dominant = max((k for k in phase_tot if k not in ("begin", "end")), key=lambda k: phase_tot[k])
-    ach = cells_flops / (cells_ms * 1e-3) / 1e9 if cells_ms > 0 else None
-    roof = {"bound": "fp64", "kernel": "k_cells (all (system, N) groups of the mix)", "achieved": ach,
-            "peak": fp64_peak, "unit": "GFLOP/s", "frac": (ach / fp64_peak) if ach else None,
-            "peak_source": "measured by aderdg_probe_peaks (dependent-FMA microkernel on this GPU); "
-                           "MEASURED_PEAKS.json carries no FP64 non-tensor figure",
-            "flops_per_launch": cells_flops, "launch_ms": cells_ms, "dominant_phase": dominant,
+    mixed = prec == aderdg.FP32_MIXED
+    peak = fp32_peak if mixed else fp64_peak
+    pred_ms = phase_tot.get("predictor", 0.0)
+    kern_ms = {k: v for k, v in phase_tot.items() if k not in ("begin", "end")}
+    dominant = max(kern_ms, key=lambda k: kern_ms[k])
+    ach = pred_flops / (pred_ms * 1e-3) / 1e9 if pred_ms > 0 else None
+    roof = {"bound": "fp32" if mixed else "fp64", "kernel": "k_predictor (all (system, N) groups of the mix)",
+            "achieved": ach, "peak": peak, "unit": "GFLOP/s", "frac": (ach / peak) if ach else None,
+            "peak_source": "FMA throughput measured on this GPU by aderdg_probe_peaks (dependent-FMA "
+                           "microkernel); MEASURED_PEAKS.json carries no non-tensor FP32/FP64 figure",
+            "flops_per_launch": pred_flops, "flop_model": "bench.py predictor_flops_per_cell x cells",
+            "launch_ms": pred_ms, "dominant_phase": dominant,
+            "phase_share": {k: v / sum(kern_ms.values()) for k, v in kern_ms.items()},
             "phase_ms_one_step": phase_tot, "traffic": None}
     try:
         with open(os.path.join(REPO, "profiles", "traffic.json")) as fh:
             tr = json.load(fh)
-        per = tr.get("k_cells_fp32mixed_bytes_per_dof")
+        per = tr.get("k_predictor_fp32mixed_bytes_per_dof" if mixed else "k_predictor_fp64_bytes_per_dof")
         if per:
             roof["traffic"] = per * total_dofs
-            roof["traffic_note"] = "DRAM bytes per DOF of k_cells from one ncu capture (profiles/), times the mix's DOFs"
+            roof["traffic_note"] = ("DRAM bytes per DOF of k_predictor from one ncu capture (profiles/traffic.json), "
+                                    "times the DOFs of the mix")
     except (OSError, ValueError):
         pass
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,

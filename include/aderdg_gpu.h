@@ -246,6 +246,11 @@ int aderdg_batch_info(aderdg_batch* b, long* used_units, long* capacity_units, l
 /* One fused step of the batch, eager, with CUDA events between its launches:
  * device ms of each in phase_ms[7] (as aderdg_profile_step). */
 int aderdg_batch_profile(aderdg_batch* b, double* phase_ms);
+/* Measurement hook: `steps` fused steps of each of n batches, the batches on
+ * their own streams concurrently, bracketed by CUDA events on a timing stream
+ * that every batch stream waits for and that waits for all of them; *ms = the
+ * device time between the two events.  Returns after the second event. */
+int aderdg_batch_run_timed(aderdg_batch* const* batches, int n, int steps, double* ms);
 const char* aderdg_batch_last_error(aderdg_batch* b);
 
 /* ---- host setup helpers (initial fields; not on the hot path) ---- */

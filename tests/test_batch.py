@@ -38,7 +38,8 @@ MEMBERS = {
 
 
 @pytest.mark.parametrize("system,N,prec", [(aderdg.SYS_EULER, 3, aderdg.FP64), (aderdg.SYS_EULER, 3, aderdg.FP32_MIXED),
-                                           (aderdg.SYS_BN, 2, aderdg.FP64), (aderdg.SYS_ADVDIFF, 4, aderdg.FP64)])
+                                           (aderdg.SYS_BN, 2, aderdg.FP64), (aderdg.SYS_BN, 3, aderdg.FP32_MIXED),
+                                           (aderdg.SYS_ADVDIFF, 4, aderdg.FP64), (aderdg.SYS_ADVDIFF, 3, aderdg.FP32_MIXED)])
 def test_batch_results_equal_alone(gpu_lib, system, N, prec):
     members = []
     for name, side, over in MEMBERS[system]:

@@ -197,6 +197,25 @@ def test_fp32_mixed_error_vs_fp64_oracle(gpu_lib, name, N, side):
     assert rel_l1(ug, o.get(po.UH)) <= 1e-5
 
 
+def test_fp32_mixed_large_magnitudes(gpu_lib):
+    """States of magnitude ~1e3 (the 2D Riemann problem with density and
+    pressure scaled by 1000): FP32 projection errors would exceed the DMP's
+    absolute tolerance 1e-4 there, so the mixed mode must take its FP64
+    projections for those cells and still agree with the FP64 oracle."""
+    cfg, ic, params, tend = aderdg.workloads.make("euler_rp2d", side=16, N=3, precision=aderdg.FP32_MIXED)
+    p = list(params)
+    for q in range(4):
+        p[2 + 4 * q] *= 1000.0
+        p[5 + 4 * q] *= 1000.0
+    o, g, uh, lh = setup_pair(cfg, ic, tuple(p))
+    t_o = t_g = 0.0
+    for _ in range(5):
+        t_o, _, n_o = o.step(t_o, tend)
+        t_g, _, n_g = g.step(t_g, tend)
+    ug, _ = g.download()
+    assert rel_l1(ug, o.get(po.UH)) <= 1e-5
+
+
 def test_nonfinite_state_reported(gpu_lib):
     cfg = aderdg.Config(system=aderdg.SYS_EULER, N=2, imax=4, jmax=4, bc=(3, 3, 3, 3), limiter=0)
     uh = np.tile(np.array([1.0, 0.0, 0.0, 2.5]), cfg.cells * 9)
