@@ -160,6 +160,8 @@ def load(build_if_missing=False):
                                   ctypes.POINTER(ctypes.c_long), ip]),
         "aderdg_batch_last_error": (ctypes.c_char_p, [vp]), "aderdg_batch_profile": (i, [vp, dp]),
         "aderdg_batch_run_timed": (i, [ctypes.POINTER(vp), i, i, dp]),
+        "aderdg_initial_condition": (i, [vp, i, dp, ip]),
+        "aderdg_batch_admit_ic": (i, [vp, cfgp, i, dp, d, ctypes.c_long, ip]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -179,7 +181,7 @@ EXPORTED = ("aderdg_create", "aderdg_destroy", "aderdg_upload", "aderdg_init_lim
             "aderdg_batch_unit_bytes", "aderdg_batch_create", "aderdg_batch_destroy", "aderdg_batch_admit",
             "aderdg_batch_release", "aderdg_batch_launch", "aderdg_batch_sync", "aderdg_batch_query",
             "aderdg_batch_download", "aderdg_batch_info", "aderdg_batch_last_error", "aderdg_batch_profile",
-            "aderdg_batch_run_timed")
+            "aderdg_batch_run_timed", "aderdg_initial_condition", "aderdg_batch_admit_ic")
 
 
 def _dp(a):
@@ -273,6 +275,15 @@ class Solver:
         n = ctypes.c_int(0)
         lh = None if lh_ic is None else np.ascontiguousarray(lh_ic, dtype=np.float64).ravel()
         self._ck(self.L.aderdg_init_limiter(self.h, None if lh is None else _dp(lh), ctypes.byref(n)))
+        return n.value
+
+    def initial_condition(self, ic, params=()):
+        """Initial field and initial limiter evaluated on the device; returns
+        the number of cells the initial limiter marked."""
+        p = np.zeros(32, dtype=np.float64)
+        p[: len(params)] = params
+        n = ctypes.c_int(0)
+        self._ck(self.L.aderdg_initial_condition(self.h, ic, _dp(p), ctypes.byref(n)))
         return n.value
 
     def upload_limiter(self, status, lh):
@@ -431,6 +442,20 @@ class Batch:
         slot = ctypes.c_int(-1)
         r = self.L.aderdg_batch_admit(self.h, ctypes.byref(c), _dp(uh), None if lh is None else _dp(lh), tend,
                                       int(max_steps), ctypes.byref(slot))
+        if r == -8:
+            return None
+        self._ck(r)
+        self.cfgs[slot.value] = cfg
+        return slot.value
+
+    def admit_ic(self, cfg, ic, params=(), tend=1e30, max_steps=0):
+        """Admission with the initial field evaluated on the device; the slot
+        id, or None when the batch has no room."""
+        c = cfg.to_c()
+        p = np.zeros(32, dtype=np.float64)
+        p[: len(params)] = params
+        slot = ctypes.c_int(-1)
+        r = self.L.aderdg_batch_admit_ic(self.h, ctypes.byref(c), ic, _dp(p), tend, int(max_steps), ctypes.byref(slot))
         if r == -8:
             return None
         self._ck(r)

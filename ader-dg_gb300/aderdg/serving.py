@@ -6,8 +6,9 @@ its group has room, into the batch of its (system, N) group; a batch steps all
 its simulations with one set of launches, each simulation with its own CFL
 time step, and groups run concurrently on their own CUDA streams.  Finished
 simulations are downloaded and released, freeing room for waiting requests
-while the others keep running on the GPU.  Initial fields are projected on a
-host thread pool so that admission does not stall the loop.
+while the others keep running on the GPU.  Initial fields are evaluated on
+the device at admission (device_setup=True, only the request's parameters
+cross to the device), or projected on a host thread pool and copied in.
 
 Reported per run: aggregate DOF-updates/s over the makespan and the p50/p99
 time-to-solution (arrival to result on the host) of the requests.
@@ -53,12 +54,16 @@ class Server:
     """Admits requests into per-(system, N) batches under an HBM budget."""
 
     def __init__(self, hbm_budget_bytes, precision=FP64, max_instances=256, sync_every=4, workers=8,
-                 keep_results=False):
+                 keep_results=False, device_setup=True, download_results=True):
         self.budget = int(hbm_budget_bytes)
         self.precision = precision
         self.max_instances = max_instances
         self.sync_every = sync_every
         self.keep_results = keep_results
+        self.download_results = download_results or keep_results
+        self.device_setup = device_setup
+        self.h2d_bytes = 0
+        self.d2h_bytes = 0
         self.groups = {}
         self.pool = concurrent.futures.ThreadPoolExecutor(max_workers=workers)
 
@@ -101,22 +106,30 @@ class Server:
             now = clock()
             while pending and pending[0].arrival <= now:
                 r = pending.popleft()
-                futures[r.rid] = self.pool.submit(self._prepare, r)
+                if not self.device_setup:
+                    futures[r.rid] = self.pool.submit(self._prepare, r)
                 waiting[r.group].append(r)
             # admit in arrival order per group while there is room
             for g, q in waiting.items():
                 b = self.groups[g]
                 while q:
                     r = q[0]
-                    f = futures[r.rid]
-                    if not f.done():
-                        break
-                    uh, lh = f.result()
-                    slot = b.admit(r.cfg, uh, lh, r.tend, r.max_steps)
-                    if slot is None:
-                        break
+                    if self.device_setup:
+                        slot = b.admit_ic(r.cfg, r.ic, r.params, r.tend, r.max_steps)
+                        if slot is None:
+                            break
+                        self.h2d_bytes += 32 * 8
+                    else:
+                        f = futures[r.rid]
+                        if not f.done():
+                            break
+                        uh, lh = f.result()
+                        slot = b.admit(r.cfg, uh, lh, r.tend, r.max_steps)
+                        if slot is None:
+                            break
+                        del futures[r.rid]
+                        self.h2d_bytes += uh.nbytes + (lh.nbytes if lh is not None else 0)
                     q.popleft()
-                    del futures[r.rid]
                     r.slot, r.admitted = slot, clock()
                     running[g][slot] = r
             active = [g for g in self.groups if running[g]]
@@ -135,8 +148,11 @@ class Server:
                     r = running[g][slot]
                     q = b.query(slot)
                     if q["done"]:
-                        if self.keep_results:
-                            r.result = b.download(slot)
+                        if self.download_results:
+                            res = b.download(slot)
+                            self.d2h_bytes += res.nbytes
+                            if self.keep_results:
+                                r.result = res
                         r.steps, r.time, r.finished = q["steps"], q["time"], clock()
                         total_steps_dofs += r.steps * r.dofs
                         b.release(slot)
@@ -152,6 +168,8 @@ class Server:
             "tts_p50_s": float(np.percentile(tts, 50)),
             "tts_p99_s": float(np.percentile(tts, 99)),
             "groups": len(self.groups),
+            "h2d_bytes": self.h2d_bytes,
+            "d2h_bytes": self.d2h_bytes,
             "requests_done": done,
         }
 

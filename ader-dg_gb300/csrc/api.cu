@@ -417,6 +417,39 @@ int aderdg_init_limiter(aderdg_ctx* c, const double* lh_ic, int* n_limited) {
   return r;
 }
 
+int aderdg_initial_condition(aderdg_ctx* c, int ic, const double* params, int* n_limited) {
+  if (!c) return fail(c, ADERDG_EINVAL, "null context");
+  if (n_limited) *n_limited = 0;
+  const int par = cur_par(c);
+  // the subcell candidates are staged in the other Lh buffer: the initial
+  // DMP copies them into both buffers for the cells it limits
+  double* lh_stage = c->limiter ? c->args.lh[par ^ 1] : nullptr;
+  std::string why;
+  cudaError_t e = aderdg::launch_initial_field(c->cfg, ic, params, c->args.uh[par], lh_stage, c->stream, &why);
+  if (e == cudaErrorInvalidValue && !why.empty()) return fail(c, ADERDG_EINVAL, why);
+  if (e != cudaSuccess) return fail_cuda(c, "initial field", e);
+  if (c->limiter) {
+    CK(c, cudaMemsetAsync(c->args.status[0], 0, c->ncells * sizeof(int), c->stream));
+    CK(c, cudaMemsetAsync(c->args.status[1], 0, c->ncells * sizeof(int), c->stream));
+  }
+  c->pending = false;
+  int r = prime(c);
+  if (!r) r = pull_state(c);
+  if (r) return r;
+  c->uploaded = true;
+  if (!c->limiter) return ADERDG_OK;
+  c->args.lh_ic = lh_stage;
+  CK(c, control(c, aderdg::kCtlPrimeReset));
+  r = cells(c, aderdg::kCellInitDmp);
+  c->args.lh_ic = nullptr;
+  if (!r) r = pull_state(c);
+  if (r) return r;
+  if (n_limited) *n_limited = c->h_st->n_recompute;
+  r = prime(c);
+  if (!r) r = pull_state(c);
+  return r;
+}
+
 int aderdg_upload_limiter(aderdg_ctx* c, const int* status, const double* lh) {
   if (!c || !status || !lh) return fail(c, ADERDG_EINVAL, "null argument");
   if (!c->limiter) return ADERDG_OK;

@@ -24,6 +24,7 @@
 
 #include "../../include/aderdg_gpu.h"
 #include "control.cuh"
+#include "ic_eval.h"
 #include "tables.h"
 
 namespace aderdg {
@@ -324,9 +325,19 @@ int aderdg_batch_destroy(aderdg_batch* b) {
   return ADERDG_OK;
 }
 
-int aderdg_batch_admit(aderdg_batch* b, const aderdg_config* cfg, const double* uh, const double* lh_ic, double tend,
-                       long max_steps, int* slot) {
-  if (!b || !cfg || !uh || !slot) return bfail(b, ADERDG_EINVAL, "null argument");
+namespace {
+
+// Admission of one simulation: its initial state comes from host arrays
+// (uh, lh_ic) or, with ic >= 0, is evaluated on the device.
+int badmit(aderdg_batch* b, const aderdg_config* cfg, const double* uh, const double* lh_ic, int ic,
+           const double* params, double tend, long max_steps, int* slot) {
+  if (!b || !cfg || !slot || (ic < 0 && !uh)) return bfail(b, ADERDG_EINVAL, "null argument");
+  if (ic >= 0) {
+    double p[32] = {0};
+    if (params) std::memcpy(p, params, sizeof(p));
+    if (!aderdg::ic_valid(cfg->system, ic, p))
+      return bfail(b, ADERDG_EINVAL, "initial field " + std::to_string(ic) + " is not defined for this system");
+  }
   std::string why;
   int r = aderdg::validate_config(cfg, &why);
   if (r) return bfail(b, r, why);
@@ -372,20 +383,31 @@ int aderdg_batch_admit(aderdg_batch* b, const aderdg_config* cfg, const double* 
   recompute_hw(b);
   r = push_table(b);
   if (r) return r;
-  // state of the new simulation (parity 0)
+  // state of the new simulation (parity 0); the subcell candidates of the
+  // initial limiter are staged in the next-parity Lh slab of this simulation
   const size_t cells = (size_t)cfg->imax * cfg->jmax, P2V = (size_t)b->P * b->P * b->V, S2V = (size_t)b->S * b->S * b->V;
-  BK(b, cudaMemcpyAsync(b->args.uh[0] + (size_t)base * P2V, uh, cells * P2V * sizeof(double), cudaMemcpyHostToDevice,
-                        b->stream));
+  double* uh_dst = b->args.uh[0] + (size_t)base * P2V;
+  double* lh_stage = b->limiter ? b->args.lh[1] + (size_t)base * S2V : nullptr;
+  bool staged = false;
+  if (ic >= 0) {
+    std::string why;
+    cudaError_t e = aderdg::launch_initial_field(*cfg, ic, params, uh_dst, lh_stage, b->stream, &why);
+    if (e != cudaSuccess) return bcuda(b, ("initial field: " + why).c_str(), e);
+    staged = lh_stage != nullptr;
+  } else {
+    BK(b, cudaMemcpyAsync(uh_dst, uh, cells * P2V * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  }
   if (b->limiter) {
     BK(b, cudaMemsetAsync(b->args.status[0] + base, 0, cells * sizeof(int), b->stream));
     BK(b, cudaMemsetAsync(b->args.status[1] + base, 0, cells * sizeof(int), b->stream));
   }
   r = bprime_one(b, pos);
   if (r) return r;
-  if (b->limiter && lh_ic) {
-    // stage the subcell candidates in the next-parity Lh slab of this simulation
-    BK(b, cudaMemcpyAsync(b->args.lh[1] + (size_t)base * S2V, lh_ic, cells * S2V * sizeof(double),
-                          cudaMemcpyHostToDevice, b->stream));
+  if (b->limiter && ic < 0 && lh_ic) {
+    BK(b, cudaMemcpyAsync(lh_stage, lh_ic, cells * S2V * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+    staged = true;
+  }
+  if (staged) {
     BK(b, bcontrol(b, aderdg::kCtlPrimeReset, pos));
     r = bcells_one(b, pos, aderdg::kCellInitDmp, b->args.lh[1]);
     if (r) return r;
@@ -396,6 +418,19 @@ int aderdg_batch_admit(aderdg_batch* b, const aderdg_config* cfg, const double* 
   if (r) return r;
   *slot = s;
   return ADERDG_OK;
+}
+
+}  // namespace
+
+int aderdg_batch_admit(aderdg_batch* b, const aderdg_config* cfg, const double* uh, const double* lh_ic, double tend,
+                       long max_steps, int* slot) {
+  return badmit(b, cfg, uh, lh_ic, -1, nullptr, tend, max_steps, slot);
+}
+
+int aderdg_batch_admit_ic(aderdg_batch* b, const aderdg_config* cfg, int ic, const double* params, double tend,
+                          long max_steps, int* slot) {
+  if (ic < 0) return bfail(b, ADERDG_EINVAL, "bad initial field id");
+  return badmit(b, cfg, nullptr, nullptr, ic, params, tend, max_steps, slot);
 }
 
 int aderdg_batch_release(aderdg_batch* b, int slot) {

@@ -115,6 +115,25 @@ __device__ __forceinline__ void rusanov_s(const PhysC<T>& pc, const T* QL, const
   if constexpr (Sys::ID == kSysBN) BNSys::roe_times_jump(pc, QL, QR, d, D);
 }
 
+// Warp-wide min/max of V values per lane (butterfly), then lane 0 of warp w
+// stores them at red[v * NW + w] (min) and red[(V + v) * NW + w] (max).
+template <class R, int V, int NW>
+__device__ __forceinline__ void warp_minmax_store(R* mn, R* mx, R* red, int t) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      mn[v] = tmin(mn[v], __shfl_xor_sync(0xffffffffu, mn[v], o));
+      mx[v] = tmax(mx[v], __shfl_xor_sync(0xffffffffu, mx[v], o));
+    }
+  if ((t & 31) == 0)
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      red[v * NW + (t >> 5)] = mn[v];
+      red[(V + v) * NW + (t >> 5)] = mx[v];
+    }
+}
+
 // T = double: the reference's FP64 arithmetic in its order (bit for bit).
 // T = float: the FP32-mixed mode; the subcell re-solve, the DMP projections
 // of the new polynomial (while their error bound allows) and its CFL
@@ -123,6 +142,7 @@ template <class Sys, int N, class T>
 __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS) k_subcell(BatchArgs a, DevOps<N, double> op, FaceConst fc) {
   using C = SubCfg<Sys, N, T>;
   constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1, V = Sys::V, R = C::R, H = C::H, NT = C::THREADS, NE = C::NE;
+  constexpr int NW = NT / 32;  // warps
   constexpr bool BN = Sys::ID == kSysBN;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sub0 = reinterpret_cast<T*>(smem_raw);
@@ -444,8 +464,7 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS) k_subcell(BatchArg
         Proj<N, V, float>::template xpass_minmax_f32<Sys>(LYf, LBf, limT, lobT, UN, op, typename Sys::FConst(ph), err,
                                                           ubf, ph, t, NT, fmn, fmx, posfail);
       }
-#pragma unroll
-      for (int v = 0; v < V; ++v) { redf[v * NT + t] = fmn[v]; redf[(V + v) * NT + t] = fmx[v]; }
+      warp_minmax_store<float, V, NW>(fmn, fmx, redf, t);
       // CFL denominator of the new polynomial (FP32 eigenvalues)
       for (int p = t; p < P2; p += NT) {
         float q[V];
@@ -457,8 +476,7 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS) k_subcell(BatchArg
 #pragma unroll
       for (int v = 0; v < V; ++v) { mn[v] = kInf; mx[v] = -kInf; }
       Proj<N, V, double>::template xpass_minmax<Sys>(UN, LY, LB, opsm, opsm + S * P, ph, t, NT, mn, mx, posfail);
-#pragma unroll
-      for (int v = 0; v < V; ++v) { red[v * NT + t] = mn[v]; red[(V + v) * NT + t] = mx[v]; }
+      warp_minmax_store<double, V, NW>(mn, mx, red, t);
       // CFL denominator of the new polynomial
       for (int p = t; p < P2; p += NT) {
         double Q[V];
@@ -475,14 +493,14 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS) k_subcell(BatchArg
       const int v = t;
       double cmn, cmx;
       if (f32) {
-        float fmn = redf[v * NT], fmx = redf[(V + v) * NT];
-        for (int q = 1; q < NT; ++q) { fmn = fminf(fmn, redf[v * NT + q]); fmx = fmaxf(fmx, redf[(V + v) * NT + q]); }
+        float fmn = redf[v * NW], fmx = redf[(V + v) * NW];
+        for (int q = 1; q < NW; ++q) { fmn = fminf(fmn, redf[v * NW + q]); fmx = fmaxf(fmx, redf[(V + v) * NW + q]); }
         cmn = UN[v * P2] + (double)fmn;
         cmx = UN[v * P2] + (double)fmx;
       } else {
-        cmn = red[v * NT];
-        cmx = red[(V + v) * NT];
-        for (int q = 1; q < NT; ++q) { cmn = fmin(cmn, red[v * NT + q]); cmx = fmax(cmx, red[(V + v) * NT + q]); }
+        cmn = red[v * NW];
+        cmx = red[(V + v) * NW];
+        for (int q = 1; q < NW; ++q) { cmn = fmin(cmn, red[v * NW + q]); cmx = fmax(cmx, red[(V + v) * NW + q]); }
       }
       dmn = cmn;
       dmx = cmx;
@@ -504,34 +522,33 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS) k_subcell(BatchArg
     __syncthreads();
     // status: recompute 1 -> limited; recompute 2 -> limited only when the DMP fails
     const bool limited = rec == 1 || (rec == 2 && flag[0] != 0);
+    // min/max over the new subcell data (get_min_max of the next step), in T
+    T* redt = reinterpret_cast<T*>(red);
     if (limited) {
       double* nl = a.lh[par ^ 1] + (size_t)c * S * S * V;
       for (int p = t; p < S * S; p += NT)
 #pragma unroll
         for (int v = 0; v < V; ++v) nl[p * V + v] = (double)sub1[v * S * S + p];
-      // min/max over the new subcell data (get_min_max of the next step)
-      for (int v = 0; v < V; ++v) { mn[v] = kInf; mx[v] = -kInf; }
+      T tmn[V], tmx[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) { tmn[v] = T(kInf); tmx[v] = T(-kInf); }
       for (int p = t; p < S * S; p += NT)
 #pragma unroll
         for (int v = 0; v < V; ++v) {
-          const double x = (double)sub1[v * S * S + p];
-          mn[v] = fmin(mn[v], x);
-          mx[v] = fmax(mx[v], x);
+          tmn[v] = tmin(tmn[v], sub1[v * S * S + p]);
+          tmx[v] = tmax(tmx[v], sub1[v * S * S + p]);
         }
-    }
-    __syncthreads();
-    if (limited) {
-#pragma unroll
-      for (int v = 0; v < V; ++v) { red[v * NT + t] = mn[v]; red[(V + v) * NT + t] = mx[v]; }
+      warp_minmax_store<T, V, NW>(tmn, tmx, redt, t);
     }
     __syncthreads();
     if (t < V) {
       const int v = t;
       double cmn = dmn, cmx = dmx;
       if (limited) {
-        cmn = red[v * NT];
-        cmx = red[(V + v) * NT];
-        for (int q = 1; q < NT; ++q) { cmn = fmin(cmn, red[v * NT + q]); cmx = fmax(cmx, red[(V + v) * NT + q]); }
+        T lo = redt[v * NW], hi = redt[(V + v) * NW];
+        for (int q = 1; q < NW; ++q) { lo = tmin(lo, redt[v * NW + q]); hi = tmax(hi, redt[(V + v) * NW + q]); }
+        cmn = (double)lo;
+        cmx = (double)hi;
       }
       mmo[v] = cmn;
       mmo[V + v] = cmx;

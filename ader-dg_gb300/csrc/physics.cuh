@@ -35,6 +35,9 @@ template <class T> __device__ __forceinline__ T tabs(T x) {
 template <class T> __device__ __forceinline__ T tmax(T a, T b) {
   if constexpr (sizeof(T) == 4) return fmaxf(a, b); else return fmax(a, b);
 }
+template <class T> __device__ __forceinline__ T tmin(T a, T b) {
+  if constexpr (sizeof(T) == 4) return fminf(a, b); else return fmin(a, b);
+}
 template <class T> __device__ __forceinline__ T tsqrt(T x) {
   if constexpr (sizeof(T) == 4) return sqrtf(x); else return sqrt(x);
 }

@@ -8,7 +8,9 @@
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <string>
 
+#include "../../include/aderdg_gpu.h"
 #include "common.cuh"
 #include "setup.h"
 
@@ -31,6 +33,12 @@ struct KernelTable {
   cudaError_t (*subcell)(const BatchArgs&, const void* ops64, const FaceConst&, int grid, int fp32, cudaStream_t) = nullptr;
   int (*subcell_grid)(int num_sms, int fp32) = nullptr;
 };
+
+// On-device initial field of one simulation (initial.cu): uh at the
+// Gauss-Legendre nodes and, when lh is non-null, the values at the subcell
+// barycentres.  cudaErrorInvalidValue with *why set for an unknown field.
+cudaError_t launch_initial_field(const aderdg_config& cfg, int ic, const double* params, double* uh, double* lh,
+                                 cudaStream_t s, std::string* why);
 
 // Returns the table for (sys, N) or nullptr when that pair was not built.
 const KernelTable* kernel_table(int sys, int N);

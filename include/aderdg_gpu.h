@@ -264,8 +264,18 @@ enum aderdg_ic {
   ADERDG_IC_BN_CYLINDER = 21  /* p = {x0, y0, R, inside (a_s,rho_s,p_s,rho_g,p_g), outside (...)} */
 };
 /* Projects an initial field onto the Gauss-Legendre nodes (uh) and evaluates
- * it at the subcell barycentres (lh_ic, nullable) as initialize does. */
+ * it at the subcell barycentres (lh_ic, nullable) as initialize does
+ * (Euler/initialize.f90:262-307), on the host.  params: up to 32 doubles. */
 int aderdg_project_initial_condition(const aderdg_config* cfg, int ic, const double* params, double* uh, double* lh_ic);
+/* The same on the device: the context's uh from the initial field, then the
+ * initial limiter (aderdg_upload + aderdg_init_limiter without host arrays).
+ * Values agree with the host set-up up to the rounding of transcendental
+ * functions by the device math library. */
+int aderdg_initial_condition(aderdg_ctx* ctx, int ic, const double* params, int* n_limited);
+/* Batch admission with the initial field evaluated on the device (no host
+ * projection, no host-to-device copy of uh / lh_ic); as aderdg_batch_admit. */
+int aderdg_batch_admit_ic(aderdg_batch* b, const aderdg_config* cfg, int ic, const double* params, double tend,
+                          long max_steps, int* slot);
 
 /* One-dimensional operators of degree N as built on the host
  * (Euler/initialize.f90:88-213), column-major.  Returns the element count. */
