@@ -92,7 +92,7 @@ long long unit_bytes(int system, int N, int precision, int limiter) {
   b += rb * P * 4 * V * (system == ADERDG_SYS_ADVDIFF ? 3 : 2);     // qbnd, fbnd / gradQbnd
   b += 8 * P * V * (system == ADERDG_SYS_BN ? 4 : 2);               // face fluxes
   if (limiter && system != ADERDG_SYS_ADVDIFF)
-    b += 8 * V * S * S * 2 + 4 * 2 + 8 * 2 * V * 3 + 1 + 4 + 4 + 8;  // Lh[2], status[2], mm[2], lminmax, flags, list, denom
+    b += 8 * V * S * S * 2 + 4 * 2 + 8 * 2 * V * 2 + 1 + 4 + 4 + 8;  // Lh[2], status[2], mm[2], flags, list, denom
   return b;
 }
 
@@ -279,7 +279,8 @@ int aderdg_batch_create(int system, int N, int precision, int limiter, long capa
     if (!r) r = balloc(b, &a.lh[1], U * S * S * V);
     if (!r) r = balloc(b, &a.mm[0], U * 2 * V);
     if (!r) r = balloc(b, &a.mm[1], U * 2 * V);
-    if (!r) r = balloc(b, &a.lminmax, U * 2 * V);
+    // no lminmax: the neighbourhood bounds are an introspection output of
+    // the single-simulation API only
     if (!r) r = balloc(b, &a.troubled, U);
     if (!r) r = balloc(b, &a.recompute, U);
     if (!r) r = balloc(b, &a.list, U);

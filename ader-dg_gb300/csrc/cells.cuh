@@ -273,6 +273,44 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
   float* REDf = LBf + V * P * P;
   unsigned* amax = amax_all + (in_cta ? lc : 0) * V;
 
+  // DMP neighbourhood bounds (get_min_max step 2, Euler/limiter.f90:147-167):
+  // thread v < V of a cell folds its 3x3 Voronoi neighbourhood now, so the
+  // global loads overlap the update and the projections
+  double nlmin = 0.0, nlmax = 0.0;
+  if (limiter && act && node < V && (mode == kCellFused || mode == kCellUpdate)) {
+    const int v = node;
+    const double* mmi = a.mm[par];
+    nlmin = mmi[(size_t)cell * 2 * V + v];
+    nlmax = mmi[(size_t)cell * 2 * V + V + v];
+    if constexpr (kFast) {
+      // integer-key min/max (the integer pipe, not FP64)
+      long long kmn = okey(nlmin), kmx = okey(nlmax);
+#pragma unroll
+      for (int jj = -1; jj <= 1; ++jj)
+#pragma unroll
+        for (int ii = -1; ii <= 1; ++ii) {
+          const int in_ = nb_index(ci, ii, in.imax, in.bc[0], in.bc[1]);
+          const int jn_ = nb_index(cj, jj, in.jmax, in.bc[2], in.bc[3]);
+          const long long nc = in.cell_base + in_ + (long long)in.imax * jn_;
+          kmn = min(kmn, okey(mmi[(size_t)nc * 2 * V + v]));
+          kmx = max(kmx, okey(mmi[(size_t)nc * 2 * V + V + v]));
+        }
+      nlmin = okey_inv(kmn);
+      nlmax = okey_inv(kmx);
+    } else {
+#pragma unroll
+      for (int jj = -1; jj <= 1; ++jj)
+#pragma unroll
+        for (int ii = -1; ii <= 1; ++ii) {
+          const int in_ = nb_index(ci, ii, in.imax, in.bc[0], in.bc[1]);
+          const int jn_ = nb_index(cj, jj, in.jmax, in.bc[2], in.bc[3]);
+          const long long nc = in.cell_base + in_ + (long long)in.imax * jn_;
+          nlmin = fmin(nlmin, mmi[(size_t)nc * 2 * V + v]);
+          nlmax = fmax(nlmax, mmi[(size_t)nc * 2 * V + V + v]);
+        }
+    }
+  }
+
   // projection operators into shared memory (lanes index them by subcell)
   for (int k = t; k < C::OPS_DBL; k += blockDim.x) {
     opsm[k] = k < S * P ? op.uh2lim[k] : op.uh2lob[k - S * P];
@@ -509,6 +547,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
       double cmn, cmx;
       if (f32red) {
         float fmn = REDf[v * P2], fmx = REDf[(V + v) * P2];
+#pragma unroll
         for (int k = 1; k < P2; ++k) { fmn = fminf(fmn, REDf[v * P2 + k]); fmx = fmaxf(fmx, REDf[(V + v) * P2 + k]); }
         const double ubar = a.uh[par][(size_t)cell * P2 * V + v];
         cmn = ubar + (double)fmn;
@@ -516,6 +555,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
       } else {
         cmn = RED[v * P2];
         cmx = RED[(V + v) * P2];
+#pragma unroll
         for (int k = 1; k < P2; ++k) { cmn = fmin(cmn, RED[v * P2 + k]); cmx = fmax(cmx, RED[(V + v) * P2 + k]); }
       }
       if (mode == kCellPrime) {
@@ -530,34 +570,9 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
           for (int k = 1; k < P2; ++k) { lmin = fmin(lmin, U[v * P2 + k]); lmax = fmax(lmax, U[v * P2 + k]); }
           argmax = 1.0e-1;
         } else {
-          // get_min_max step 2 (Euler/limiter.f90:147-167): 3x3 Voronoi neighbourhood
-          const double* mmi = a.mm[par];
-          const long long base = in.cell_base;
-          lmin = mmi[(size_t)cell * 2 * V + v];
-          lmax = mmi[(size_t)cell * 2 * V + V + v];
-          if constexpr (kFast) {
-            // integer-key min/max (the integer pipe, not FP64)
-            long long kmn = okey(lmin), kmx = okey(lmax);
-            for (int jj = -1; jj <= 1; ++jj)
-              for (int ii = -1; ii <= 1; ++ii) {
-                const int in_ = nb_index(ci, ii, in.imax, in.bc[0], in.bc[1]);
-                const int jn_ = nb_index(cj, jj, in.jmax, in.bc[2], in.bc[3]);
-                const long long nc = base + in_ + (long long)in.imax * jn_;
-                kmn = min(kmn, okey(mmi[(size_t)nc * 2 * V + v]));
-                kmx = max(kmx, okey(mmi[(size_t)nc * 2 * V + V + v]));
-              }
-            lmin = okey_inv(kmn);
-            lmax = okey_inv(kmx);
-          } else {
-            for (int jj = -1; jj <= 1; ++jj)
-              for (int ii = -1; ii <= 1; ++ii) {
-                const int in_ = nb_index(ci, ii, in.imax, in.bc[0], in.bc[1]);
-                const int jn_ = nb_index(cj, jj, in.jmax, in.bc[2], in.bc[3]);
-                const long long nc = base + in_ + (long long)in.imax * jn_;
-                lmin = fmin(lmin, mmi[(size_t)nc * 2 * V + v]);
-                lmax = fmax(lmax, mmi[(size_t)nc * 2 * V + V + v]);
-              }
-          }
+          // get_min_max step 2: the neighbourhood bounds folded at the start
+          lmin = nlmin;
+          lmax = nlmax;
           argmax = 0.0;
           if (a.lminmax) {
             a.lminmax[(size_t)cell * 2 * V + v] = lmin;
