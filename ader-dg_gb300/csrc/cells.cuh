@@ -204,15 +204,17 @@ __device__ __forceinline__ double cfl_denom(const InstDesc& in, const double* Q)
   }
 }
 // FP32-mixed: eigenvalues and the node's denominator in FP32 (the maximum
-// over nodes, and dt, in FP64)
+// over nodes, and dt, in FP64); states whose FP32 pressure is not settled
+// take the FP64 evaluation on Qd
 template <class Sys, int N>
-__device__ __forceinline__ double cfl_denom_f32(const InstDesc& in, const typename Sys::FConst& fc, const float* q) {
+__device__ __forceinline__ double cfl_denom_f32(const InstDesc& in, const typename Sys::FConst& fc, const float* q,
+                                                const double* Qd) {
   if constexpr (Sys::ID == kSysAD) {
     return cfl_denom<Sys, N>(in, nullptr);
   } else {
     float ex, ey;
-    Sys::max_eig2_f32(fc, q, ex, ey);
-    return (double)(ex * in.idxf + ey * in.idyf);
+    if (Sys::max_eig2_f32(fc, q, ex, ey)) return (double)(ex * in.idxf + ey * in.idyf);
+    return cfl_denom<Sys, N>(in, Qd);
   }
 }
 
@@ -431,7 +433,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
   const bool want_cfl = mode != kCellInitDmp;
   if (act && want_cfl) {
     double dn;
-    if constexpr (kFast) dn = cfl_denom_f32<Sys, N>(in, typename Sys::FConst(in.ph), uf);
+    if constexpr (kFast) dn = cfl_denom_f32<Sys, N>(in, typename Sys::FConst(in.ph), uf, u);
     else dn = cfl_denom<Sys, N>(in, u);
     atomicMax(&cmax[lc], (unsigned long long)__double_as_longlong(dn));
   }
@@ -453,15 +455,15 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a,
         }
       }
       __syncthreads();
-      // FP32 projections of the deviations when their error bound stays a
-      // tenth of the DMP's absolute tolerance (1e-4) for every variable
-      // (smooth cells); otherwise this cell takes the FP64 projections.
+      // FP32 projections of the deviations when their error bound stays
+      // within the DMP's absolute tolerance (1e-4) for every variable;
+      // otherwise this cell takes the FP64 projections.
       float err[V];
       bool f32ok = true;
 #pragma unroll
       for (int v = 0; v < V; ++v) {
         err[v] = op.perr * __uint_as_float(amax[v]);
-        f32ok = f32ok && err[v] <= 1.0e-5f;
+        f32ok = f32ok && err[v] <= 1.0e-4f;
       }
       if (act && !from_lh) {
         if (f32ok) Proj<N, V, float>::template ypass<true>(Uf, LYf, LBf, opsf, opsf + S * P, node, P2);

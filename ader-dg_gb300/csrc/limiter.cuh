@@ -136,8 +136,9 @@ __device__ __forceinline__ void warp_minmax_store(R* mn, R* mx, R* red, int t) {
 
 // T = double: the reference's FP64 arithmetic in its order (bit for bit).
 // T = float: the FP32-mixed mode; the subcell re-solve, the DMP projections
-// of the new polynomial (while their error bound allows) and its CFL
-// eigenvalues in FP32; the state, Lh and min/max in FP64.
+// of the new polynomial (while their error bound allows) and the CFL
+// eigenvalues (where the FP32 pressure is settled) in FP32; the state, Lh
+// and min/max in FP64.
 template <class Sys, int N, class T>
 __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS) k_subcell(BatchArgs a, DevOps<N, double> op, FaceConst fc) {
   using C = SubCfg<Sys, N, T>;
@@ -431,7 +432,7 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS) k_subcell(BatchArg
       __syncthreads();
     }
     // ---- DMP of the new polynomial (recompute = 2) and the next min/max.
-    // FP32-mixed: FP32 projections when their error bound stays a tenth of the
+    // FP32-mixed: FP32 projections when their error bound stays within the
     // DMP's absolute tolerance, else FP64 (as in the cell kernel).
     float err[V];
     bool f32 = false;
@@ -440,7 +441,7 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS) k_subcell(BatchArg
 #pragma unroll
       for (int v = 0; v < V; ++v) {
         err[v] = op.perr * __uint_as_float(amax[v]);
-        f32 = f32 && err[v] <= 1.0e-5f;
+        f32 = f32 && err[v] <= 1.0e-4f;
       }
     }
     if constexpr (sizeof(T) == 4) {
@@ -465,25 +466,28 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS) k_subcell(BatchArg
                                                           ubf, ph, t, NT, fmn, fmx, posfail);
       }
       warp_minmax_store<float, V, NW>(fmn, fmx, redf, t);
-      // CFL denominator of the new polynomial (FP32 eigenvalues)
-      for (int p = t; p < P2; p += NT) {
-        float q[V];
-#pragma unroll
-        for (int v = 0; v < V; ++v) q[v] = (float)UN[v * P2 + p];
-        atomicMax(cmaxp, (unsigned long long)__double_as_longlong(cfl_denom_f32<Sys, N>(in, typename Sys::FConst(ph), q)));
-      }
     } else {
 #pragma unroll
       for (int v = 0; v < V; ++v) { mn[v] = kInf; mx[v] = -kInf; }
       Proj<N, V, double>::template xpass_minmax<Sys>(UN, LY, LB, opsm, opsm + S * P, ph, t, NT, mn, mx, posfail);
       warp_minmax_store<double, V, NW>(mn, mx, red, t);
-      // CFL denominator of the new polynomial
-      for (int p = t; p < P2; p += NT) {
-        double Q[V];
+    }
+    // CFL denominator of the new polynomial (FP32-mixed: FP32 eigenvalues
+    // where the FP32 pressure is settled, FP64 otherwise)
+    for (int p = t; p < P2; p += NT) {
+      double Q[V];
 #pragma unroll
-        for (int v = 0; v < V; ++v) Q[v] = UN[v * P2 + p];
-        atomicMax(cmaxp, (unsigned long long)__double_as_longlong(cfl_denom<Sys, N>(in, Q)));
+      for (int v = 0; v < V; ++v) Q[v] = UN[v * P2 + p];
+      double dn;
+      if constexpr (sizeof(T) == 4) {
+        float q[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) q[v] = (float)Q[v];
+        dn = cfl_denom_f32<Sys, N>(in, typename Sys::FConst(ph), q, Q);
+      } else {
+        dn = cfl_denom<Sys, N>(in, Q);
       }
+      atomicMax(cmaxp, (unsigned long long)__double_as_longlong(dn));
     }
     if (posfail) atomicOr(&flag[0], 1);
     __syncthreads();

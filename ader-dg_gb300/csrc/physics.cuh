@@ -86,12 +86,17 @@ struct EulerSys {
     __device__ explicit FConst(const Phys& ph) : gm1((float)(ph.gamma - 1.0)), gamma((float)ph.gamma) {}
   };
   // FP32 eigenvalues for the mixed-precision CFL
-  __device__ static void max_eig2_f32(const FConst& fc, const float* q, float& ex, float& ey) {
+  // False when the FP32 pressure is not settled (within 1e-4 of the energy
+  // terms it cancels, or not positive): the caller evaluates in FP64.
+  __device__ static bool max_eig2_f32(const FConst& fc, const float* q, float& ex, float& ey) {
     const float iq = 1.0f / q[0];
-    const float p = fc.gm1 * (q[3] - 0.5f * (q[1] * q[1] + q[2] * q[2]) * iq);
+    const float ke = 0.5f * (q[1] * q[1] + q[2] * q[2]) * iq;
+    const float p = fc.gm1 * (q[3] - ke);
+    if (!(p > 1.0e-4f * fc.gm1 * (fabsf(q[3]) + ke)) || !(q[0] > 0.0f)) return false;
     const float c = sqrtf(fc.gamma * p * iq);
     ex = fabsf(q[1] * iq) + c;
     ey = fabsf(q[2] * iq) + c;
+    return ex < 1.0e30f && ey < 1.0e30f;
   }
   // True when every state within e (componentwise) of the FP32 state q passes
   // positive()'s test, with a margin for this evaluation's own rounding.  False
@@ -249,16 +254,26 @@ struct BNSys {
         : gs((float)ph.gs), gg((float)ph.gg), gs1((float)(ph.gs - 1.0)), gg1((float)(ph.gg - 1.0)),
           gsps((float)(ph.gs * ph.ps)), ggpg((float)(ph.gg * ph.pg)), ps((float)ph.ps), pg((float)ph.pg) {}
   };
-  __device__ static void max_eig2_f32(const FConst& fc, const float* q, float& ex, float& ey) {
+  // False when an FP32 pressure p + pi is not settled (within 1e-4 of the
+  // terms it cancels, or not positive) or a fraction is out of (0.01, 0.99):
+  // the caller evaluates in FP64.
+  __device__ static bool max_eig2_f32(const FConst& fc, const float* q, float& ex, float& ey) {
     const float a = q[8], b = 1.0f - q[8];
+    if (!(a > 0.01f) || !(b > 0.01f) || !(q[0] > 0.0f) || !(q[4] > 0.0f)) return false;
     const float irs = 1.0f / q[0], irg = 1.0f / q[4];
     const float us = q[1] * irs, vs = q[2] * irs, ug = q[5] * irg, vg = q[6] * irg;
     const float rs = q[0] / a, rg = q[4] / b;
-    const float ps = fc.gs1 * (q[3] / a - 0.5f * rs * (us * us + vs * vs)) - fc.gsps;
-    const float pg = fc.gg1 * (q[7] / b - 0.5f * rg * (ug * ug + vg * vg)) - fc.ggpg;
-    const float as = sqrtf(fc.gs * (ps + fc.ps) / rs), ag = sqrtf(fc.gg * (pg + fc.pg) / rg);
+    const float es = q[3] / a, kes = 0.5f * rs * (us * us + vs * vs);
+    const float eg = q[7] / b, keg = 0.5f * rg * (ug * ug + vg * vg);
+    const float pps = fc.gs1 * (es - kes) - fc.gsps + fc.ps;  // p_s + pi_s
+    const float ppg = fc.gg1 * (eg - keg) - fc.ggpg + fc.pg;  // p_g + pi_g
+    if (!(pps > 1.0e-4f * (fc.gs1 * (fabsf(es) + kes) + fabsf(fc.gsps) + fabsf(fc.ps))) ||
+        !(ppg > 1.0e-4f * (fc.gg1 * (fabsf(eg) + keg) + fabsf(fc.ggpg) + fabsf(fc.pg))))
+      return false;
+    const float as = sqrtf(fc.gs * pps / rs), ag = sqrtf(fc.gg * ppg / rg);
     ex = fmaxf(fabsf(ug) + ag, fabsf(us) + as);
     ey = fmaxf(fabsf(vg) + ag, fabsf(vs) + as);
+    return ex < 1.0e30f && ey < 1.0e30f;
   }
   // True when every state within e (componentwise) of the FP32 state q passes
   // positive()'s test (rho_s, rho_g, p_s + pi_s, p_g + pi_g above 1e-12 and
