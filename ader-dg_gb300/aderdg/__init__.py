@@ -14,3 +14,4 @@ from .core import (OP_DUDX, OP_F0, OP_FL, OP_FR, OP_IK1, OP_KXI, OP_LIM2UH, OP_U
                    OP_XI, OP_XILIMBARY)
 from . import workloads  # noqa: F401,E402
 from . import serving  # noqa: F401,E402
+from . import output  # noqa: F401,E402

@@ -54,6 +54,7 @@ def _jobs():
         jobs.append(([nv] + _common_flags() + ["-c", os.path.join(CSRC, src)], src.replace(".cu", ".o")))
     jobs.append(([nv] + _common_flags() + ["--fmad=false", "-c", os.path.join(CSRC, "noalloc.cu")], "noalloc.o"))
     jobs.append(([nv] + _common_flags() + ["--fmad=false", "-c", os.path.join(CSRC, "initial.cu")], "initial.o"))
+    jobs.append(([nv] + _common_flags() + ["--fmad=false", "-c", os.path.join(CSRC, "output.cu")], "output.o"))
     jobs.append((["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I" + INCLUDE, "-c",
                   os.path.join(CSRC, "setup.cpp")], "setup.o"))
     return jobs

@@ -162,6 +162,8 @@ def load(build_if_missing=False):
         "aderdg_batch_run_timed": (i, [ctypes.POINTER(vp), i, i, dp]),
         "aderdg_initial_condition": (i, [vp, i, dp, ip]),
         "aderdg_batch_admit_ic": (i, [vp, cfgp, i, dp, d, ctypes.c_long, ip]),
+        "aderdg_cell_averages": (i, [vp, i, dp]), "aderdg_batch_cell_averages": (i, [vp, i, i, dp]),
+        "aderdg_error_norms": (i, [vp, i, dp, i, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -181,7 +183,8 @@ EXPORTED = ("aderdg_create", "aderdg_destroy", "aderdg_upload", "aderdg_init_lim
             "aderdg_batch_unit_bytes", "aderdg_batch_create", "aderdg_batch_destroy", "aderdg_batch_admit",
             "aderdg_batch_release", "aderdg_batch_launch", "aderdg_batch_sync", "aderdg_batch_query",
             "aderdg_batch_download", "aderdg_batch_info", "aderdg_batch_last_error", "aderdg_batch_profile",
-            "aderdg_batch_run_timed", "aderdg_initial_condition", "aderdg_batch_admit_ic")
+            "aderdg_batch_run_timed", "aderdg_initial_condition", "aderdg_batch_admit_ic",
+            "aderdg_cell_averages", "aderdg_batch_cell_averages", "aderdg_error_norms")
 
 
 def _dp(a):
@@ -285,6 +288,22 @@ class Solver:
         n = ctypes.c_int(0)
         self._ck(self.L.aderdg_initial_condition(self.h, ic, _dp(p), ctypes.byref(n)))
         return n.value
+
+    def cell_averages(self, primitive=True):
+        """Cell averages [cell][nVar] of uh (primitive variables by default),
+        the field the reference writes to its VTK files."""
+        out = np.empty(self.cfg.cells * self.cfg.nvar, dtype=np.float64)
+        self._ck(self.L.aderdg_cell_averages(self.h, 1 if primitive else 0, _dp(out)))
+        return out.reshape(self.cfg.cells, self.cfg.nvar)
+
+    def error_norms(self, ic, params=(), var=0):
+        """(mean |e|, rms e, max |e|) of the cell averages of variable `var`
+        against the exact field at the current time."""
+        p = np.zeros(32, dtype=np.float64)
+        p[: len(params)] = params
+        out = np.zeros(3, dtype=np.float64)
+        self._ck(self.L.aderdg_error_norms(self.h, ic, _dp(p), var, _dp(out)))
+        return tuple(out)
 
     def upload_limiter(self, status, lh):
         st = np.ascontiguousarray(status, dtype=np.int32).ravel()
@@ -485,6 +504,12 @@ class Batch:
         uh = np.empty(cfg.dofs, dtype=np.float64)
         self._ck(self.L.aderdg_batch_download(self.h, slot, _dp(uh)))
         return uh
+
+    def cell_averages(self, slot, primitive=True):
+        cfg = self.cfgs[slot]
+        out = np.empty(cfg.cells * cfg.nvar, dtype=np.float64)
+        self._ck(self.L.aderdg_batch_cell_averages(self.h, slot, 1 if primitive else 0, _dp(out)))
+        return out.reshape(cfg.cells, cfg.nvar)
 
     def profile(self):
         """Device milliseconds of each launch of one eager step of the batch."""

@@ -450,6 +450,47 @@ int aderdg_initial_condition(aderdg_ctx* c, int ic, const double* params, int* n
   return r;
 }
 
+int aderdg_cell_averages(aderdg_ctx* c, int primitive, double* out) {
+  if (!c || !out) return fail(c, ADERDG_EINVAL, "null argument");
+  if (!c->uploaded) return fail(c, ADERDG_ESTATE, "no state yet");
+  const int par = cur_par(c) ^ (c->pending ? 1 : 0);
+  const size_t n = (size_t)c->ncells * c->V;
+  double* tmp = nullptr;
+  CK(c, cudaMallocAsync(&tmp, n * sizeof(double), c->stream));
+  std::string why;
+  cudaError_t e = aderdg::launch_cell_averages(c->cfg, c->args.uh[par], primitive, tmp, c->stream, &why);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, tmp, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  cudaFreeAsync(tmp, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return fail_cuda(c, ("cell averages: " + why).c_str(), e);
+  return ADERDG_OK;
+}
+
+int aderdg_error_norms(aderdg_ctx* c, int ic, const double* params, int var, double* norms) {
+  if (!c || !norms) return fail(c, ADERDG_EINVAL, "null argument");
+  if (!c->uploaded) return fail(c, ADERDG_ESTATE, "no state yet");
+  int r = pull_state(c);
+  if (r) return r;
+  const int par = cur_par(c) ^ (c->pending ? 1 : 0);
+  double* sums = nullptr;
+  CK(c, cudaMallocAsync(&sums, 3 * sizeof(double), c->stream));
+  CK(c, cudaMemsetAsync(sums, 0, 3 * sizeof(double), c->stream));
+  std::string why;
+  cudaError_t e = aderdg::launch_error_norms(c->cfg, c->args.uh[par], ic, params, var, c->h_st->time, sums,
+                                             reinterpret_cast<unsigned long long*>(sums + 2), c->stream, &why);
+  double h[3] = {0, 0, 0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+  cudaFreeAsync(sums, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e == cudaErrorInvalidValue && !why.empty()) return fail(c, ADERDG_EINVAL, why);
+  if (e != cudaSuccess) return fail_cuda(c, "error norms", e);
+  const double ncells = (double)c->ncells;
+  norms[0] = h[0] / ncells;             // mean |e| (L1 per cell)
+  norms[1] = std::sqrt(h[1] / ncells);  // root mean square
+  norms[2] = h[2];                      // max |e| (analyze_soln)
+  return ADERDG_OK;
+}
+
 int aderdg_upload_limiter(aderdg_ctx* c, const int* status, const double* lh) {
   if (!c || !status || !lh) return fail(c, ADERDG_EINVAL, "null argument");
   if (!c->limiter) return ADERDG_OK;

@@ -54,6 +54,7 @@ struct aderdg_batch {
   std::vector<InstDesc> h_inst;       // table order: used entries sorted by base, then unused
   std::vector<int> slot_at;           // table position -> slot id
   std::vector<int> pos_of;            // slot id -> table position (-1: free)
+  std::vector<aderdg_config> cfg_of;  // slot id -> its configuration
   std::vector<std::pair<long long, long long>> free_ranges;  // (base, size), sorted
   long long hw = 0;                   // end of the highest occupied unit
   BatchArgs args{};
@@ -298,6 +299,7 @@ int aderdg_batch_create(int system, int N, int precision, int limiter, long capa
   }
   b->slot_at.assign(max_instances, -1);
   b->pos_of.assign(max_instances, -1);
+  b->cfg_of.assign(max_instances, aderdg_config{});
   b->free_ranges.push_back({0, capacity_units});
   b->ops64.assign(kt->ops64_size, 0);
   kt->make_ops64(b->ops, b->ops64.data());
@@ -372,6 +374,7 @@ int badmit(aderdg_batch* b, const aderdg_config* cfg, const double* uh, const do
   while (b->pos_of[s] >= 0) ++s;
   b->slot_at[pos] = s;
   b->pos_of[s] = pos;
+  b->cfg_of[s] = *cfg;
   ++b->n_used;
   InstDesc& in = b->h_inst[pos];
   in = aderdg::make_inst_desc(cfg);
@@ -554,6 +557,27 @@ int aderdg_batch_download(aderdg_batch* b, int slot, double* uh) {
   BK(b, cudaMemcpyAsync(uh, b->args.uh[par] + (size_t)in.cell_base * P2V, cells * P2V * sizeof(double),
                         cudaMemcpyDeviceToHost, b->stream));
   BK(b, cudaStreamSynchronize(b->stream));
+  return ADERDG_OK;
+}
+
+int aderdg_batch_cell_averages(aderdg_batch* b, int slot, int primitive, double* out) {
+  if (!b || !out || slot < 0 || slot >= b->max_inst || b->pos_of[slot] < 0) return bfail(b, ADERDG_EINVAL, "bad slot");
+  int r = pull_states(b);
+  if (r) return r;
+  const int pos = b->pos_of[slot];
+  const InstDesc& in = b->h_inst[pos];
+  const int par = (int)(b->h_st[pos].steps & 1);
+  const size_t cells = (size_t)in.imax * in.jmax, P2V = (size_t)b->P * b->P * b->V;
+  double* tmp = nullptr;
+  BK(b, cudaMallocAsync(&tmp, cells * b->V * sizeof(double), b->stream));
+  std::string why;
+  cudaError_t e = aderdg::launch_cell_averages(b->cfg_of[slot], b->args.uh[par] + (size_t)in.cell_base * P2V,
+                                               primitive, tmp, b->stream, &why);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out, tmp, cells * b->V * sizeof(double), cudaMemcpyDeviceToHost, b->stream);
+  cudaFreeAsync(tmp, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) return bcuda(b, ("cell averages: " + why).c_str(), e);
   return ADERDG_OK;
 }
 

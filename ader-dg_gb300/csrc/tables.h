@@ -40,6 +40,15 @@ struct KernelTable {
 cudaError_t launch_initial_field(const aderdg_config& cfg, int ic, const double* params, double* uh, double* lh,
                                  cudaStream_t s, std::string* why);
 
+// Cell averages (or their primitive variables) of uh, [cell][V] (output.cu).
+cudaError_t launch_cell_averages(const aderdg_config& cfg, const double* uh, int primitive, double* out,
+                                 cudaStream_t s, std::string* why);
+// Error of the cell averages of variable var against an exact field at time
+// `time`: sums_dev[0] += sum |e|, sums_dev[1] += sum e^2, *max_dev = max |e| bits.
+cudaError_t launch_error_norms(const aderdg_config& cfg, const double* uh, int ic, const double* params, int var,
+                               double time, double* sums_dev, unsigned long long* max_dev, cudaStream_t s,
+                               std::string* why);
+
 // Returns the table for (sys, N) or nullptr when that pair was not built.
 const KernelTable* kernel_table(int sys, int N);
 

@@ -27,6 +27,7 @@
 #include <cstring>
 #include <fstream>
 #include <sstream>
+#include <cmath>
 #include <string>
 #include <vector>
 
@@ -151,6 +152,94 @@ bool read_params(const char* sys, const char* path, Params& p, std::string& err)
   return true;
 }
 
+// Fortran Ew.d edit descriptor: 0.ddd...E+xx right-aligned in w columns
+std::string fortran_e(double x, int w, int d) {
+  char buf[64];
+  if (!std::isfinite(x)) {
+    std::snprintf(buf, sizeof(buf), "%*s", w, x != x ? "NaN" : (x > 0 ? "Infinity" : "-Infinity"));
+    return buf;
+  }
+  std::string s;
+  if (x == 0.0) {
+    s = "0." + std::string(d, '0') + "E+00";
+  } else {
+    std::snprintf(buf, sizeof(buf), "%.*E", d - 1, std::fabs(x));  // correctly rounded d significant digits
+    std::string m(buf);
+    const size_t epos = m.find('E');
+    std::string digits = m.substr(0, 1) + (epos > 2 ? m.substr(2, epos - 2) : std::string());
+    const int e = std::atoi(m.c_str() + epos + 1) + 1;
+    std::snprintf(buf, sizeof(buf), "%s0.%sE%c%02d", x < 0 ? "-" : "", digits.c_str(), e < 0 ? '-' : '+', std::abs(e));
+    s = buf;
+  }
+  if ((int)s.size() < w) s = std::string(w - s.size(), ' ') + s;
+  return s;
+}
+
+// write_data (Euler/write_data.f90:8-95 and the BN / AD copies): cell-average
+// primitive variables on the cell centres, legacy ASCII VTK
+bool write_vtk(const std::string& path, const aderdg_config& c, const std::vector<double>& wh, double time) {
+  FILE* f = std::fopen(path.c_str(), "w");
+  if (!f) return false;
+  const int I = c.imax, J = c.jmax;
+  const int V = c.system == ADERDG_SYS_ADVDIFF ? 1 : c.system == ADERDG_SYS_EULER ? 4 : 9;
+  const double dx = (c.xr[0] - c.xl[0]) / I, dy = (c.xr[1] - c.xl[1]) / J;
+  std::fprintf(f, "# vtk DataFile Version 2.0\n2D Euler\nASCII\nDATASET STRUCTURED_GRID\nFIELD FieldData 1\n");
+  std::fprintf(f, "TIME 1 1 double\n%s\n", fortran_e(time, 15, 9).c_str());
+  std::fprintf(f, "DIMENSIONS %5d%5d%5d\nPOINTS %10d double\n", I, J, 1, I * J);
+  for (int j = 0; j < J; ++j)
+    for (int i = 0; i < I; ++i)
+      std::fprintf(f, "%s%s%s\n", fortran_e(c.xl[0] + ((double)(i + 1) - 0.5) * dx, 15, 7).c_str(),
+                   fortran_e(c.xl[1] + ((double)(j + 1) - 0.5) * dy, 15, 7).c_str(), fortran_e(0.0, 15, 7).c_str());
+  std::fprintf(f, "POINT_DATA%10d\n", I * J);
+  struct Field { bool vec; const char* name; int a, b; };
+  static const Field euler[] = {{false, "Density", 0, 0}, {true, "Velocity", 1, 2}, {false, "Pressure", 3, 0}};
+  static const Field bn[] = {{false, "RHO_S", 0, 0}, {true, "V_S", 1, 2}, {false, "P_S", 3, 0}, {false, "RHO_G", 4, 0},
+                             {true, "V_G", 5, 6},     {false, "P_G", 7, 0}, {false, "PHI_S", 8, 0}};
+  static const Field ad[] = {{false, "U", 0, 0}};
+  const Field* fields = c.system == ADERDG_SYS_EULER ? euler : c.system == ADERDG_SYS_BN ? bn : ad;
+  const int nf = c.system == ADERDG_SYS_EULER ? 3 : c.system == ADERDG_SYS_BN ? 7 : 1;
+  for (int k = 0; k < nf; ++k) {
+    if (fields[k].vec) std::fprintf(f, "VECTORS %s double\n", fields[k].name);
+    else std::fprintf(f, "SCALARS %s double 1\nLOOKUP_TABLE default\n", fields[k].name);
+    for (long q = 0; q < (long)I * J; ++q) {
+      if (fields[k].vec)
+        std::fprintf(f, "%s%s%s\n", fortran_e(wh[q * V + fields[k].a], 15, 7).c_str(),
+                     fortran_e(wh[q * V + fields[k].b], 15, 7).c_str(), fortran_e(0.0, 15, 7).c_str());
+      else
+        std::fprintf(f, "%s\n", fortran_e(wh[q * V + fields[k].a], 15, 7).c_str());
+    }
+  }
+  std::fclose(f);
+  return true;
+}
+
+// plot_troubled_cells (Euler/write_data.f90:101-192): the recompute map on the mesh
+bool write_troubled_vtk(const std::string& path, const aderdg_config& c, const std::vector<int>& rec, double time) {
+  FILE* f = std::fopen(path.c_str(), "w");
+  if (!f) return false;
+  const int I = c.imax, J = c.jmax;
+  const long nn = (long)(I + 1) * (J + 1), ne = (long)I * J;
+  const double dx = (c.xr[0] - c.xl[0]) / I, dy = (c.xr[1] - c.xl[1]) / J;
+  std::fprintf(f, "# vtk DataFile Version 2.0\n2D Euler\nASCII\nDATASET UNSTRUCTURED_GRID\nFIELD FieldData 1\n");
+  std::fprintf(f, "TIME 1 1 double\n%s\nPOINTS %10ld double\n", fortran_e(time, 15, 9).c_str(), nn);
+  for (int j = 0; j <= J; ++j)
+    for (int i = 0; i <= I; ++i)
+      std::fprintf(f, "%s%s%s\n", fortran_e(c.xl[0] + i * dx, 15, 7).c_str(), fortran_e(c.xl[1] + j * dy, 15, 7).c_str(),
+                   fortran_e(0.0, 15, 7).c_str());
+  std::fprintf(f, "CELLS %10ld%10ld\n", ne, ne * 5);
+  auto idxn = [&](int i, int j) { return (long)i + (long)(I + 1) * j; };
+  for (int j = 0; j < J; ++j)
+    for (int i = 0; i < I; ++i)
+      std::fprintf(f, "%10d%10ld%10ld%10ld%10ld\n", 4, idxn(i, j), idxn(i + 1, j), idxn(i + 1, j + 1), idxn(i, j + 1));
+  std::fprintf(f, "CELL_TYPES %10ld\n", ne);
+  for (long q = 0; q < ne; ++q) std::fprintf(f, "%5d\n", 9);
+  std::fprintf(f, "CELL_DATA%10ld\nSCALARS TCells double 1\nLOOKUP_TABLE default\n", ne);
+  for (long q = 0; q < ne; ++q)
+    std::fprintf(f, "%s\n", fortran_e(rec[q] == 1 ? 2.0 : rec[q] == 2 ? 1.0 : 0.0, 15, 7).c_str());
+  std::fclose(f);
+  return true;
+}
+
 int die(aderdg_ctx* ctx, int code, const char* what) {
   std::fprintf(stderr, "%s failed (%d): %s\n", what, code, aderdg_last_error(ctx));
   return 1;
@@ -160,7 +249,10 @@ int die(aderdg_ctx* ctx, int code, const char* what) {
 
 int main(int argc, char** argv) {
   if (argc < 3) {
-    std::fprintf(stderr, "usage: %s euler|bn|ad params.ini [--phases] [--N n] [--max-steps k] [--quiet]\n", argv[0]);
+    std::fprintf(stderr,
+                 "usage: %s euler|bn|ad params.ini [--phases] [--N n] [--max-steps k] [--quiet] [--dump file]\n"
+                 "       [--vtk basename] [--analyze]\n",
+                 argv[0]);
     return 2;
   }
   Params p;
@@ -172,12 +264,16 @@ int main(int argc, char** argv) {
   bool phases = false, quiet = false;
   long max_steps = -1;
   const char* dump = nullptr;
+  const char* vtk = nullptr;  // write_data every WriteInterval steps: <basename>-<timestep>.vtk
+  bool analyze = false;       // analyze_soln at the end
   for (int a = 3; a < argc; ++a) {
     if (!std::strcmp(argv[a], "--phases")) phases = true;
     else if (!std::strcmp(argv[a], "--quiet")) quiet = true;
     else if (!std::strcmp(argv[a], "--N") && a + 1 < argc) p.cfg.N = std::atoi(argv[++a]);
     else if (!std::strcmp(argv[a], "--max-steps") && a + 1 < argc) max_steps = std::atol(argv[++a]);
     else if (!std::strcmp(argv[a], "--dump") && a + 1 < argc) dump = argv[++a];
+    else if (!std::strcmp(argv[a], "--vtk") && a + 1 < argc) vtk = argv[++a];
+    else if (!std::strcmp(argv[a], "--analyze")) analyze = true;
   }
   const aderdg_config& c = p.cfg;
   const int V = c.system == ADERDG_SYS_ADVDIFF ? 1 : c.system == ADERDG_SYS_EULER ? 4 : 9;
@@ -197,7 +293,30 @@ int main(int argc, char** argv) {
   int nrec = 0;
   long steps = 0;
   const auto t0 = std::chrono::steady_clock::now();
+  std::vector<double> wh(vtk ? (size_t)V * cells : 0);
+  auto write_out = [&](long timestep) -> int {
+    if (!vtk) return 0;
+    int rr = aderdg_cell_averages(ctx, 1, wh.data());
+    if (rr) return rr;
+    char name[64];
+    std::snprintf(name, sizeof(name), "-%08ld.vtk", timestep);
+    if (!write_vtk(std::string(vtk) + name, c, wh, time)) return ADERDG_EINVAL;
+    if (c.limiter && c.system != ADERDG_SYS_ADVDIFF) {
+      std::vector<int> rec((size_t)cells);
+      rr = aderdg_get_array(ctx, ADERDG_A_RECOMPUTE, rec.data());
+      if (rr) return rr;
+      const std::string base(vtk);
+      const size_t slash = base.find_last_of('/');
+      const std::string dir = slash == std::string::npos ? std::string() : base.substr(0, slash + 1);
+      std::snprintf(name, sizeof(name), "Tcells-%08ld.vtk", timestep);
+      if (!write_troubled_vtk(dir + name, c, rec, time)) return ADERDG_EINVAL;
+    }
+    return 0;
+  };
   while (time < p.tend && (max_steps < 0 || steps < max_steps)) {
+    // Euler/main.f90:25-28: write_data every WriteInterval steps
+    if (vtk && p.write_interval > 0 && steps % p.write_interval == 0)
+      if ((r = write_out(steps))) return die(ctx, r, "write_data");
     if (phases) {
       // the loop body of Euler/main.f90:24-100, one call per phase
       if ((r = aderdg_calc_time_step(ctx, time, p.tend, &dt))) return die(ctx, r, "calc_time_step");
@@ -221,6 +340,13 @@ int main(int argc, char** argv) {
   std::printf(" nRecomp = %d t = %.15g dt = %.15g\n", nrec, time, dt);
   std::printf(" steps = %ld  initially limited = %d  wall time = %.6f s  DOF-updates/s = %.4e\n", steps, nlim, secs,
               (double)V * P * P * cells * steps / (secs > 0 ? secs : 1));
+  if (vtk && (r = write_out(steps))) return die(ctx, r, "write_data");
+  if (analyze) {
+    // analyze_soln (Euler/analyze_soln.f90:10-56): max over cells of the cell-average error of variable 1
+    double norms[3];
+    if ((r = aderdg_error_norms(ctx, p.ic, icp.data(), 0, norms))) return die(ctx, r, "aderdg_error_norms");
+    std::printf(" %.15g\n", norms[2]);
+  }
   if ((r = aderdg_download(ctx, uh.data(), nullptr))) return die(ctx, r, "aderdg_download");
   if (dump) {
     FILE* f = std::fopen(dump, "wb");

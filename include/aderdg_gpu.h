@@ -253,6 +253,21 @@ int aderdg_batch_profile(aderdg_batch* b, double* phase_ms);
 int aderdg_batch_run_timed(aderdg_batch* const* batches, int n, int steps, double* ms);
 const char* aderdg_batch_last_error(aderdg_batch* b);
 
+/* ---- output and error analysis (not on the hot path) ---- */
+/* Cell averages of uh, out[(i + IMAX*j)*nVar + v] (the reference's wh(nVar,IMAX,JMAX));
+ * primitive != 0: converted with PDECons2Prim, i.e. exactly the field
+ * write_data writes (Euler/write_data.f90:17-33). */
+int aderdg_cell_averages(aderdg_ctx* ctx, int primitive, double* out);
+int aderdg_batch_cell_averages(aderdg_batch* b, int slot, int primitive, double* out);
+/* Error of the cell averages of variable `var` against an exact field at the
+ * context's current time: norms = {mean |e|, root mean square of e, max |e|}.
+ * max |e| at time 0 against the initial field is analyze_soln's number
+ * (Euler/analyze_soln.f90:10-56); the isentropic vortex (translated with its
+ * free stream) and the sine wave (translated with (cx, cy), damped by
+ * exp(-8 pi^2 a t)) are compared with their exact solutions at that time,
+ * other fields with the initial field. */
+int aderdg_error_norms(aderdg_ctx* ctx, int ic, const double* params, int var, double* norms);
+
 /* ---- host setup helpers (initial fields; not on the hot path) ---- */
 enum aderdg_ic {
   ADERDG_IC_AD_ZERO = 0,      /* Advection-Diffusion/initialize.f90:148-164 */
