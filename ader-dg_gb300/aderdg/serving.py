@@ -178,3 +178,38 @@ class Server:
             b.close()
         self.groups.clear()
         self.pool.shutdown(wait=False)
+
+
+def main(argv=None):
+    """Serve the seeded request mix at one or more Poisson arrival rates and
+    print one JSON line per rate: throughput and time-to-solution percentiles.
+
+        python -m aderdg.serving --requests 1024 --steps 50 --rates 10,30,100,300,500
+    """
+    import argparse
+    import json
+
+    from .core import FP32_MIXED, FP64
+
+    ap = argparse.ArgumentParser(prog="python -m aderdg.serving")
+    ap.add_argument("--requests", type=int, default=256)
+    ap.add_argument("--seed", type=int, default=0, help="request_mix seed")
+    ap.add_argument("--rates", default="100", help="comma-separated arrival rates, requests/s")
+    ap.add_argument("--steps", type=int, default=50, help="steps per request (0: to its end time)")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--budget-gb", type=float, default=160.0, help="HBM budget of the batches")
+    ap.add_argument("--host-setup", action="store_true", help="project initial fields on the host")
+    args = ap.parse_args(argv)
+    prec = FP32_MIXED if args.precision == "fp32" else FP64
+    specs = workloads.request_mix(max(args.requests, 1024), seed=args.seed)[:args.requests]
+    for rate in [float(x) for x in args.rates.split(",")]:
+        srv = Server(hbm_budget_bytes=args.budget_gb * 1e9, precision=prec, device_setup=not args.host_setup)
+        rep = srv.run(specs, rate=rate, seed=args.seed, max_steps=args.steps)
+        rep.pop("requests_done")
+        srv.close()
+        rep.update(rate=rate, seed=args.seed, steps=args.steps, precision=args.precision)
+        print(json.dumps(rep), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -101,15 +101,17 @@ struct EulerSys {
   // True when every state within e (componentwise) of the FP32 state q passes
   // positive()'s test, with a margin for this evaluation's own rounding.  False
   // means "not settled": the caller re-evaluates the state in FP64.
+  // With rho >= r_lo and kinetic energy <= K / r_lo (K from the largest
+  // momenta), p >= (gamma - 1) (E_lo - K / r_lo); the test is written times
+  // r_lo, without a division.
   __device__ static bool admissible_box_f32(const FConst& fc, const float* q, const float* e) {
     const float r_lo = q[0] - e[0];
     if (!(r_lo > 2.0e-12f) || !(fc.gm1 > 0.0f)) return false;
     const float m1 = fabsf(q[1]) + e[1], m2 = fabsf(q[2]) + e[2];
-    const float ke_hi = 0.5f * (m1 * m1 + m2 * m2) / r_lo;
-    const float x_lo = (q[3] - e[3]) - ke_hi;
-    const float margin = 1.0e-5f * (fabsf(q[3]) + e[3] + ke_hi);
-    const float p_lo = fc.gm1 * (x_lo - margin);
-    return p_lo > 2.0e-12f && margin < 1.0e30f;
+    const float K = 0.5f * (m1 * m1 + m2 * m2);
+    const float mag = (fabsf(q[3]) + e[3]) * r_lo + K;
+    const float lhs = fc.gm1 * (((q[3] - e[3]) * r_lo - K) - 1.0e-5f * mag);
+    return lhs > 2.0e-12f * r_lo && mag < 1.0e30f;
   }
   // Euler/pde.f90:29-40
   template <class T>

@@ -129,6 +129,78 @@ __device__ __forceinline__ void contract(const R* __restrict__ cs, int l, int i,
   }
 }
 
+// Volume integral (duh; kVolume) and face extrapolation (qbnd, fbnd /
+// gradQbnd) of one cell from the time averages in shared memory cs: Q [V][P2], FX [V][P2],
+// FY [V][P2] (AD: + GX, GY); Sh is the node's time-averaged -NCP (BN).  Called
+// by the P2 threads of the cell (node = 0..P2-1).
+template <class Sys, int N, class R, bool kVolume>
+__device__ __forceinline__ void predictor_outputs(const BatchArgs& a, const DevOps<N, R>& op, const InstDesc& in,
+                                                  const R* cs, long long cell, int node, int i, int j, const R* Sh) {
+  constexpr int P = N + 1, P2 = P * P, V = Sys::V;
+  const R* sQ = cs;
+  const R* sX = cs + V * P2;
+  const R* sY = cs + 2 * V * P2;
+  if constexpr (kVolume) {
+    // volume integral: duh = (w_j/dx) sum_k Kxi(i,k) Fhi_x(k,j) + (w_i/dy) sum_k Kxi(j,k) Fhi_y(i,k) [+ w_i w_j Shi]
+    // duh is stored in the compute precision R (FP32 in the mixed mode)
+    R vx, vy;
+    if constexpr (sizeof(R) == 4) {
+      vx = op.w[j] * R(in.idxf);
+      vy = op.w[i] * R(in.idyf);
+    } else {
+      vx = op.w[j] / R(in.dx);
+      vy = op.w[i] / R(in.dy);
+    }
+    R* dst = reinterpret_cast<R*>(a.duh) + ((size_t)cell * P2 + node) * V;
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      R sxv = R(0), syv = R(0);
+#pragma unroll
+      for (int k = 0; k < P; ++k) {
+        sxv = fma(op.Kxi[i + P * k], sX[v * P2 + k + P * j], sxv);
+        syv = fma(op.Kxi[j + P * k], sY[v * P2 + i + P * k], syv);
+      }
+      R d = sxv * vx + syv * vy;
+      if constexpr (Sys::ID == kSysBN) d = fma(op.w[i] * op.w[j], Sh[v], d);
+      dst[v] = d;
+    }
+  }
+  // face extrapolation: faces 0 left, 1 right (x), 2 bottom, 3 top (y); point l
+  R* qb = reinterpret_cast<R*>(a.qbnd);
+  R* fb = reinterpret_cast<R*>(a.fbnd);
+  for (int idx = node; idx < 4 * P; idx += P2) {
+    const int f = idx / P, l = idx - f * P;
+    const R* c = (f == 0 || f == 2) ? op.FL : op.FR;
+    const size_t o = ((size_t)cell * P + l) * 4 + f;
+    const bool xdir = f < 2;
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      R sq = R(0), sf = R(0);
+#pragma unroll
+      for (int m = 0; m < P; ++m) {
+        const int nd = xdir ? (m + P * l) : (l + P * m);
+        sq = fma(c[m], sQ[v * P2 + nd], sq);
+        if constexpr (Sys::ID != kSysAD) sf = fma(c[m], (xdir ? sX : sY)[v * P2 + nd], sf);
+      }
+      qb[o * V + v] = sq;
+      if constexpr (Sys::ID != kSysAD) fb[o * V + v] = sf;
+    }
+    if constexpr (Sys::ID == kSysAD) {
+      // gradQbnd(v,d,f,l)
+#pragma unroll
+      for (int d = 0; d < 2; ++d) {
+        R sg = R(0);
+#pragma unroll
+        for (int m = 0; m < P; ++m) {
+          const int nd = xdir ? (m + P * l) : (l + P * m);
+          sg = fma(c[m], cs[(3 + d) * P2 + nd], sg);
+        }
+        fb[o * 2 + d] = sg;
+      }
+    }
+  }
+}
+
 template <class Sys, int N, class R, bool kPhase>
 __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R>::MIN_BLOCKS)
     k_predictor(BatchArgs a, DevOps<N, R> op) {
@@ -421,65 +493,9 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
       a.fhi[(base * 2 + 1) * V + v] = (double)Fh[1][v];
       if constexpr (Sys::ID == kSysBN) a.shi[base * V + v] = (double)Sh[v];
     }
+    predictor_outputs<Sys, N, R, false>(a, op, in, cs, cell, node, i, j, Sh);
   } else {
-    // volume integral: duh = (w_j/dx) sum_k Kxi(i,k) Fhi_x(k,j) + (w_i/dy) sum_k Kxi(j,k) Fhi_y(i,k) [+ w_i w_j Shi]
-    // duh is stored in the compute precision R (FP32 in the mixed mode)
-    R vx, vy;
-    if constexpr (sizeof(R) == 4) {
-      vx = op.w[j] * R(in.idxf);
-      vy = op.w[i] * R(in.idyf);
-    } else {
-      vx = op.w[j] / R(in.dx);
-      vy = op.w[i] / R(in.dy);
-    }
-    R* dst = reinterpret_cast<R*>(a.duh) + ((size_t)cell * P2 + node) * V;
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-      R sxv = R(0), syv = R(0);
-#pragma unroll
-      for (int k = 0; k < P; ++k) {
-        sxv = fma(op.Kxi[i + P * k], sX[v * P2 + k + P * j], sxv);
-        syv = fma(op.Kxi[j + P * k], sY[v * P2 + i + P * k], syv);
-      }
-      R d = sxv * vx + syv * vy;
-      if constexpr (Sys::ID == kSysBN) d = fma(op.w[i] * op.w[j], Sh[v], d);
-      dst[v] = d;
-    }
-  }
-
-  // face extrapolation: faces 0 left, 1 right (x), 2 bottom, 3 top (y); point l
-  R* qb = reinterpret_cast<R*>(a.qbnd);
-  R* fb = reinterpret_cast<R*>(a.fbnd);
-  for (int idx = node; idx < 4 * P; idx += P2) {
-    const int f = idx / P, l = idx - f * P;
-    const R* c = (f == 0 || f == 2) ? op.FL : op.FR;
-    const size_t o = ((size_t)cell * P + l) * 4 + f;
-    const bool xdir = f < 2;
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-      R sq = R(0), sf = R(0);
-#pragma unroll
-      for (int m = 0; m < P; ++m) {
-        const int nd = xdir ? (m + P * l) : (l + P * m);
-        sq = fma(c[m], sQ[v * P2 + nd], sq);
-        if constexpr (Sys::ID != kSysAD) sf = fma(c[m], (xdir ? sX : sY)[v * P2 + nd], sf);
-      }
-      qb[o * V + v] = sq;
-      if constexpr (Sys::ID != kSysAD) fb[o * V + v] = sf;
-    }
-    if constexpr (Sys::ID == kSysAD) {
-      // gradQbnd(v,d,f,l)
-#pragma unroll
-      for (int d = 0; d < 2; ++d) {
-        R sg = R(0);
-#pragma unroll
-        for (int m = 0; m < P; ++m) {
-          const int nd = xdir ? (m + P * l) : (l + P * m);
-          sg = fma(c[m], cs[(3 + d) * P2 + nd], sg);
-        }
-        fb[o * 2 + d] = sg;
-      }
-    }
+    predictor_outputs<Sys, N, R, true>(a, op, in, cs, cell, node, i, j, Sh);
   }
 }
 

@@ -113,6 +113,30 @@ module aderdg_gpu
             real(c_double), intent(out) :: dt
             integer(c_int), intent(out) :: n_recompute
         end function
+        ! write_data's field: cell-average primitive variables wh(nVar,IMAX,JMAX)
+        integer(c_int) function aderdg_cell_averages(ctx, primitive, wh) bind(C, name="aderdg_cell_averages")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: primitive
+            real(c_double), intent(out) :: wh(*)
+        end function
+        ! analyze_soln: norms(3) = max over cells of the cell-average error of variable var+1
+        integer(c_int) function aderdg_error_norms(ctx, ic, params, var, norms) bind(C, name="aderdg_error_norms")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: ic, var
+            real(c_double), intent(in) :: params(32)
+            real(c_double), intent(out) :: norms(3)
+        end function
+        ! the initial field and the initial limiter evaluated on the device
+        integer(c_int) function aderdg_initial_condition(ctx, ic, params, n_limited) &
+                bind(C, name="aderdg_initial_condition")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: ic
+            real(c_double), intent(in) :: params(32)
+            integer(c_int), intent(out) :: n_limited
+        end function
         type(c_ptr) function aderdg_last_error(ctx) bind(C, name="aderdg_last_error")
             import :: c_ptr
             type(c_ptr), value :: ctx
