@@ -231,10 +231,17 @@ struct CellCfg {
   static constexpr int OPS_DBL = S * P + P * P;  // uh2lim, uh2lob (FP64, then FP32 in the mixed mode)
   static constexpr int SMEM_BYTES = CPB * CELL_DBL * 8 + OPS_DBL * 12 + CPB * 8 /*cell max*/ + CPB * 4 /*flags*/ +
                                     CPB * V * 4 /*|U| max*/ + 16;
+  // blocks per SM the register allocation aims at: Euler's FP32-mixed cell
+  // kernel is latency-bound and gains from a fourth block; the other
+  // variants keep the allocation they reach unconstrained
+  static constexpr int min_blocks(bool fast) {
+    return Sys::ID == kSysEuler ? (fast ? 4 : 3) : (Sys::ID == kSysBN ? 2 : 4);
+  }
 };
 
 template <class Sys, int N, bool kFast>
-__global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS) k_cells(BatchArgs a, DevOps<N, double> op) {
+__global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min_blocks(kFast))
+    k_cells(BatchArgs a, DevOps<N, double> op) {
   using C = CellCfg<Sys, N>;
   constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1, V = Sys::V, CPB = C::CPB;
   extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -139,14 +139,18 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- helpers
-def dist_init():
+def dist_init(backend="nccl"):
+    """Replicas: one process per GPU (torchrun), no data exchange; the
+    process group only carries the barrier and the max over ranks of the
+    timings."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws > 1:
         import torch
         import torch.distributed as dist
         lr = int(os.environ.get("LOCAL_RANK", "0"))
-        torch.cuda.set_device(lr)
-        dist.init_process_group("nccl")
+        if backend == "nccl":
+            torch.cuda.set_device(lr)
+        dist.init_process_group(backend)
         return dist, int(os.environ["RANK"]), ws, lr
     return None, 0, 1, 0
 
@@ -160,7 +164,8 @@ def allmax(dist, x):
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 

@@ -52,6 +52,25 @@ def test_step_parity_fp64(gpu_lib, name, N, side):
             assert (st != o.get_int(po.STATUS)).sum() <= 0 if step == 0 else True
 
 
+@pytest.mark.parametrize("ictype,N", [(3, 4), (1, 2), (2, 3), (7, 2)])
+def test_bn_shock_tubes_as_shipped(gpu_lib, ictype, N):
+    """Baer-Nunziato/baer_nunziato_params.ini (ICType 3, N=4; here 40x4) and
+    the other shock tubes of Baer-Nunziato/initialize.f90:302-407."""
+    cfg = aderdg.Config(system=aderdg.SYS_BN, N=N, imax=40, jmax=4, xl=(-0.5, -0.05), xr=(0.5, 0.05),
+                        bc=(1, 1, 1, 1))
+    o, g, uh, lh = setup_pair(cfg, aderdg.IC_BN_RP1D, (float(ictype), 0.0))
+    t_o = t_g = 0.0
+    for step in range(3):
+        t_o, dt_o, n_o = o.step(t_o, 0.1)
+        t_g, dt_g, n_g = g.step(t_g, 0.1)
+        if step == 0:
+            assert dt_g == dt_o and n_g == n_o
+            assert np.array_equal(g.get(aderdg.A_RECOMPUTE), o.get_int(po.RECOMPUTE))
+        ug, _ = g.download()
+        uo = o.get(po.UH)
+        assert rel_l1(ug, uo) <= TOL and rel_linf(ug, uo) <= TOL, (step, rel_l1(ug, uo), rel_linf(ug, uo))
+
+
 def test_dmr_as_shipped(gpu_lib):
     """Euler/params.ini as shipped: N=1 double Mach reflection (here 48x12)."""
     cfg = aderdg.Config(system=aderdg.SYS_EULER, N=1, imax=48, jmax=12, xr=(4.0, 1.0), bc=(1, 1, 1, 1), bc_mode=1)
