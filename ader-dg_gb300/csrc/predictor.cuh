@@ -33,9 +33,13 @@ struct PredCfg {
   static constexpr int P = N + 1, P2 = P * P, V = Sys::V;
   // variables of one node padded to whole 16-byte vectors (AD: scalar)
   static constexpr int VEC = 16 / (int)sizeof(R);
-  // FP32: pad to whole float4; FP64: double2 only when V is even (padding
-  // Baer-Nunziato's 9 doubles costs more registers than it saves loads)
-  static constexpr int VP = (V == 1) ? 1 : (sizeof(R) == 4 ? ((V + VEC - 1) / VEC) * VEC : V);
+  // flux components stored and contracted: Baer-Nunziato's volume fraction
+  // has no conservative flux (its ninth component is 0, Baer-Nunziato/pde.f90:74-119),
+  // so FP32 stores 8 (two float4) where that does not make the register
+  // allocation spill (N <= 3); elsewhere all 9 (measured)
+  static constexpr int VF = (Sys::ID == kSysBN && sizeof(R) == 4 && N <= 3) ? 8 : V;
+  // FP32: pad to whole float4; FP64: double2 when VF is even
+  static constexpr int VP = (VF == 1) ? 1 : (sizeof(R) == 4 ? ((VF + VEC - 1) / VEC) * VEC : VF);
   // shared-memory elements per cell: flux buffer [P][2][P2][VP] (+ BN volume
   // fraction [P][P2]; AD: flux [P][2][P2] + state [P][P2]), rounded to 16 bytes;
   // the epilogue reuses it as [V][P2] x 3 (AD: x 5)
@@ -86,7 +90,7 @@ template <class R, int V, int VP>
 __device__ __forceinline__ void vstore(R* __restrict__ p, const R* in) {
   if constexpr (VP % (16 / sizeof(R)) != 0) {
 #pragma unroll
-    for (int q = 0; q < V; ++q) p[q] = in[q];
+    for (int q = 0; q < (V < VP ? V : VP); ++q) p[q] = in[q];
   } else if constexpr (sizeof(R) == 4) {
 #pragma unroll
     for (int q = 0; q < VP / 4; ++q) {
@@ -367,6 +371,21 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
     constexpr bool BN = Sys::ID == kSysBN;
     R* as = cs + (size_t)2 * VP * P * P2;  // BN volume fraction [P][P2]
     R pg[P], us[P], vs[P];                // BN: NCP scalars per time level
+    // contraction of level l at this node: b = sum_k Dx Fx + sum_k Dy Fy (+ BN: ax, ay)
+    auto node_contract = [&](int l, R* b, R& ax, R& ay) {
+      contract<C::VF, VP, P>(cs, l, i, j, Dx, Dy, b);
+      if constexpr (BN) {
+        ax = R(0);
+        ay = R(0);
+#pragma unroll
+        for (int k = 0; k < P; ++k) {
+          ax = fma(Gx[k], as[l * P2 + k + P * j], ax);
+          ay = fma(Gy[k], as[l * P2 + i + P * k], ay);
+        }
+      }
+#pragma unroll
+      for (int v = C::VF; v < V; ++v) b[v] = R(0);
+    };
     // iteration 1: the state is constant in time
     {
       R Fx[V], Fy[V];
@@ -379,15 +398,9 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
       vstore<R, V, VP>(cs + fidx(0, 0, 0), Fx);
       vstore<R, V, VP>(cs + fidx(0, 1, 0), Fy);
       __syncthreads();
-      R b[V];
-      contract<V, VP, P>(cs, 0, i, j, Dx, Dy, b);
+      R b[V], ax, ay;
+      node_contract(0, b, ax, ay);
       if constexpr (BN) {
-        R ax = R(0), ay = R(0);
-#pragma unroll
-        for (int k = 0; k < P; ++k) {
-          ax = fma(Gx[k], as[k + P * j], ax);
-          ay = fma(Gy[k], as[i + P * k], ay);
-        }
         R n[9];
         BNSys::pncp<R>(pg[0], us[0], vs[0], ax, ay, n);
 #pragma unroll
@@ -437,15 +450,9 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
       }
 #pragma unroll
       for (int l = 0; l < P; ++l) {
-        R b[V];
-        contract<V, VP, P>(cs, l, i, j, Dx, Dy, b);
+        R b[V], ax, ay;
+        node_contract(l, b, ax, ay);
         if constexpr (BN) {
-          R ax = R(0), ay = R(0);
-#pragma unroll
-          for (int k = 0; k < P; ++k) {
-            ax = fma(Gx[k], as[l * P2 + k + P * j], ax);
-            ay = fma(Gy[k], as[l * P2 + i + P * k], ay);
-          }
           R n[9];
           BNSys::pncp<R>(pg[l], us[l], vs[l], ax, ay, n);
 #pragma unroll
