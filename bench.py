@@ -27,8 +27,9 @@ Ours:
               --rate req/s, initial fields projected and copied host->device on
               admission, results copied device->host on completion; it reports
               the p50/p99 time-to-solution;
-  roofline    the dominant kernel of the batched step (k_cells, FP64-pipe bound)
-              from its CUDA-event durations measured live;
+  roofline    the dominant kernel of the batched step (k_predictor, FP32-pipe
+              bound in the mixed mode) from its CUDA-event durations measured
+              live and the flop model predictor_flops_per_cell;
   cpu_baseline the FP64 CPU restatement of the reference (oracle/), one thread,
               on a bounded sample of the same requests.
 The reference arm times the same restatement on the host (the Fortran
@@ -73,20 +74,50 @@ def parse():
 
 
 # ---------------------------------------------------------------- work models
-def predictor_flops_per_cell(system, N):
-    """Floating-point operations the predictor executes per cell (FMA = 2,
-    division = 1) from the loop structure of predictor.cuh: the first Picard
-    iteration once (constant in time), N-1 full iterations, the last one
-    contracted to the time average, then volume integral and face extrapolation."""
+def predictor_flops_per_cell(system, N, ad_fused=True):
+    """Floating-point operations of the predictor per cell from the loop
+    structure of predictor.cuh: per node the operator rows (setup), the first
+    Picard iteration once (state constant in time), N-1 middle iterations, the
+    last one contracted to the time average and the volume integral; per cell
+    the face extrapolation.  A fused multiply-add is 2, a division 1; an
+    accumulation of n terms from zero is 2n - 1; Baer-Nunziato's structurally
+    zero components (ninth flux component, two NCP components) cost nothing.
+    Equal to the instrumented count of tests/test_flop_model.py.  ad_fused: the
+    advection-diffusion flux includes the convective part."""
     P, V = N + 1, NVAR[system]
-    cflux = {0: 6, 1: 19, 2: 60}[system]
-    extra = {0: 8 * P, 1: 0, 2: 8 * P + 12 + 2 * V}[system]
-    contract = 4 * P * V
-    it1 = cflux + contract + extra + 3 * P * V
-    mid = P * (cflux + contract + extra) + P * V + 2 * P * P * V
-    last = P * (cflux + 4 * V + contract + extra) + V + 2 * P * V
-    vol = V * (4 * P + 3)
-    return P * P * (it1 + max(N - 1, 0) * mid + last + vol) + 4 * P * V * 2 * 2 * P
+    P2 = P * P
+    mids = max(N - 1, 0)
+    dot = lambda n: 2 * n - 1  # noqa: E731  (n-term accumulation)
+    if system == 0:
+        flux = 2 * dot(P) + 2 + (4 if ad_fused else 0)  # gradient, -a grad, + c q
+        contract = dot(2 * P)
+        setup = 4 * P + 6             # Dx, Dy, Gx, Gy rows and scales, volume scales
+        it1 = flux + contract + 3 * P  # q(l) = g u - ts b
+        mid = P * (flux + 1 + contract + 2 * P)
+        last = P * flux + 4 * dot(P) + 1 + P * (contract + 2)
+        vol = 2 * dot(P) + 3
+        faces = 4 * P * 3 * dot(P)    # qbnd and the two gradQbnd components
+    elif system == 1:
+        cflux = 18                    # EulerSys::pflux
+        contract = V * dot(2 * P)
+        setup = 2 * P + 6
+        it1 = cflux + contract + 3 * P * V
+        mid = P * (cflux + contract + V + 2 * P * V)
+        last = P * (cflux + contract) + 2 * V * dot(P) + V * (1 + 2 * P)
+        vol = V * (2 * dot(P) + 3)
+        faces = 4 * P * V * 2 * dot(P)
+    else:
+        cflux = 42                    # BNSys::pflux
+        VF, VN = 8, 7                 # non-zero flux / NCP components
+        contract = VF * dot(2 * P)
+        ncp = 2 * dot(P) + 9 + 2 * (VN - 1) + 1  # grad alpha, NCP, b += dt NCP
+        setup = 4 * P + 6
+        it1 = cflux + contract + ncp + 3 * P * V
+        mid = P * (cflux + contract + ncp + V + 2 * P * V)
+        last = P * (cflux + contract + ncp) + 2 * VF * dot(P) + VN * dot(P) + V * (1 + 2 * P)
+        vol = (VF - 2) * (2 * dot(P) + 5) + 2 * (2 * dot(P) + 3) + 1
+        faces = 4 * P * (V + VF) * dot(P)
+    return P2 * (setup + it1 + mids * mid + last + vol) + faces
 
 
 # ---------------------------------------------------------------- clocks
@@ -313,7 +344,7 @@ def run_mix(args, aderdg, dist, rank, ws, lr):
         for k, v in ph.items():
             phase_tot[k] = phase_tot.get(k, 0.0) + v
     for spec, cfg, ic, key in members:
-        pred_flops += predictor_flops_per_cell(cfg.system, cfg.N) * cfg.cells
+        pred_flops += predictor_flops_per_cell(cfg.system, cfg.N, ad_fused=cfg.ad_flux_mode != 0) * cfg.cells
     dev_bytes = sum(g.info()["device_bytes"] for g in groups.values())
     for g in groups.values():
         g.close()
@@ -411,7 +442,7 @@ def run_single(args, aderdg, dist, rank, ws, lr):
         return None
     fp64_peak, fp32_peak = aderdg.probe_peaks()
     fpeak = fp32_peak if prec == aderdg.FP32_MIXED else fp64_peak
-    flops = predictor_flops_per_cell(cfg.system, cfg.N) * cfg.cells
+    flops = predictor_flops_per_cell(cfg.system, cfg.N, ad_fused=cfg.ad_flux_mode != 0) * cfg.cells
     ach = flops / (phases["predictor"] * 1e-3) / 1e9
     host = np.empty(cfg.dofs, dtype=np.float64)
     s.download_into(host)
