@@ -230,7 +230,7 @@ struct CellCfg {
   static_assert(8 * V * P2 + 4 * (3 * V * P2 + V * S * P + V * P * P) <= 8 * CELL_DBL, "FP32 cell layout");
   static constexpr int OPS_DBL = S * P + P * P;  // uh2lim, uh2lob (FP64, then FP32 in the mixed mode)
   static constexpr int SMEM_BYTES = CPB * CELL_DBL * 8 + OPS_DBL * 12 + CPB * 8 /*cell max*/ + CPB * 4 /*flags*/ +
-                                    CPB * V * 4 /*|U| max*/ + 16;
+                                    CPB * V * 4 /*|U| max*/ + CPB * V * 4 /*FP32 reference state*/ + 16;
   // blocks per SM the register allocation aims at: Euler's FP32-mixed cell
   // kernel is latency-bound and gains from a fourth block; the other
   // variants keep the allocation they reach unconstrained
@@ -251,6 +251,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
   unsigned long long* cmax = reinterpret_cast<unsigned long long*>(opsf + C::OPS_DBL + (C::OPS_DBL & 1));
   int* cflag = reinterpret_cast<int*>(cmax + CPB);
   unsigned* amax_all = reinterpret_cast<unsigned*>(cflag + CPB);  // [CPB][V]
+  float* ubs_all = reinterpret_cast<float*>(amax_all + CPB * V);  // [CPB][V]
 
   const int mode = a.mode;
   const int t = threadIdx.x;
@@ -281,6 +282,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
   float* LBf = LYf + V * S * P;
   float* REDf = LBf + V * P * P;
   unsigned* amax = amax_all + (in_cta ? lc : 0) * V;
+  float* ubs = ubs_all + (in_cta ? lc : 0) * V;
 
   // DMP neighbourhood bounds (get_min_max step 2, Euler/limiter.f90:147-167):
   // thread v < V of a cell folds its 3x3 Voronoi neighbourhood now, so the
@@ -329,7 +331,11 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
     cmax[lc] = 0ull;
     cflag[lc] = 0;
   }
-  if (kFast && in_cta && node < V) amax[node] = 0u;
+  if (kFast && in_cta && node < V) {
+    // the cell's FP32 reference state ubar: its start-of-step state at node 0, rounded to FP32
+    amax[node] = 0u;
+    ubs[node] = act ? (float)a.uh[par][(size_t)cell * P2 * V + node] : 0.0f;
+  }
   __syncthreads();
 
   // ---------------------------------------------------------------- update
@@ -424,15 +430,14 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
   if (mode == kCellSurface) return;  // uniform per launch: no barrier follows
 
   // FP32-mixed: the node's state in FP32, and its deviation from the cell's
-  // reference state ubar (the start-of-step state at node 0) in FP32
+  // FP32 reference state ubar, formed in FP32 (one conversion per value)
   float uf[V], du[V], ubf[V];
   if constexpr (kFast) {
-    const double* ub = a.uh[par] + (size_t)(valid ? cell : 0) * P2 * V;
 #pragma unroll
     for (int v = 0; v < V; ++v) {
+      ubf[v] = ubs[v];
       uf[v] = act ? (float)u[v] : 0.0f;
-      du[v] = act ? (float)(u[v] - ub[v]) : 0.0f;
-      ubf[v] = uf[v] - du[v];
+      du[v] = act ? uf[v] - ubf[v] : 0.0f;
     }
   }
 
@@ -469,7 +474,8 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
       bool f32ok = true;
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        err[v] = op.perr * __uint_as_float(amax[v]);
+        const float am = __uint_as_float(amax[v]);
+        err[v] = op.perr * am + op.pdev * (fabsf(ubf[v]) + 2.0f * am);
         f32ok = f32ok && err[v] <= 1.0e-4f;
       }
       if (act && !from_lh) {
@@ -558,7 +564,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
         float fmn = REDf[v * P2], fmx = REDf[(V + v) * P2];
 #pragma unroll
         for (int k = 1; k < P2; ++k) { fmn = fminf(fmn, REDf[v * P2 + k]); fmx = fmaxf(fmx, REDf[(V + v) * P2 + k]); }
-        const double ubar = a.uh[par][(size_t)cell * P2 * V + v];
+        const double ubar = (double)ubs[v];
         cmn = ubar + (double)fmn;
         cmx = ubar + (double)fmx;
       } else {

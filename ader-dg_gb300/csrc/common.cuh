@@ -91,6 +91,9 @@ struct DevOps {
   float uh2limf[S * P];
   float uh2lobf[P * P];
   float perr;
+  // deviations d = fl(fl(uh) - ubar) formed in FP32 from the FP32-rounded
+  // state: their rounding adds at most pdev * (|ubar| + 2 max|d|) to the projections
+  float pdev;
 };
 
 // Arguments shared by all kernels of one (system, N) batch.  The state that

@@ -95,6 +95,8 @@ void make_ops(const HostOps& h, void* out) {
     lam = r > lam ? r : lam;
   }
   o.perr = (float)(4.0 * (2 * P + 4) * std::ldexp(1.0, -24) * lam * lam);
+  // a rounding of 2^-24 (|uh| + |d|) per node, through the two passes; factor 2 of safety
+  o.pdev = (float)(2.0 * std::ldexp(1.0, -24) * lam * lam);
   *reinterpret_cast<DevOps<N, R>*>(out) = o;
 }
 

@@ -70,6 +70,8 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--host-setup", action="store_true", help="serve with host-projected initial fields")
+    ap.add_argument("--to-tend", action="store_true",
+                    help="single workload: also run it from t=0 to its end time (time-to-solution, exact-solution error)")
     return ap.parse_args()
 
 
@@ -453,6 +455,7 @@ def run_single(args, aderdg, dist, rank, ws, lr):
     e2e_s = time.perf_counter() - t_e
     info = s.info()
     s.close()
+    to_tend = run_to_tend(aderdg, cfg, ic, params, tend) if args.to_tend else None
     return {"metric": METRIC, "value": cfg.dofs * args.steps * ws / (total_ms * 1e-3), "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -467,7 +470,30 @@ def run_single(args, aderdg, dist, rank, ws, lr):
                          "peak_source": "aderdg_probe_peaks on this GPU"},
             "e2e": {"value": cfg.dofs * n_e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": cfg.dofs * 8,
                     "d2h_bytes_per_step": cfg.dofs * 8, "api": "aderdg_step_host"},
-            "clocks": clk.summary(), "limited_cells": info["n_limited"]}
+            "clocks": clk.summary(), "limited_cells": info["n_limited"], "to_tend": to_tend}
+
+
+def run_to_tend(aderdg, cfg, ic, params, tend):
+    """The whole simulation, t = 0 to its end time, with the device-resident run
+    loop (aderdg_run: graph replays, dt on the device, one host synchronisation
+    every 64 steps): time-to-solution from the initial field to the final state,
+    and for the fields with an exact solution (isentropic vortex, sine wave) the
+    error norms of the final cell averages."""
+    import torch
+    s = aderdg.Solver(cfg)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.initial_condition(ic, params)
+    t, n = s.run(0.0, tend, 10 ** 8, sync_every=64)
+    torch.cuda.synchronize()
+    tts = time.perf_counter() - t0
+    out = {"tend": tend, "time_reached": t, "steps": n, "tts_s": tts, "dof_updates_per_s": cfg.dofs * n / tts,
+           "limited_cells_at_end": s.info()["n_limited"]}
+    if ic in (aderdg.IC_EULER_VORTEX, aderdg.IC_AD_SINE):
+        e1, e2, ei = s.error_norms(ic, params)
+        out["error_vs_exact"] = {"l1": e1, "l2": e2, "linf": ei, "variable": 0}
+    s.close()
+    return out
 
 
 def run_ours(args):
