@@ -231,6 +231,25 @@ InstDesc make_inst_desc(const aderdg_config* cfg) {
   in.ph.cy = cfg->cy;
   in.ph.a = cfg->a;
   in.ph.ad_fused = cfg->ad_flux_mode;
+  if (cfg->system == ADERDG_SYS_ADVDIFF) {
+    // the expressions of the face kernel and of calc_time_step, evaluated once
+    const double pi = 4.0 * std::atan(1.0);
+    const double factor = (double)(2 * cfg->N + 1);
+    const double eta = factor / (in.dx * std::sqrt(0.5 * pi));
+    for (int d = 0; d < 2; ++d) {
+      const double nv0 = d == 0 ? 1.0 : 0.0, nv1 = d == 0 ? 0.0 : 1.0;
+      const double LL = cfg->cx * nv0 + cfg->cy * nv1, LR = LL;
+      const double smax_c = std::fmax(std::fabs(LL), std::fabs(LR));
+      const double smax_v = std::fmax(cfg->a, cfg->a);
+      in.ad_smax[d] = smax_c + 2.0 * eta * smax_v;
+    }
+    const double smax_v = std::fabs(cfg->a);
+    const double ex = std::fabs(cfg->cx * 1.0 + cfg->cy * 0.0), ey = std::fabs(cfg->cx * 0.0 + cfg->cy * 1.0);
+    double denom = 0.0;
+    denom = denom + (ex + 2.0 * smax_v * factor / in.dx) / in.dx;
+    denom = denom + (ey + 2.0 * smax_v * factor / in.dy) / in.dy;
+    in.ad_denom = denom;
+  }
   return in;
 }
 
@@ -304,17 +323,19 @@ int aderdg_create(const aderdg_config* cfg, aderdg_ctx** out) {
   if (!r) r = dalloc(c, &c->d_st, 1);
   if (!r) r = dalloc(c, &a.uh[0], st_elems);
   if (!r) r = dalloc(c, &a.uh[1], st_elems);
-  if (!r) r = dalloc(c, &a.duh, st_elems);
+  // duh and the face fluxes hold FP32 values in the FP32-mixed mode: half the doubles
+  auto stor = [&](size_t n) { return c->fp32 ? (n + 1) / 2 : n; };
+  if (!r) r = dalloc(c, &a.duh, stor(st_elems));
   unsigned char *qb = nullptr, *fb = nullptr;
   const size_t nbnd = nc * P * 4 * V;
   if (!r) r = dalloc(c, &qb, nbnd * rb);
   if (!r) r = dalloc(c, &fb, nbnd * rb * (cfg->system == ADERDG_SYS_ADVDIFF ? 2 : 1));
   a.qbnd = qb;
   a.fbnd = fb;
-  if (!r) r = dalloc(c, &a.fu, (size_t)c->nfx * P * V);
-  if (!r) r = dalloc(c, &a.gu, (size_t)c->nfy * P * V);
-  if (!r && cfg->system == ADERDG_SYS_BN) r = dalloc(c, &a.fp, (size_t)c->nfx * P * V);
-  if (!r && cfg->system == ADERDG_SYS_BN) r = dalloc(c, &a.gp, (size_t)c->nfy * P * V);
+  if (!r) r = dalloc(c, &a.fu, stor((size_t)c->nfx * P * V));
+  if (!r) r = dalloc(c, &a.gu, stor((size_t)c->nfy * P * V));
+  if (!r && cfg->system == ADERDG_SYS_BN) r = dalloc(c, &a.fp, stor((size_t)c->nfx * P * V));
+  if (!r && cfg->system == ADERDG_SYS_BN) r = dalloc(c, &a.gp, stor((size_t)c->nfy * P * V));
   if (!r) r = dalloc(c, &a.list_count, 1);
   if (c->limiter) {
     if (!r) r = dalloc(c, &a.status[0], nc);

@@ -89,9 +89,9 @@ int nvar(int sys) { return sys == ADERDG_SYS_ADVDIFF ? 1 : sys == ADERDG_SYS_EUL
 long long unit_bytes(int system, int N, int precision, int limiter) {
   const long long V = nvar(system), P = N + 1, S = 2 * N + 1;
   const long long rb = precision == ADERDG_FP32_MIXED ? 4 : 8;
-  long long b = 8 * V * P * P * 3;                                   // uh[2], duh
+  long long b = 8 * V * P * P * 2 + rb * V * P * P;                 // uh[2], duh
   b += rb * P * 4 * V * (system == ADERDG_SYS_ADVDIFF ? 3 : 2);     // qbnd, fbnd / gradQbnd
-  b += 8 * P * V * (system == ADERDG_SYS_BN ? 4 : 2);               // face fluxes
+  b += rb * P * V * (system == ADERDG_SYS_BN ? 4 : 2);              // face fluxes
   if (limiter && system != ADERDG_SYS_ADVDIFF)
     b += 8 * V * S * S * 2 + 4 * 2 + 8 * 2 * V * 2 + 1 + 4 + 4 + 8;  // Lh[2], status[2], mm[2], flags, list, denom
   return b;
@@ -262,16 +262,18 @@ int aderdg_batch_create(int system, int N, int precision, int limiter, long capa
   if (!r) r = balloc(b, &b->d_st, (size_t)max_instances);
   if (!r) r = balloc(b, &a.uh[0], U * P * P * V);
   if (!r) r = balloc(b, &a.uh[1], U * P * P * V);
-  if (!r) r = balloc(b, &a.duh, U * P * P * V);
+  // duh and the face fluxes hold FP32 values in the FP32-mixed mode: half the doubles
+  auto stor = [&](size_t n) { return precision ? (n + 1) / 2 : n; };
+  if (!r) r = balloc(b, &a.duh, stor(U * P * P * V));
   unsigned char *qb = nullptr, *fb = nullptr;
   if (!r) r = balloc(b, &qb, U * P * 4 * V * rb);
   if (!r) r = balloc(b, &fb, U * P * 4 * V * rb * (system == ADERDG_SYS_ADVDIFF ? 2 : 1));
   a.qbnd = qb;
   a.fbnd = fb;
-  if (!r) r = balloc(b, &a.fu, U * P * V);
-  if (!r) r = balloc(b, &a.gu, U * P * V);
-  if (!r && system == ADERDG_SYS_BN) r = balloc(b, &a.fp, U * P * V);
-  if (!r && system == ADERDG_SYS_BN) r = balloc(b, &a.gp, U * P * V);
+  if (!r) r = balloc(b, &a.fu, stor(U * P * V));
+  if (!r) r = balloc(b, &a.gu, stor(U * P * V));
+  if (!r && system == ADERDG_SYS_BN) r = balloc(b, &a.fp, stor(U * P * V));
+  if (!r && system == ADERDG_SYS_BN) r = balloc(b, &a.gp, stor(U * P * V));
   if (!r) r = balloc(b, &a.list_count, 1);
   if (b->limiter) {
     if (!r) r = balloc(b, &a.status[0], U);

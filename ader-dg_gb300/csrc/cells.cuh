@@ -188,12 +188,9 @@ __device__ __forceinline__ int nb_index(int x, int d, int n, int bc_lo, int bc_h
 template <class Sys, int N>
 __device__ __forceinline__ double cfl_denom(const InstDesc& in, const double* Q) {
   if constexpr (Sys::ID == kSysAD) {
-    const double factor = (double)(2 * N + 1);
-    double denom = 0.0;
-    const double smax_v = fabs(in.ph.a);
-    denom = denom + (ADSys::max_eig_c(in.ph, 0) + 2.0 * smax_v * factor / in.dx) / in.dx;
-    denom = denom + (ADSys::max_eig_c(in.ph, 1) + 2.0 * smax_v * factor / in.dy) / in.dy;
-    return denom;
+    // (|c_x| + 2 a (2N+1)/dx)/dx + (|c_y| + 2 a (2N+1)/dy)/dy, the same at every
+    // node: formed on the host in this order
+    return in.ad_denom;
   } else {
     double ex, ey;
     Sys::max_eig2(in.ph, Q, ex, ey);
@@ -447,7 +444,8 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
     double dn;
     if constexpr (kFast) dn = cfl_denom_f32<Sys, N>(in, typename Sys::FConst(in.ph), uf, u);
     else dn = cfl_denom<Sys, N>(in, u);
-    atomicMax(&cmax[lc], (unsigned long long)__double_as_longlong(dn));
+    // advection-diffusion: the denominator is the instance's constant, folded below
+    if constexpr (Sys::ID != kSysAD) atomicMax(&cmax[lc], (unsigned long long)__double_as_longlong(dn));
   }
 
   // ------------------------------------------------------------- DMP part
@@ -636,25 +634,18 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
     if (act && node == 0) a.denom[cell] = __longlong_as_double((long long)cmax[lc]);
     return;
   }
-  if (t == 0) {
-    // fold the CTA's cells per instance, one atomic per instance
-    int cur = -1;
+  // fold the CTA's cells per instance: the node-0 thread of the first cell of
+  // each instance in this CTA folds that instance's cells (a contiguous run)
+  // and issues one atomic
+  if (act && node == 0 && (lc == 0 || cell - 1 < in.cell_base)) {
     unsigned long long m = 0ull;
-    for (int c = 0; c < CPB; ++c) {
-      const long long cc = a.cell0 + (long long)blockIdx.x * CPB + c;
-      if (cc >= a.ncells) break;
-      const int kk = find_inst_cell(a.inst, a.ninst, cc);
-      if (kk < 0) continue;
-      const bool ok = priming ? (a.only_inst < 0 || kk == a.only_inst) : a.st[kk].active != 0;
-      if (!ok) continue;
-      if (kk != cur) {
-        if (cur >= 0) atomicMax(&a.st[cur].denom_next, m);
-        cur = kk;
-        m = 0ull;
-      }
-      m = m > cmax[c] ? m : cmax[c];
+    if constexpr (Sys::ID == kSysAD) {
+      m = (unsigned long long)__double_as_longlong(in.ad_denom);
+    } else {
+      const long long end = in.cell_base + (long long)in.imax * in.jmax;
+      for (int c = lc; c < CPB && cell + (c - lc) < end; ++c) m = m > cmax[c] ? m : cmax[c];
     }
-    if (cur >= 0) atomicMax(&a.st[cur].denom_next, m);
+    atomicMax(&a.st[kc].denom_next, m);
   }
 }
 

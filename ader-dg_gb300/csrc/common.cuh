@@ -42,6 +42,13 @@ struct InstDesc {
   int bc_mode;
   double cfl_pnpm;             // CFL * PNPMTable(N)
   Phys ph;
+  // advection-diffusion: constants of the instance formed once on the host in
+  // the reference's FP64 operation order (equal to the per-point values bit for
+  // bit): the face dissipation smax per direction (PDEViscLLFRiemannSolver,
+  // Advection-Diffusion/pde.f90:121-152) and the CFL denominator of every node
+  // (Advection-Diffusion/calc_time_step.f90:37-50)
+  double ad_smax[2];
+  double ad_denom;
 };
 
 // Mutable per-instance state, device resident.

@@ -155,8 +155,23 @@ __global__ void __launch_bounds__(256) k_faces(BatchArgs a, FaceConst fc) {
   if (gid >= nx + ny) return;
   const R* qb = reinterpret_cast<const R*>(a.qbnd);
   const R* fb = reinterpret_cast<const R*>(a.fbnd);
-  const bool xdir = gid < nx;
-  const long long g = xdir ? gid : gid - nx;
+  // x and y face points interleave warp by warp, so that the x faces and the
+  // y faces of the same cells run at the same time: a cell's face states lie
+  // side by side ([cell][P][4 faces][V]) and each DRAM burst then serves both
+  // directions instead of being fetched once per direction
+  const long long mw = (nx < ny ? nx : ny) >> 5;  // interleaved warp pairs
+  bool xdir;
+  long long g;
+  if (gid < 64 * mw) {
+    const long long w = gid >> 5;
+    xdir = (w & 1) == 0;
+    g = (w >> 1) * 32 + (gid & 31);
+  } else {
+    // the rest: x points [32 mw, nx), then y points [32 mw, ny)
+    const long long r = gid - 64 * mw, rx = nx - 32 * mw;
+    xdir = r < rx;
+    g = 32 * mw + (xdir ? r : r - rx);
+  }
   const long long face = g / P;
   const int l = (int)(g - face * P);
   const int k = xdir ? find_inst_fx(a.inst, a.ninst, face) : find_inst_fy(a.inst, a.ninst, face);
@@ -182,13 +197,15 @@ __global__ void __launch_bounds__(256) k_faces(BatchArgs a, FaceConst fc) {
   }
 
   if constexpr (Sys::ID == kSysAD) {
-    // Advection-Diffusion/riemann_problem.f90 with PDEViscLLFRiemannSolver (pde.f90:121-152)
-    double QL[1], QR[1], gL[2], gR[2];
-    auto get = [&](long long c, int f, double* Q, double* gq) {
+    // Advection-Diffusion/riemann_problem.f90 with PDEViscLLFRiemannSolver (pde.f90:121-152);
+    // compute type: FP64 (reference order), FP32 in the mixed mode
+    using CT = typename std::conditional<sizeof(R) == 4, float, double>::type;
+    CT QL[1], QR[1], gL[2], gR[2];
+    auto get = [&](long long c, int f, CT* Q, CT* gq) {
       const size_t o = (((size_t)c * P + l) * 4 + f);
-      Q[0] = (double)qb[o];
-      gq[0] = (double)fb[o * 2 + 0];
-      gq[1] = (double)fb[o * 2 + 1];
+      Q[0] = (CT)qb[o];
+      gq[0] = (CT)fb[o * 2 + 0];
+      gq[1] = (CT)fb[o * 2 + 1];
     };
     const long long cL = xdir ? cid(i - 1, j) : cid(i, j - 1);
     const long long cR = cid(i, j);
@@ -202,7 +219,7 @@ __global__ void __launch_bounds__(256) k_faces(BatchArgs a, FaceConst fc) {
           // y = (j-1 + xi_l) dy (Advection-Diffusion/riemann_problem.f90:37-40)
           get(cid(I - 1, j), 1, QR, gR);
           const double y = ((double)j + fc.xi[l]) * in.dy;
-          QL[0] = -QR[0] + 2.0 * sin(fc.pi * y);
+          QL[0] = -QR[0] + (CT)(2.0 * sin(fc.pi * y));
         } else {
           get(cR, fl, QR, gR);
           QL[0] = -QR[0];
@@ -231,17 +248,14 @@ __global__ void __launch_bounds__(256) k_faces(BatchArgs a, FaceConst fc) {
       get(cL, fr, QL, gL);
       get(cR, fl, QR, gR);
     }
-    const double nv0 = xdir ? 1.0 : 0.0, nv1 = xdir ? 0.0 : 1.0;
-    const double LL = ph.cx * nv0 + ph.cy * nv1, LR = LL;
-    const double factor = (double)(2 * N + 1);
-    const double eta = factor / (in.dx * sqrt(0.5 * fc.pi));
-    const double smax_c = fmax(fabs(LL), fabs(LR));
-    const double smax_v = fmax(ph.a, ph.a);
-    const double smax = smax_c + 2.0 * eta * smax_v;
-    const double FL0 = ph.cx * QL[0] + -ph.a * gL[0], FL1 = ph.cy * QL[0] + -ph.a * gL[1];
-    const double FR0 = ph.cx * QR[0] + -ph.a * gR[0], FR1 = ph.cy * QR[0] + -ph.a * gR[1];
+    const CT nv0 = xdir ? CT(1) : CT(0), nv1 = xdir ? CT(0) : CT(1);
+    // smax = max(|c.n|) + 2 eta a, eta = (2N+1) / (dx sqrt(pi/2)): formed on the host
+    const CT smax = (CT)in.ad_smax[xdir ? 0 : 1];
+    const CT cx = (CT)ph.cx, cy = (CT)ph.cy, ca = (CT)ph.a;
+    const CT FL0 = cx * QL[0] + -ca * gL[0], FL1 = cy * QL[0] + -ca * gL[1];
+    const CT FR0 = cx * QR[0] + -ca * gR[0], FR1 = cy * QR[0] + -ca * gR[1];
     R* dst = reinterpret_cast<R*>(xdir ? a.fu : a.gu);
-    dst[out] = (R)(0.5 * ((FL0 + FR0) * nv0 + (FL1 + FR1) * nv1) - 0.5 * smax * (QR[0] - QL[0]));
+    dst[out] = (R)(CT(0.5) * ((FL0 + FR0) * nv0 + (FL1 + FR1) * nv1) - CT(0.5) * smax * (QR[0] - QL[0]));
   } else {
     // compute type: FP64 (reference order), FP32 for Baer-Nunziato in the mixed mode
     using CT = typename std::conditional<sizeof(R) == 4, float, double>::type;
