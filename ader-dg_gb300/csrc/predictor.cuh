@@ -23,6 +23,8 @@
 // the reference, where lFh is not recomputed after the final iK1 update.
 #pragma once
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "physics.cuh"
 
@@ -315,13 +317,15 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
       for (int l = 0; l < P; ++l) q[l][0] = op.g[l] * u[0] - op.ts[l] * b[0];
     }
     __syncthreads();
-#pragma unroll 1
-    for (int it = 2; it <= P; ++it) {
-      const bool last = it == P;
+    // the Picard iterations 2..P; the last one is instantiated apart, so that
+    // its time averages (Fh, qh, ...) hold no registers in the others
+    auto picard = [&](auto last_tag) {
+      constexpr bool last = decltype(last_tag)::value;
+
 #pragma unroll
       for (int l = 0; l < P; ++l) qs[l * P2 + node] = q[l][0];
       __syncthreads();
-      if (last) { Fh[0][0] = Fh[1][0] = R(0); Gh[0] = Gh[1] = R(0); }
+      if constexpr (last) { Fh[0][0] = Fh[1][0] = R(0); Gh[0] = Gh[1] = R(0); }
 #pragma unroll
       for (int l = 0; l < P; ++l) {
         R gx = R(0), gy = R(0);
@@ -337,7 +341,7 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
         }
         cs[fidx(l, 0, 0)] = fx;
         cs[fidx(l, 1, 0)] = fy;
-        if (last) {
+        if constexpr (last) {
           Fh[0][0] = fma(op.w[l], fx, Fh[0][0]);
           Fh[1][0] = fma(op.w[l], fy, Fh[1][0]);
           Gh[0] = fma(op.w[l], gx, Gh[0]);
@@ -345,7 +349,7 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
         }
       }
       __syncthreads();
-      if (!last) {
+      if constexpr (!last) {
 #pragma unroll
         for (int l = 0; l < P; ++l) q[l][0] = op.g[l] * u[0];
 #pragma unroll
@@ -365,7 +369,10 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
         }
       }
       __syncthreads();
-    }
+    };
+#pragma unroll 1
+    for (int it = 2; it < P; ++it) picard(std::false_type{});
+    picard(std::true_type{});
   } else {
     // ------------------------------------------------- Euler / Baer-Nunziato
     constexpr bool BN = Sys::ID == kSysBN;
@@ -412,10 +419,12 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
         for (int v = 0; v < V; ++v) q[l][v] = op.g[l] * u[v] - op.ts[l] * b[v];
       __syncthreads();
     }
-#pragma unroll 1
-    for (int it = 2; it <= P; ++it) {
-      const bool last = it == P;
-      if (last) {
+    // the Picard iterations 2..P; the last one is instantiated apart, so that
+    // its time averages (Fh, qh, ...) hold no registers in the others
+    auto picard = [&](auto last_tag) {
+      constexpr bool last = decltype(last_tag)::value;
+
+      if constexpr (last) {
 #pragma unroll
         for (int v = 0; v < V; ++v) { Fh[0][v] = R(0); Fh[1][v] = R(0); }
       }
@@ -430,7 +439,7 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
         }
         vstore<R, V, VP>(cs + fidx(l, 0, 0), Fx);
         vstore<R, V, VP>(cs + fidx(l, 1, 0), Fy);
-        if (last) {
+        if constexpr (last) {
 #pragma unroll
           for (int v = 0; v < V; ++v) {
             Fh[0][v] = fma(op.w[l], Fx[v], Fh[0][v]);
@@ -439,7 +448,7 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
         }
       }
       __syncthreads();
-      if (!last) {
+      if constexpr (!last) {
 #pragma unroll
         for (int l = 0; l < P; ++l)
 #pragma unroll
@@ -458,10 +467,10 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
 #pragma unroll
           for (int v = 0; v < V; ++v) {
             b[v] = fma(rdt, n[v], b[v]);
-            if (last) Sh[v] = fma(-op.w[l], n[v], Sh[v]);
+            if constexpr (last) Sh[v] = fma(-op.w[l], n[v], Sh[v]);
           }
         }
-        if (!last) {
+        if constexpr (!last) {
 #pragma unroll
           for (int lp = 0; lp < P; ++lp)
 #pragma unroll
@@ -472,7 +481,10 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
         }
       }
       __syncthreads();
-    }
+    };
+#pragma unroll 1
+    for (int it = 2; it < P; ++it) picard(std::false_type{});
+    picard(std::true_type{});
   }
 
   // ------------------------------------------------------------- epilogue
