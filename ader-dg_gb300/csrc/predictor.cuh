@@ -53,11 +53,14 @@ struct PredCfg {
   static constexpr int CPB_S = SMEM_BUDGET / (CELL_ELEMS * (int)sizeof(R));
   static constexpr int CPB = (CPB_T < CPB_S ? CPB_T : CPB_S) < 1 ? 1 : (CPB_T < CPB_S ? CPB_T : CPB_S);
   static constexpr int THREADS = ((CPB * P2 + 31) / 32) * 32;
-  // FP32 is latency-bound at one CTA per SM: ask for two, three where the
-  // time column is short (advection-diffusion, Euler N <= 2); FP64 is
-  // pipe-bound either way
+  // FP32: CTAs per SM the register allocation aims at, measured per system
+  // and degree (more resident warps hide the shared-memory latency of the
+  // contractions; Baer-Nunziato's time column does not fit in fewer
+  // registers without spilling at N >= 3); FP64 is pipe-bound either way
   static constexpr int MIN_BLOCKS =
-      (sizeof(R) == 4 && THREADS > 128) ? ((Sys::ID == kSysAD || (Sys::ID == kSysEuler && N <= 2)) ? 3 : 2) : 1;
+      (sizeof(R) == 4 && THREADS > 128)
+          ? (Sys::ID == kSysAD ? 4 : Sys::ID == kSysEuler ? (N <= 3 ? 4 : 3) : (N <= 2 ? 3 : 2))
+          : 1;
   // threads past CPB*P2 (the tail of the last warp) take part in the barriers
   // and get a scratch slot of their own so they never touch a real cell's data
   static constexpr int SLOTS = CPB + (THREADS > CPB * P2 ? 1 : 0);
