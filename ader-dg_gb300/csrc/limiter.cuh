@@ -71,6 +71,9 @@ struct SubCfg {
   static constexpr int R = S + 4;  // gathered region: subcells -1 .. S+2 (1-based)
   static constexpr int H = S + 2;  // reconstructed region: 0 .. S+1
   static constexpr int THREADS = 128;
+  // CTAs per SM the register allocation aims at (FP32: one more than the
+  // unconstrained allocation allows where that does not spill)
+  static constexpr int MIN_BLOCKS = sizeof(T) == 4 ? (Sys::ID == kSysBN ? (N == 3 ? 4 : N == 2 ? 5 : 1) : 6) : 1;
   static constexpr int NE = (S + 1) * S;               // x edges (and y edges) of the subgrid
   static constexpr int NEF = (Sys::ID == kSysBN ? 4 : 2) * V * NE;  // edge fluxes (+ BN fluctuations)
   // compute-type (T) elements: sub0 [V][R*R], slopes x/y/t and wLx wRx wLy wRy
@@ -85,9 +88,9 @@ struct SubCfg {
   static_assert(V * P2 + V * S * P + V * P * P <= TSLOPE, "FP32 DMP room");
   static constexpr int TBYTES = ((TEL * (int)sizeof(T) + 15) / 16) * 16;
   // FP64 elements: new polynomial UN [V][P2], DMP y pass LY [V][S][P], LB
-  // [V][P][P], reduction [2][V][THREADS], operators uh2lim, uh2lob (FP64)
+  // [V][P][P], reduction [2][V][warps], operators uh2lim, uh2lob (FP64)
   static constexpr int OPS_DBL = S * P + P * P;
-  static constexpr int DEL = V * P2 + V * S * P + V * P * P + 2 * V * THREADS + OPS_DBL;
+  static constexpr int DEL = V * P2 + V * S * P + V * P * P + 2 * V * (THREADS / 32) + OPS_DBL;
   // misc: flags, CFL max, neighbour cells and their status
   static constexpr int MISC = 16 + 9 * 8 + 9 * 4 + 4 * V + 12;
   static constexpr int SMEM_BYTES = TBYTES + DEL * 8 + MISC;
@@ -140,7 +143,7 @@ __device__ __forceinline__ void warp_minmax_store(R* mn, R* mx, R* red, int t) {
 // eigenvalues (where the FP32 pressure is settled) in FP32; the state, Lh
 // and min/max in FP64.
 template <class Sys, int N, class T>
-__global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS) k_subcell(BatchArgs a, DevOps<N, double> op, FaceConst fc) {
+__global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>::MIN_BLOCKS) k_subcell(BatchArgs a, DevOps<N, double> op, FaceConst fc) {
   using C = SubCfg<Sys, N, T>;
   constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1, V = Sys::V, R = C::R, H = C::H, NT = C::THREADS, NE = C::NE;
   constexpr int NW = NT / 32;  // warps
@@ -165,8 +168,8 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS) k_subcell(BatchArg
   double* UN = reinterpret_cast<double*>(smem_raw + C::TBYTES);  // [V][P2]
   double* LY = UN + V * P2;          // DMP y pass [V][S][P]
   double* LB = LY + V * S * P;       // [V][P][P]
-  double* red = LB + V * P * P;      // [2][V][NT]
-  double* opsm = red + 2 * V * NT;   // uh2lim, uh2lob (FP64)
+  double* red = LB + V * P * P;      // [2][V][NW]
+  double* opsm = red + 2 * V * NW;   // uh2lim, uh2lob (FP64)
   unsigned char* misc = reinterpret_cast<unsigned char*>(opsm + C::OPS_DBL);
   int* flag = reinterpret_cast<int*>(misc);
   unsigned long long* cmaxp = reinterpret_cast<unsigned long long*>(misc + 8);
@@ -176,7 +179,7 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS) k_subcell(BatchArg
   float* UNf = reinterpret_cast<float*>(slx);                // FP32-mixed DMP (after the re-solve)
   float* LYf = UNf + V * P2;
   float* LBf = LYf + V * S * P;
-  float* redf = reinterpret_cast<float*>(red);              // [2][V][NT]
+  float* redf = reinterpret_cast<float*>(red);              // [2][V][NW]
 
   const int t = threadIdx.x;
   for (int k = t; k < C::OPS_DBL; k += NT) opsm[k] = k < S * P ? op.uh2lim[k] : op.uh2lob[k - S * P];
