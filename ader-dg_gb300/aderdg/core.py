@@ -147,6 +147,7 @@ def load(build_if_missing=False):
         "aderdg_last_error": (ctypes.c_char_p, [vp]),
         "aderdg_project_initial_condition": (i, [cfgp, i, dp, dp, dp]),
         "aderdg_probe_peaks": (i, [dp, dp]), "aderdg_set_array": (i, [vp, i, vp]),
+        "aderdg_host_alloc": (i, [ctypes.c_size_t, ctypes.POINTER(vp)]), "aderdg_host_free": (i, [vp]),
         "aderdg_operator": (i, [i, i, dp]), "aderdg_step_host": (i, [vp, dp, dp, d, dp, ip]),
         "aderdg_time_steps": (i, [vp, dp, d, i, i, dp]), "aderdg_profile_step": (i, [vp, dp, d, dp]),
         "aderdg_batch_unit_bytes": (ctypes.c_long, [i, i, i, i]),
@@ -184,7 +185,8 @@ EXPORTED = ("aderdg_create", "aderdg_destroy", "aderdg_upload", "aderdg_init_lim
             "aderdg_batch_release", "aderdg_batch_launch", "aderdg_batch_sync", "aderdg_batch_query",
             "aderdg_batch_download", "aderdg_batch_info", "aderdg_batch_last_error", "aderdg_batch_profile",
             "aderdg_batch_run_timed", "aderdg_initial_condition", "aderdg_batch_admit_ic",
-            "aderdg_cell_averages", "aderdg_batch_cell_averages", "aderdg_error_norms")
+            "aderdg_cell_averages", "aderdg_batch_cell_averages", "aderdg_error_norms", "aderdg_host_alloc",
+            "aderdg_host_free")
 
 
 def _dp(a):
@@ -221,6 +223,27 @@ def operator(N, which):
     if n < 0:
         raise AderdgError(n, "bad operator request")
     return out[:n].copy()
+
+
+class PinnedArray:
+    """A float64 numpy array in page-locked host memory (aderdg_host_alloc),
+    freed when this object goes away; `.array` is the numpy view."""
+
+    def __init__(self, n):
+        L = load()
+        self._L = L
+        self._p = ctypes.c_void_p()
+        r = L.aderdg_host_alloc(ctypes.c_size_t(max(int(n), 1) * 8), ctypes.byref(self._p))
+        if r != 0:
+            raise AderdgError(r, "aderdg_host_alloc of %d doubles failed" % n)
+        buf = (ctypes.c_double * max(int(n), 1)).from_address(self._p.value)
+        self.array = np.frombuffer(buf, dtype=np.float64, count=int(n))
+
+    def __del__(self):
+        p = getattr(self, "_p", None)
+        if p is not None and p.value:
+            self._L.aderdg_host_free(p)
+            self._p = None
 
 
 def probe_peaks():
@@ -499,9 +522,15 @@ class Batch:
                                       ctypes.byref(done))
         return dict(time=t.value, dt=dt.value, steps=st.value, done=bool(done.value), status=r)
 
-    def download(self, slot):
+    def download(self, slot, out=None):
+        """The simulation's uh; into `out` (a float64 C-contiguous array of at
+        least its DOFs, e.g. a PinnedArray's) when given, as a view of it."""
         cfg = self.cfgs[slot]
-        uh = np.empty(cfg.dofs, dtype=np.float64)
+        if out is None:
+            uh = np.empty(cfg.dofs, dtype=np.float64)
+        else:
+            assert out.dtype == np.float64 and out.flags.c_contiguous and out.size >= cfg.dofs
+            uh = out[: cfg.dofs]
         self._ck(self.L.aderdg_batch_download(self.h, slot, _dp(uh)))
         return uh
 

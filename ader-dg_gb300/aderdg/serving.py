@@ -20,7 +20,7 @@ import time
 
 import numpy as np
 
-from .core import FP64, SYS_ADVDIFF, Batch, project_initial_condition
+from .core import FP64, SYS_ADVDIFF, Batch, PinnedArray, project_initial_condition
 from . import workloads
 
 
@@ -46,6 +46,10 @@ class Request:
 
 
 def poisson_arrivals(n, rate, seed):
+    """Arrival times of a Poisson process of `rate` requests/s; an infinite
+    (or non-positive) rate is a burst: every request arrives at t = 0."""
+    if not np.isfinite(rate) or rate <= 0:
+        return np.zeros(n)
     rng = np.random.default_rng(seed + 1000)
     return np.cumsum(rng.exponential(1.0 / rate, size=n)) - 0.0
 
@@ -94,6 +98,10 @@ class Server:
             need[r.group] = max(need[r.group], Batch.units(r.cfg))
         for r in reqs:  # all batches exist before the clock starts
             self._group(r, len(need), need[r.group])
+        # results that are not kept land in one page-locked buffer (full-rate
+        # device-to-host copies, no first-touch page faults)
+        stage = PinnedArray(max(r.dofs for r in reqs)) if (self.download_results and not self.keep_results
+                                                           and reqs) else None
         pending = collections.deque(reqs)
         waiting = {g: collections.deque() for g in self.groups}
         running = {g: {} for g in self.groups}
@@ -149,7 +157,7 @@ class Server:
                     q = b.query(slot)
                     if q["done"]:
                         if self.download_results:
-                            res = b.download(slot)
+                            res = b.download(slot, out=None if stage is None else stage.array)
                             self.d2h_bytes += res.nbytes
                             if self.keep_results:
                                 r.result = res

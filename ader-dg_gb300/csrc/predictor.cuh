@@ -37,9 +37,9 @@ struct PredCfg {
   static constexpr int VEC = 16 / (int)sizeof(R);
   // flux components stored and contracted: Baer-Nunziato's volume fraction
   // has no conservative flux (its ninth component is 0, Baer-Nunziato/pde.f90:74-119),
-  // so FP32 stores 8 (two float4) where that does not make the register
-  // allocation spill (N <= 3); elsewhere all 9 (measured)
-  static constexpr int VF = (Sys::ID == kSysBN && sizeof(R) == 4 && N <= 3) ? 8 : V;
+  // so FP32 stores 8 (two float4) where that is faster (N <= 4; at N = 5
+  // the larger cells-per-CTA it allows spill registers); elsewhere all 9 (measured)
+  static constexpr int VF = (Sys::ID == kSysBN && sizeof(R) == 4 && N <= 4) ? 8 : V;
   // FP32: pad to whole float4; FP64: double2 when VF is even
   static constexpr int VP = (VF == 1) ? 1 : (sizeof(R) == 4 ? ((VF + VEC - 1) / VEC) * VEC : VF);
   // shared-memory elements per cell: flux buffer [P][2][P2][VP] (+ BN volume

@@ -66,3 +66,15 @@ extern "C" int aderdg_probe_peaks(double* fp64_gflops, double* fp32_gflops) {
   if (!r && fp32_gflops) r = measure<float>(fp32_gflops, sms);
   return r;
 }
+
+extern "C" int aderdg_host_alloc(size_t bytes, void** ptr) {
+  if (!ptr) return ADERDG_EINVAL;
+  *ptr = nullptr;
+  if (bytes == 0) return ADERDG_OK;
+  return cudaMallocHost(ptr, bytes) == cudaSuccess ? ADERDG_OK : ADERDG_ENOMEM;
+}
+
+extern "C" int aderdg_host_free(void* ptr) {
+  if (!ptr) return ADERDG_OK;
+  return cudaFreeHost(ptr) == cudaSuccess ? ADERDG_OK : ADERDG_ECUDA;
+}

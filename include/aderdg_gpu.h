@@ -21,6 +21,8 @@
 #ifndef ADERDG_GPU_H
 #define ADERDG_GPU_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -318,6 +320,14 @@ int aderdg_calc_time_step_noalloc(const aderdg_config* cfg, const double* uh, do
 /* Measured device peaks for roofline reporting: FP64 and FP32 FMA throughput
  * (GFLOP/s) from dependent-FMA microkernels on the current device. */
 int aderdg_probe_peaks(double* fp64_gflops, double* fp32_gflops);
+
+/* Page-locked host memory for the host side of uploads and downloads
+ * (aderdg_upload / aderdg_download / aderdg_batch_download and friends copy
+ * at the interconnect's full rate from and into it; pageable buffers go
+ * through a staging copy).  Not part of the reference's interface: its arrays
+ * are Fortran allocatables, which a caller may keep using. */
+int aderdg_host_alloc(size_t bytes, void** ptr);
+int aderdg_host_free(void* ptr);
 
 #ifdef __cplusplus
 }

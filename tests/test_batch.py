@@ -124,3 +124,18 @@ def test_batch_rejects_mismatched_config(gpu_lib):
     with pytest.raises(aderdg.AderdgError):
         _admit(b, cfg, ic, params, tend)
     b.close()
+
+
+def test_download_into_pinned_buffer(gpu_lib):
+    """aderdg_host_alloc memory as the target of a batch download: the same
+    values as a download into ordinary memory."""
+    cfg, ic, params, tend = aderdg.workloads.make("euler_rp2d", side=14, N=2, precision=aderdg.FP32_MIXED)
+    b = aderdg.Batch(cfg.system, cfg.N, aderdg.FP32_MIXED, 1, capacity_units=400, max_instances=4)
+    slot = b.admit_ic(cfg, ic, params, tend, 3)
+    b.launch(3)
+    b.sync()
+    plain = b.download(slot)
+    pin = aderdg.PinnedArray(cfg.dofs + 7)
+    got = b.download(slot, out=pin.array)
+    assert got.size == cfg.dofs and np.array_equal(got, plain)
+    b.close()
