@@ -117,7 +117,10 @@ class Server:
                 if not self.device_setup:
                     futures[r.rid] = self.pool.submit(self._prepare, r)
                 waiting[r.group].append(r)
-            # admit in arrival order per group while there is room
+            # admit in arrival order per group while there is room, and start the
+            # group's steps before admitting into the next group, so that its
+            # kernels overlap the next admissions
+            active = []
             for g, q in waiting.items():
                 b = self.groups[g]
                 while q:
@@ -140,15 +143,15 @@ class Server:
                     q.popleft()
                     r.slot, r.admitted = slot, clock()
                     running[g][slot] = r
-            active = [g for g in self.groups if running[g]]
+                if running[g]:
+                    b.launch(self.sync_every)
+                    active.append(g)
             if not active:
                 if pending:
                     time.sleep(max(0.0, min(pending[0].arrival - clock(), 0.01)))
                 else:
                     time.sleep(0.0005)
                 continue
-            for g in active:
-                self.groups[g].launch(self.sync_every)
             for g in active:
                 b = self.groups[g]
                 b.sync()
