@@ -442,11 +442,10 @@ int aderdg_initial_condition(aderdg_ctx* c, int ic, const double* params, int* n
   if (!c) return fail(c, ADERDG_EINVAL, "null context");
   if (n_limited) *n_limited = 0;
   const int par = cur_par(c);
-  // the subcell candidates are staged in the other Lh buffer: the initial
-  // DMP copies them into both buffers for the cells it limits
-  double* lh_stage = c->limiter ? c->args.lh[par ^ 1] : nullptr;
+  // the subcell candidates are formed after the initial DMP, for the cells it
+  // limits only, in both Lh buffers
   std::string why;
-  cudaError_t e = aderdg::launch_initial_field(c->cfg, ic, params, c->args.uh[par], lh_stage, c->stream, &why);
+  cudaError_t e = aderdg::launch_initial_field(c->cfg, ic, params, c->args.uh[par], nullptr, c->stream, &why);
   if (e == cudaErrorInvalidValue && !why.empty()) return fail(c, ADERDG_EINVAL, why);
   if (e != cudaSuccess) return fail_cuda(c, "initial field", e);
   if (c->limiter) {
@@ -459,11 +458,13 @@ int aderdg_initial_condition(aderdg_ctx* c, int ic, const double* params, int* n
   if (r) return r;
   c->uploaded = true;
   if (!c->limiter) return ADERDG_OK;
-  c->args.lh_ic = lh_stage;
+  c->args.lh_ic = nullptr;
   CK(c, control(c, aderdg::kCtlPrimeReset));
   r = cells(c, aderdg::kCellInitDmp);
-  c->args.lh_ic = nullptr;
-  if (!r) r = pull_state(c);
+  if (r) return r;
+  e = aderdg::launch_initial_lh(c->cfg, ic, params, c->args.status[0], c->args.lh[0], c->args.lh[1], c->stream, &why);
+  if (e != cudaSuccess) return fail_cuda(c, "initial limiter", e);
+  r = pull_state(c);
   if (r) return r;
   if (n_limited) *n_limited = c->h_st->n_recompute;
   r = prime(c);

@@ -389,17 +389,19 @@ int badmit(aderdg_batch* b, const aderdg_config* cfg, const double* uh, const do
   recompute_hw(b);
   r = push_table(b);
   if (r) return r;
-  // state of the new simulation (parity 0); the subcell candidates of the
-  // initial limiter are staged in the next-parity Lh slab of this simulation
+  // state of the new simulation (parity 0); host-given subcell candidates of
+  // the initial limiter are staged in the next-parity Lh slab of this
+  // simulation, device-evaluated ones are formed after the initial DMP for the
+  // cells it limits only
   const size_t cells = (size_t)cfg->imax * cfg->jmax, P2V = (size_t)b->P * b->P * b->V, S2V = (size_t)b->S * b->S * b->V;
   double* uh_dst = b->args.uh[0] + (size_t)base * P2V;
   double* lh_stage = b->limiter ? b->args.lh[1] + (size_t)base * S2V : nullptr;
   bool staged = false;
+  const bool lazy_lh = ic >= 0 && b->limiter;
   if (ic >= 0) {
     std::string why;
-    cudaError_t e = aderdg::launch_initial_field(*cfg, ic, params, uh_dst, lh_stage, b->stream, &why);
+    cudaError_t e = aderdg::launch_initial_field(*cfg, ic, params, uh_dst, nullptr, b->stream, &why);
     if (e != cudaSuccess) return bcuda(b, ("initial field: " + why).c_str(), e);
-    staged = lh_stage != nullptr;
   } else {
     BK(b, cudaMemcpyAsync(uh_dst, uh, cells * P2V * sizeof(double), cudaMemcpyHostToDevice, b->stream));
   }
@@ -413,10 +415,17 @@ int badmit(aderdg_batch* b, const aderdg_config* cfg, const double* uh, const do
     BK(b, cudaMemcpyAsync(lh_stage, lh_ic, cells * S2V * sizeof(double), cudaMemcpyHostToDevice, b->stream));
     staged = true;
   }
-  if (staged) {
+  if (staged || lazy_lh) {
     BK(b, bcontrol(b, aderdg::kCtlPrimeReset, pos));
-    r = bcells_one(b, pos, aderdg::kCellInitDmp, b->args.lh[1]);
+    r = bcells_one(b, pos, aderdg::kCellInitDmp, staged ? b->args.lh[1] : nullptr);
     if (r) return r;
+    if (lazy_lh) {
+      std::string why;
+      cudaError_t e = aderdg::launch_initial_lh(*cfg, ic, params, b->args.status[0] + base,
+                                                b->args.lh[0] + (size_t)base * S2V, b->args.lh[1] + (size_t)base * S2V,
+                                                b->stream, &why);
+      if (e != cudaSuccess) return bcuda(b, ("initial limiter: " + why).c_str(), e);
+    }
     r = bprime_one(b, pos);
     if (r) return r;
   }

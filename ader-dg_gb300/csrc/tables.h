@@ -39,6 +39,10 @@ struct KernelTable {
 // barycentres.  cudaErrorInvalidValue with *why set for an unknown field.
 cudaError_t launch_initial_field(const aderdg_config& cfg, int ic, const double* params, double* uh, double* lh,
                                  cudaStream_t s, std::string* why);
+// The subcell barycentre values of the cells with status != 0 only, into lh0
+// and lh1 (the initial limiter's candidates of the cells it limited).
+cudaError_t launch_initial_lh(const aderdg_config& cfg, int ic, const double* params, const int* status, double* lh0,
+                              double* lh1, cudaStream_t s, std::string* why);
 
 // Cell averages (or their primitive variables) of uh, [cell][V] (output.cu).
 cudaError_t launch_cell_averages(const aderdg_config& cfg, const double* uh, int primitive, double* out,
