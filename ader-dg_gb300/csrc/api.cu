@@ -71,7 +71,9 @@ int dalloc(aderdg_ctx* c, T** p, size_t n) {
   void* q = nullptr;
   cudaError_t e = cudaMalloc(&q, n * sizeof(T));
   if (e != cudaSuccess) return fail(c, ADERDG_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-  e = cudaMemset(q, 0, n * sizeof(T));
+  // zeroed in the context's stream: a plain cudaMemset runs on the legacy
+  // default stream, which the context's non-blocking stream does not wait for
+  e = cudaMemsetAsync(q, 0, n * sizeof(T), c->stream);
   if (e != cudaSuccess) {
     cudaFree(q);
     return fail_cuda(c, "cudaMemset", e);
@@ -362,7 +364,8 @@ int aderdg_create(const aderdg_config* cfg, aderdg_ctx** out) {
 
   InstDesc& in = c->h_inst;
   in = aderdg::make_inst_desc(cfg);
-  e = cudaMemcpy(c->d_inst, &in, sizeof(InstDesc), cudaMemcpyHostToDevice);
+  e = cudaMemcpyAsync(c->d_inst, &in, sizeof(InstDesc), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return bail(fail_cuda(nullptr, "cudaMemcpy inst", e));
 
   c->fc = aderdg::make_face_const(c->ops);

@@ -50,7 +50,10 @@ struct aderdg_batch {
   int num_sms = 0, subcell_grid = 0;
   InstDesc* d_inst = nullptr;
   InstState* d_st = nullptr;
+  InstDesc* d_inst_scr = nullptr;     // scratch copies for the table edits on the device
+  InstState* d_st_scr = nullptr;
   InstState* h_st = nullptr;          // pinned, max_inst entries (table order)
+  bool st_stale = false;              // h_st predates a table edit: pull before reading it
   std::vector<InstDesc> h_inst;       // table order: used entries sorted by base, then unused
   std::vector<int> slot_at;           // table position -> slot id
   std::vector<int> pos_of;            // slot id -> table position (-1: free)
@@ -104,8 +107,10 @@ int balloc(aderdg_batch* b, T** p, size_t n) {
   void* q = nullptr;
   cudaError_t e = cudaMalloc(&q, n * sizeof(T));
   if (e != cudaSuccess) return bfail(b, ADERDG_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-  e = cudaMemset(q, 0, n * sizeof(T));
-  if (e != cudaSuccess) return bcuda(b, "cudaMemset", e);
+  // zeroed in the batch's stream: a plain cudaMemset runs on the legacy
+  // default stream, which the batch's non-blocking stream does not wait for
+  e = cudaMemsetAsync(q, 0, n * sizeof(T), b->stream);
+  if (e != cudaSuccess) return bcuda(b, "cudaMemsetAsync", e);
   b->allocs.push_back(q);
   b->bytes += n * sizeof(T);
   *p = static_cast<T*>(q);
@@ -135,6 +140,57 @@ int push_table(aderdg_batch* b) {
 int pull_states(aderdg_batch* b) {
   BK(b, cudaMemcpyAsync(b->h_st, b->d_st, sizeof(InstState) * b->max_inst, cudaMemcpyDeviceToHost, b->stream));
   BK(b, cudaStreamSynchronize(b->stream));
+  b->st_stale = false;
+  return ADERDG_OK;
+}
+
+// Table edits on the device, in stream order with the steps already queued,
+// so that admission and release never wait for the GPU.  The device table
+// (descriptors and the live states) of n used entries gets an entry inserted
+// at pos (the rest move up one) or removed from pos (the rest move down one,
+// `fresh` fills the freed last entry), staged through scratch copies.
+template <class T>
+__device__ __forceinline__ void copy_words(T* dst, const T* src, int w) {
+  reinterpret_cast<unsigned long long*>(dst)[w] = reinterpret_cast<const unsigned long long*>(src)[w];
+}
+static_assert(sizeof(InstDesc) % 8 == 0 && sizeof(InstState) % 8 == 0, "table entries copied as 8-byte words");
+
+__global__ void k_table_stage(const InstDesc* ti, const InstState* ts, InstDesc* si, InstState* ss, int n, int pos,
+                              int insert, InstDesc fi, InstState fs) {
+  constexpr int WI = sizeof(InstDesc) / 8, WS = sizeof(InstState) / 8;
+  const int end = insert ? n + 1 : n;
+  const long long total = (long long)(end - pos) * (WI + WS);
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (long long)gridDim.x * blockDim.x) {
+    const int p = pos + (int)(k / (WI + WS)), w = (int)(k % (WI + WS));
+    const bool fresh = insert ? p == pos : p == n - 1;
+    const int q = insert ? p - 1 : p + 1;  // source entry of a moved one
+    if (w < WI) copy_words(&si[p], fresh ? &fi : &ti[q], w);
+    else copy_words(&ss[p], fresh ? &fs : &ts[q], w - WI);
+  }
+}
+
+__global__ void k_table_commit(InstDesc* ti, InstState* ts, const InstDesc* si, const InstState* ss, int lo, int hi) {
+  constexpr int WI = sizeof(InstDesc) / 8, WS = sizeof(InstState) / 8;
+  const long long total = (long long)(hi - lo) * (WI + WS);
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (long long)gridDim.x * blockDim.x) {
+    const int p = lo + (int)(k / (WI + WS)), w = (int)(k % (WI + WS));
+    if (w < WI) copy_words(&ti[p], &si[p], w);
+    else copy_words(&ts[p], &ss[p], w - WI);
+  }
+}
+
+// n: used entries before the edit
+int btable_edit(aderdg_batch* b, int n, int pos, bool insert, const InstDesc& fi, const InstState& fs) {
+  const int end = insert ? n + 1 : n;
+  if (end <= pos) return ADERDG_OK;
+  const long long words = (long long)(end - pos) * ((sizeof(InstDesc) + sizeof(InstState)) / 8);
+  const unsigned blocks = (unsigned)std::min<long long>((words + 255) / 256, 64);
+  k_table_stage<<<blocks, 256, 0, b->stream>>>(b->d_inst, b->d_st, b->d_inst_scr, b->d_st_scr, n, pos, insert ? 1 : 0,
+                                               fi, fs);
+  BK(b, cudaGetLastError());
+  k_table_commit<<<blocks, 256, 0, b->stream>>>(b->d_inst, b->d_st, b->d_inst_scr, b->d_st_scr, pos, end);
+  BK(b, cudaGetLastError());
+  b->st_stale = true;
   return ADERDG_OK;
 }
 
@@ -260,6 +316,8 @@ int aderdg_batch_create(int system, int N, int precision, int limiter, long capa
   std::memset(&a, 0, sizeof(a));
   int r = balloc(b, &b->d_inst, (size_t)max_instances);
   if (!r) r = balloc(b, &b->d_st, (size_t)max_instances);
+  if (!r) r = balloc(b, &b->d_inst_scr, (size_t)max_instances);
+  if (!r) r = balloc(b, &b->d_st_scr, (size_t)max_instances);
   if (!r) r = balloc(b, &a.uh[0], U * P * P * V);
   if (!r) r = balloc(b, &a.uh[1], U * P * P * V);
   // duh and the face fluxes hold FP32 values in the FP32-mixed mode: half the doubles
@@ -361,14 +419,14 @@ int badmit(aderdg_batch* b, const aderdg_config* cfg, const double* uh, const do
       break;
     }
   if (base < 0) return bfail(b, ADERDG_ENOSPACE, "no free range of " + std::to_string(need) + " units");
-  r = pull_states(b);
-  if (r) return r;
-  // insert into the table, keeping it sorted by base
+  // insert into the table, keeping it sorted by base: the descriptors on the
+  // host, the device table (descriptors and live states) by a table edit in
+  // stream order after the steps already queued
+  const int n_before = b->n_used;
   int pos = 0;
   while (pos < b->n_used && b->h_inst[pos].cell_base < base) ++pos;
   for (int p = b->n_used; p > pos; --p) {
     b->h_inst[p] = b->h_inst[p - 1];
-    b->h_st[p] = b->h_st[p - 1];
     b->slot_at[p] = b->slot_at[p - 1];
     b->pos_of[b->slot_at[p]] = p;
   }
@@ -381,13 +439,13 @@ int badmit(aderdg_batch* b, const aderdg_config* cfg, const double* uh, const do
   InstDesc& in = b->h_inst[pos];
   in = aderdg::make_inst_desc(cfg);
   in.cell_base = in.fx_base = in.fy_base = base;
-  InstState& st = b->h_st[pos];
+  InstState st;
   std::memset(&st, 0, sizeof(st));
   st.time = 0.0;
   st.tend = tend;
   st.max_steps = max_steps;
   recompute_hw(b);
-  r = push_table(b);
+  r = btable_edit(b, n_before, pos, true, in, st);
   if (r) return r;
   // state of the new simulation (parity 0); host-given subcell candidates of
   // the initial limiter are staged in the next-parity Lh slab of this
@@ -429,8 +487,8 @@ int badmit(aderdg_batch* b, const aderdg_config* cfg, const double* uh, const do
     r = bprime_one(b, pos);
     if (r) return r;
   }
-  r = pull_states(b);
-  if (r) return r;
+  // nothing waits for the GPU: the host mirror of the states is refreshed at
+  // the next sync (or query)
   *slot = s;
   return ADERDG_OK;
 }
@@ -450,14 +508,12 @@ int aderdg_batch_admit_ic(aderdg_batch* b, const aderdg_config* cfg, int ic, con
 
 int aderdg_batch_release(aderdg_batch* b, int slot) {
   if (!b || slot < 0 || slot >= b->max_inst || b->pos_of[slot] < 0) return bfail(b, ADERDG_EINVAL, "bad slot");
-  int r = pull_states(b);
-  if (r) return r;
   const int pos = b->pos_of[slot];
+  const int n_before = b->n_used;
   const InstDesc in = b->h_inst[pos];
   const long long size = (long long)(in.imax + 1) * (in.jmax + 1);
   for (int p = pos; p < b->n_used - 1; ++p) {
     b->h_inst[p] = b->h_inst[p + 1];
-    b->h_st[p] = b->h_st[p + 1];
     b->slot_at[p] = b->slot_at[p + 1];
     b->pos_of[b->slot_at[p]] = p;
   }
@@ -466,7 +522,10 @@ int aderdg_batch_release(aderdg_batch* b, int slot) {
   d = InstDesc{};
   d.imax = d.jmax = 1;
   d.cell_base = d.fx_base = d.fy_base = kUnusedBase;
-  std::memset(&b->h_st[b->n_used], 0, sizeof(InstState));
+  InstState zero;
+  std::memset(&zero, 0, sizeof(zero));
+  int r = btable_edit(b, n_before, pos, false, d, zero);
+  if (r) return r;
   b->slot_at[b->n_used] = -1;
   b->pos_of[slot] = -1;
   // return the range to the free list, merging neighbours
@@ -480,7 +539,7 @@ int aderdg_batch_release(aderdg_batch* b, int slot) {
   }
   fr.swap(merged);
   recompute_hw(b);
-  return push_table(b);
+  return ADERDG_OK;
 }
 
 int aderdg_batch_launch(aderdg_batch* b, int steps) {
@@ -548,6 +607,10 @@ int aderdg_batch_sync(aderdg_batch* b, int* n_running) {
 
 int aderdg_batch_query(aderdg_batch* b, int slot, double* time, double* dt, long* steps, int* done) {
   if (!b || slot < 0 || slot >= b->max_inst || b->pos_of[slot] < 0) return bfail(b, ADERDG_EINVAL, "bad slot");
+  if (b->st_stale) {
+    const int r = pull_states(b);
+    if (r) return r;
+  }
   const InstState& s = b->h_st[b->pos_of[slot]];
   if (time) *time = s.time;
   if (dt) *dt = s.dt;
