@@ -139,3 +139,37 @@ def test_download_into_pinned_buffer(gpu_lib):
     got = b.download(slot, out=pin.array)
     assert got.size == cfg.dofs and np.array_equal(got, plain)
     b.close()
+
+
+def test_admissions_queue_without_waiting(gpu_lib):
+    """Admissions and releases edit the device table in stream order without
+    waiting for the GPU: many admissions straight after the batch is created,
+    then K steps; every simulation has made exactly K steps and equals its run
+    alone."""
+    members = [("euler_rp2d", 10 + k % 5, {}) for k in range(10)]
+    cfgs = []
+    b = aderdg.Batch(aderdg.SYS_EULER, 2, aderdg.FP64, 1, capacity_units=3000, max_instances=16)
+    slots = []
+    for name, side, over in members:
+        cfg, ic, params, tend = aderdg.workloads.make(name, side=side, N=2, **over)
+        slots.append(b.admit_ic(cfg, ic, params, tend, 4))
+        cfgs.append((cfg, ic, params, tend))
+    b.release(slots[3])  # a release in the middle of the queued admissions
+    b.launch(6)
+    b.sync()
+    for k, slot in enumerate(slots):
+        if k == 3:
+            continue
+        q = b.query(slot)
+        assert q["steps"] == 4 and q["done"] and q["status"] == 0, (k, q)
+    for k in (0, 9):
+        cfg, ic, params, tend = cfgs[k]
+        s = aderdg.Solver(cfg)
+        s.initial_condition(ic, params)
+        t = 0.0
+        for _ in range(4):
+            t, _, _ = s.step(t, tend)
+        alone, _ = s.download()
+        s.close()
+        assert np.array_equal(b.download(slots[k]), alone)
+    b.close()
