@@ -1,0 +1,79 @@
+"""The four base cases at their full sizes (AD 64^2 N=3, Euler vortex 256^2
+N=4, Euler 2D Riemann problem 512^2 N=3, Baer-Nunziato cylinder 400^2 N=3).
+
+- One FP64 step against the oracle: relative L1 / L-infinity of uh <= 1e-11,
+  the same time step and the same troubled-cell mask.
+- Size-independent properties over several steps: conservation of the totals
+  on the periodic vortex (FP64 and FP32-mixed) and free-stream preservation
+  of a uniform flow on the vortex grid.
+"""
+import numpy as np
+import pytest
+
+import aderdg
+import pyoracle as po
+
+from helpers import rel_l1, rel_linf, setup_pair
+
+pytestmark = pytest.mark.gpu
+
+FULL = [("ad_sine", 3, 64), ("euler_vortex", 4, 256), ("euler_rp2d", 3, 512), ("bn_cylinder", 3, 400)]
+
+
+@pytest.mark.parametrize("name,N,side", FULL)
+def test_full_size_step_parity_fp64(gpu_lib, name, N, side):
+    cfg, ic, params, tend = aderdg.workloads.make(name, side=side, N=N)
+    o, g, uh, lh = setup_pair(cfg, ic, params)
+    t_o, dt_o, n_o = o.step(0.0, tend)
+    t_g, dt_g, n_g = g.step(0.0, tend)
+    assert dt_g == dt_o, (dt_g, dt_o)
+    assert n_g == n_o
+    ug, _ = g.download()
+    uo = o.get(po.UH)
+    e1, ei = rel_l1(ug, uo), rel_linf(ug, uo)
+    assert e1 <= 1e-11 and ei <= 1e-11, (e1, ei)
+    if cfg.limiter and cfg.system != aderdg.SYS_ADVDIFF:
+        assert np.array_equal(g.get(aderdg.A_RECOMPUTE), o.get_int(po.RECOMPUTE))
+    g.close()
+
+
+def _totals(cfg, uh):
+    """Integral of every conserved variable over the domain (Gauss-Legendre)."""
+    P, V = cfg.N + 1, cfg.nvar
+    w = aderdg.operator(cfg.N, aderdg.OP_W)
+    W = np.outer(w, w).ravel()  # node i + P j
+    dx = (cfg.xr[0] - cfg.xl[0]) / cfg.imax
+    dy = (cfg.xr[1] - cfg.xl[1]) / cfg.jmax
+    u = uh.reshape(cfg.cells, P * P, V)
+    return np.einsum("n,cnv->v", W, u) * dx * dy
+
+
+@pytest.mark.parametrize("precision,tol", [(aderdg.FP64, 1e-13), (aderdg.FP32_MIXED, 1e-8)])
+def test_full_size_conservation_vortex(gpu_lib, precision, tol):
+    cfg, ic, params, tend = aderdg.workloads.make("euler_vortex", precision=precision)
+    s = aderdg.Solver(cfg)
+    s.initial_condition(ic, params)
+    u0, _ = s.download()
+    before = _totals(cfg, u0)
+    t, n = s.run(0.0, tend, 5)
+    assert n == 5
+    u1, _ = s.download()
+    after = _totals(cfg, u1)
+    s.close()
+    # mass and energy are O(100) on the 10x10 domain; the momenta are too (u = v = 1)
+    assert np.all(np.abs(after - before) <= tol * np.abs(before)), (before, after)
+
+
+@pytest.mark.parametrize("precision,tol", [(aderdg.FP64, 1e-13), (aderdg.FP32_MIXED, 1e-6)])
+def test_full_size_free_stream(gpu_lib, precision, tol):
+    cfg, ic, params, tend = aderdg.workloads.make("euler_vortex", precision=precision)
+    params = (0.0,) + tuple(params[1:])  # vortex strength 0: the uniform free stream
+    s = aderdg.Solver(cfg)
+    s.initial_condition(ic, params)
+    u0, _ = s.download()
+    t, n = s.run(0.0, tend, 3)
+    assert n == 3
+    u1, st = s.download()
+    s.close()
+    assert rel_linf(u1, u0) <= tol, rel_linf(u1, u0)
+    assert not st.any()  # nothing limited
