@@ -29,9 +29,11 @@ Ours:
               batched steps, each result copied device->host when its request
               ends; a second served run with Poisson arrivals at --rate req/s
               gives the p50/p99 time-to-solution (latency_s);
-  roofline    the dominant kernel of the batched step (k_predictor, FP32-pipe
-              bound in the mixed mode) from its CUDA-event durations measured
-              live and the flop model predictor_flops_per_cell;
+  roofline    the dominant kernel of the batched step (k_predictor) against
+              the FP32 (mixed mode) or FP64 FMA peak, from its CUDA-event
+              durations measured live and the flop model
+              predictor_flops_per_cell; in the mixed mode it is bound by the
+              shared-memory wavefronts of its contractions, not by the pipe;
   cpu_baseline the FP64 CPU restatement of the reference (oracle/), one thread,
               on a bounded sample of the same requests.
 The reference arm times the same restatement on the host (the Fortran
@@ -368,7 +370,10 @@ def run_mix(args, aderdg, dist, rank, ws, lr):
             "flops_per_launch": pred_flops, "flop_model": "bench.py predictor_flops_per_cell x cells",
             "launch_ms": pred_ms, "dominant_phase": dominant,
             "phase_share": {k: v / sum(kern_ms.values()) for k, v in kern_ms.items()},
-            "phase_ms_one_step": phase_tot, "traffic": None}
+            "phase_ms_one_step": phase_tot, "traffic": None,
+            "limiter": ("FP32: shared-memory wavefronts of the flux contractions (86% of peak in the ncu capture of "
+                        "profiles/k_predictor_k_cells_euler_vortex_256_N4.md), not the FP32 pipe; FP64: the FP64 pipe"
+                        if mixed else "the FP64 pipe (90% busy in profiles/k_predictor_k_cells_euler_vortex_256_N4.md)")}
     try:
         with open(os.path.join(REPO, "profiles", "traffic.json")) as fh:
             tr = json.load(fh)
