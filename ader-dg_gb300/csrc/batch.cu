@@ -487,8 +487,10 @@ int badmit(aderdg_batch* b, const aderdg_config* cfg, const double* uh, const do
     r = bprime_one(b, pos);
     if (r) return r;
   }
-  // nothing waits for the GPU: the host mirror of the states is refreshed at
-  // the next sync (or query)
+  // nothing waits for the GPU (the host mirror of the states is refreshed at
+  // the next sync or query), except that host arrays are copied before the
+  // call returns, so that the caller may reuse them
+  if (ic < 0) BK(b, cudaStreamSynchronize(b->stream));
   *slot = s;
   return ADERDG_OK;
 }

@@ -233,7 +233,12 @@ int aderdg_batch_destroy(aderdg_batch* b);
 /* Admits one simulation (cfg must match the batch; uh and lh_ic as in
  * aderdg_upload / aderdg_init_limiter, lh_ic nullable) that runs until tend
  * or max_steps steps (<= 0: no limit).  *slot receives its id.
- * ADERDG_ENOSPACE when no free range or table entry is left. */
+ * ADERDG_ENOSPACE when no free range or table entry is left.  The set-up is
+ * queued on the batch's stream behind the steps already launched; the call
+ * returns once uh and lh_ic have been copied (they may be reused), and
+ * aderdg_batch_admit_ic returns without waiting for the GPU at all.
+ * aderdg_batch_release frees the simulation's units and table entry, also
+ * without waiting. */
 int aderdg_batch_admit(aderdg_batch* b, const aderdg_config* cfg, const double* uh, const double* lh_ic, double tend,
                        long max_steps, int* slot);
 int aderdg_batch_release(aderdg_batch* b, int slot);
@@ -242,6 +247,9 @@ int aderdg_batch_release(aderdg_batch* b, int slot);
  * back and gives the number still running. */
 int aderdg_batch_launch(aderdg_batch* b, int steps);
 int aderdg_batch_sync(aderdg_batch* b, int* n_running);
+/* One simulation's state as read back by the last aderdg_batch_sync (read
+ * back now, waiting for the batch's stream, when an admission or release came
+ * after it). */
 int aderdg_batch_query(aderdg_batch* b, int slot, double* time, double* dt, long* steps, int* done);
 int aderdg_batch_download(aderdg_batch* b, int slot, double* uh);
 int aderdg_batch_info(aderdg_batch* b, long* used_units, long* capacity_units, long* device_bytes, int* n_instances);
