@@ -215,6 +215,28 @@ __device__ __forceinline__ double cfl_denom_f32(const InstDesc& in, const typena
   }
 }
 
+// Maximum over the P2 lanes of a cell when every cell is an aligned segment
+// of a warp (P2 = 4 or 16): xor shuffles within the segment; every lane of the
+// warp must call it.
+template <int P2>
+__device__ __forceinline__ unsigned seg_max(unsigned x) {
+#pragma unroll
+  for (int o = P2 / 2; o > 0; o >>= 1) {
+    const unsigned y = __shfl_xor_sync(0xffffffffu, x, o, P2);
+    x = x > y ? x : y;
+  }
+  return x;
+}
+template <int P2>
+__device__ __forceinline__ unsigned long long seg_max(unsigned long long x) {
+#pragma unroll
+  for (int o = P2 / 2; o > 0; o >>= 1) {
+    const unsigned long long y = __shfl_xor_sync(0xffffffffu, x, o, P2);
+    x = x > y ? x : y;
+  }
+  return x;
+}
+
 template <class Sys, int N>
 struct CellCfg {
   static constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1, V = Sys::V;
@@ -440,7 +462,22 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
 
   // ------------------------------------------------------------- CFL part
   const bool want_cfl = mode != kCellInitDmp;
-  if (act && want_cfl) {
+  // cells as aligned warp segments: per-cell maxima by shuffles, one store per
+  // cell instead of P2 atomics on one shared address
+  constexpr bool kSeg = (32 % P2) == 0 && (C::THREADS % 32) == 0 && C::CPB * P2 == C::THREADS;
+  if constexpr (kSeg && Sys::ID != kSysAD) {
+    if (want_cfl) {
+      unsigned long long bits = 0ull;
+      if (act) {
+        double dn;
+        if constexpr (kFast) dn = cfl_denom_f32<Sys, N>(in, typename Sys::FConst(in.ph), uf, u);
+        else dn = cfl_denom<Sys, N>(in, u);
+        bits = (unsigned long long)__double_as_longlong(dn);
+      }
+      bits = seg_max<P2>(bits);
+      if (act && node == 0) cmax[lc] = bits;
+    }
+  } else if (act && want_cfl) {
     double dn;
     if constexpr (kFast) dn = cfl_denom_f32<Sys, N>(in, typename Sys::FConst(in.ph), uf, u);
     else dn = cfl_denom<Sys, N>(in, u);
@@ -461,7 +498,15 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
         for (int v = 0; v < V; ++v) {
           U[v * P2 + node] = u[v];
           Uf[v * P2 + node] = du[v];
-          atomicMax(&amax[v], __float_as_uint(fabsf(du[v])));
+          if constexpr (!kSeg) atomicMax(&amax[v], __float_as_uint(fabsf(du[v])));
+        }
+      }
+      if constexpr (kSeg) {
+        // du = 0 in lanes of inactive cells
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          const unsigned m = seg_max<P2>(__float_as_uint(fabsf(du[v])));
+          if (act && node == 0) amax[v] = m;
         }
       }
       __syncthreads();
