@@ -819,6 +819,30 @@ long aderdg_array_size(aderdg_ctx* c, int which) {
   return ADERDG_EINVAL;
 }
 
+namespace {
+
+// The face states are stored face-major on the device ([cell][face][point][e])
+// and exchanged in the reference's order qbnd(e, face, point, cell); e runs
+// over V values (2 V for gradQbnd).  0 for the other arrays.
+int face_state_width(const aderdg_ctx* c, int which) {
+  if (which == ADERDG_A_QBND || which == ADERDG_A_FBND) return c->V;
+  if (which == ADERDG_A_GRADQBND) return 2 * c->V;
+  return 0;
+}
+
+void face_order(const double* src, double* dst, long ncells, int P, int E, bool to_reference) {
+  for (long cc = 0; cc < ncells; ++cc)
+    for (int f = 0; f < 4; ++f)
+      for (int l = 0; l < P; ++l) {
+        const size_t mine = (((size_t)cc * 4 + f) * P + l) * E, ref = (((size_t)cc * P + l) * 4 + f) * E;
+        const double* s = src + (to_reference ? mine : ref);
+        double* d = dst + (to_reference ? ref : mine);
+        for (int e = 0; e < E; ++e) d[e] = s[e];
+      }
+}
+
+}  // namespace
+
 int aderdg_get_array(aderdg_ctx* c, int which, void* out) {
   if (!c || !out) return fail(c, ADERDG_EINVAL, "null argument");
   const long n = aderdg_array_size(c, which);
@@ -863,10 +887,15 @@ int aderdg_get_array(aderdg_ctx* c, int which, void* out) {
     CK(c, cudaStreamSynchronize(c->stream));
     double* o = static_cast<double*>(out);
     for (long k = 0; k < n; ++k) o[k] = (double)tmp[k];
-    return ADERDG_OK;
+  } else {
+    CK(c, cudaMemcpyAsync(out, src, n * esz, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
   }
-  CK(c, cudaMemcpyAsync(out, src, n * esz, cudaMemcpyDeviceToHost, c->stream));
-  CK(c, cudaStreamSynchronize(c->stream));
+  if (const int E = face_state_width(c, which)) {
+    double* o = static_cast<double*>(out);
+    std::vector<double> mine(o, o + n);
+    face_order(mine.data(), o, (long)c->ncells, c->P, E, true);
+  }
   return ADERDG_OK;
 }
 
@@ -898,6 +927,12 @@ int aderdg_set_array(aderdg_ctx* c, int which, const void* in) {
     default: return fail(c, ADERDG_EINVAL, "array is read-only");
   }
   if (!dst) return fail(c, ADERDG_ESTATE, "array not allocated yet");
+  std::vector<double> mine;
+  if (const int E = face_state_width(c, which)) {
+    mine.resize((size_t)n);
+    face_order(static_cast<const double*>(in), mine.data(), (long)c->ncells, c->P, E, false);
+    in = mine.data();
+  }
   if (narrow) {
     std::vector<float> tmp((size_t)n);
     const double* s = static_cast<const double*>(in);

@@ -5,8 +5,9 @@
 //   range [cell_base, cell_base + imax*jmax), cell = i + imax*j inside it.
 //   uh      [cell][P*P nodes][V]   FP64, exactly the Fortran uh(v,i,j,I,J)
 //   duh     [cell][P*P][V]         FP64 (FP32 in the FP32-mixed mode)
-//   qbnd    [cell][P][4][V]        reference qbnd(v,face,l,I,J)
-//   fbnd    [cell][P][4][V]        (AD: gradQbnd [cell][P][4][2][V])
+//   qbnd    [cell][4][P][V]        face-major: a face's P points contiguous
+//   fbnd    [cell][4][P][V]        (AD: gradQbnd [cell][4][P][2][V]); the API's
+//                                  get/set give the reference's qbnd(v,face,l,I,J)
 //   fu/gu   x faces [fx_base + i + (imax+1)*j][P][V], y faces [fy_base + i + imax*j][P][V]
 //           (FP32 in the FP32-mixed mode)
 //   lh      [cell][S*S][V]         subcell state of limited cells

@@ -43,7 +43,7 @@ __device__ __forceinline__ int find_inst_fy(const InstDesc* inst, int n, long lo
 
 template <int V, class R, class T>
 __device__ __forceinline__ void load_face_state(const R* qb, const R* fb, long long cell, int P, int l, int f, T* Q, T* F) {
-  const size_t o = (((size_t)cell * P + l) * 4 + f) * V;
+  const size_t o = (((size_t)cell * 4 + f) * P + l) * V;  // [cell][face][point][v]
 #pragma unroll
   for (int v = 0; v < V; ++v) {
     Q[v] = (T)qb[o + v];
@@ -95,7 +95,7 @@ __device__ void faces_euler_fp32(const BatchArgs& a, const FaceConst& fc, const 
   const int I = in.imax, J = in.jmax;
   auto cid = [&](int ci, int cj) { return in.cell_base + (long long)ci + (long long)I * cj; };
   auto load = [&](long long c, int f, float* Q, float* F) {
-    const size_t o = (((size_t)c * P + l) * 4 + f) * V;
+    const size_t o = (((size_t)c * 4 + f) * P + l) * V;
 #pragma unroll
     for (int v = 0; v < V; ++v) { Q[v] = qb[o + v]; F[v] = fb[o + v]; }
   };
@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(256) k_faces(BatchArgs a, FaceConst fc) {
     using CT = typename std::conditional<sizeof(R) == 4, float, double>::type;
     CT QL[1], QR[1], gL[2], gR[2];
     auto get = [&](long long c, int f, CT* Q, CT* gq) {
-      const size_t o = (((size_t)c * P + l) * 4 + f);
+      const size_t o = (((size_t)c * 4 + f) * P + l);
       Q[0] = (CT)qb[o];
       gq[0] = (CT)fb[o * 2 + 0];
       gq[1] = (CT)fb[o * 2 + 1];

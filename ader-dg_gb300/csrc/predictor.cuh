@@ -183,7 +183,7 @@ __device__ __forceinline__ void predictor_outputs(const BatchArgs& a, const DevO
   for (int idx = node; idx < 4 * P; idx += P2) {
     const int f = idx / P, l = idx - f * P;
     const R* c = (f == 0 || f == 2) ? op.FL : op.FR;
-    const size_t o = ((size_t)cell * P + l) * 4 + f;
+    const size_t o = ((size_t)cell * 4 + f) * P + l;  // [cell][face][point]
     const bool xdir = f < 2;
 #pragma unroll
     for (int v = 0; v < V; ++v) {
