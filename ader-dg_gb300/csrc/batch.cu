@@ -484,7 +484,9 @@ int badmit(aderdg_batch* b, const aderdg_config* cfg, const double* uh, const do
                                                 b->stream, &why);
       if (e != cudaSuccess) return bcuda(b, ("initial limiter: " + why).c_str(), e);
     }
-    r = bprime_one(b, pos);
+    // the limited cells' min/max from their subcell data; the others' and the
+    // CFL denominator (uh only) stay those of the first priming pass
+    r = bcells_one(b, pos, aderdg::kCellPrimeLimited, nullptr);
     if (r) return r;
   }
   // nothing waits for the GPU (the host mirror of the states is refreshed at

@@ -16,6 +16,9 @@
 //   kCellInitDmp initial limiter: DMP with argmax 0.1 against the cell's own
 //                nodal min/max; failing cells take the initial subcell data
 //   kCellCfl     CFL denominators of the current state only
+//   kCellPrimeLimited  kCellPrime for the limited cells only (their min/max
+//                come from Lh), no CFL: after the initial limiter, where the
+//                other cells' min/max and the CFL are those of kCellPrime
 #pragma once
 
 #include "common.cuh"
@@ -284,8 +287,9 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
   const int kc = valid ? k_found : 0;
   const InstDesc& in = a.inst[kc];
   const InstState& st = a.st[kc];
-  const bool priming = mode == kCellPrime || mode == kCellInitDmp || mode == kCellCfl;
-  const bool act = valid && (priming ? (a.only_inst < 0 || kc == a.only_inst) : st.active != 0);
+  const bool priming = mode == kCellPrime || mode == kCellInitDmp || mode == kCellCfl || mode == kCellPrimeLimited;
+  const bool act = valid && (priming ? (a.only_inst < 0 || kc == a.only_inst) : st.active != 0) &&
+                   (mode != kCellPrimeLimited || a.status[parity(st)][cell] != 0);
   if (!__syncthreads_or(act)) return;  // nothing to do in this CTA
   const int par = parity(st);
   const long long lcell = cell - in.cell_base;
@@ -461,7 +465,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
   }
 
   // ------------------------------------------------------------- CFL part
-  const bool want_cfl = mode != kCellInitDmp;
+  const bool want_cfl = mode != kCellInitDmp && mode != kCellPrimeLimited;
   // cells as aligned warp segments: per-cell maxima by shuffles, one store per
   // cell instead of P2 atomics on one shared address
   constexpr bool kSeg = (32 % P2) == 0 && (C::THREADS % 32) == 0 && C::CPB * P2 == C::THREADS;
@@ -490,7 +494,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
   if (want_dmp) {
     // Cells whose limiter is active keep their min/max from the subcell data
     // (get_min_max, Euler/limiter.f90:134-139) in the priming pass.
-    const bool from_lh = act && mode == kCellPrime && a.status[par][valid ? cell : 0] != 0;
+    const bool from_lh = act && (mode == kCellPrime || mode == kCellPrimeLimited) && a.status[par][valid ? cell : 0] != 0;
     bool f32red = false;  // the cell's partial min/max are in REDf (FP32)
     if constexpr (kFast) {
       if (act) {
@@ -616,7 +620,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
 #pragma unroll
         for (int k = 1; k < P2; ++k) { cmn = fmin(cmn, RED[v * P2 + k]); cmx = fmax(cmx, RED[(V + v) * P2 + k]); }
       }
-      if (mode == kCellPrime) {
+      if (mode == kCellPrime || mode == kCellPrimeLimited) {
         a.mm[par][(size_t)cell * 2 * V + v] = cmn;
         a.mm[par][(size_t)cell * 2 * V + V + v] = cmx;
       } else {
@@ -646,7 +650,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
       }
     }
     __syncthreads();
-    if (act && mode != kCellPrime) {
+    if (act && mode != kCellPrime && mode != kCellPrimeLimited) {
       const bool bad = cflag[lc] != 0;
       if (mode == kCellInitDmp) {
         if (bad) {

@@ -21,7 +21,8 @@ namespace aderdg {
 enum SysId { kSysAD = 0, kSysEuler = 1, kSysBN = 2 };
 
 // Modes of the cell kernel K3 (cells.cuh).
-enum CellMode { kCellFused = 0, kCellSurface = 1, kCellUpdate = 2, kCellPrime = 3, kCellInitDmp = 4, kCellCfl = 5 };
+enum CellMode { kCellFused = 0, kCellSurface = 1, kCellUpdate = 2, kCellPrime = 3, kCellInitDmp = 4, kCellCfl = 5,
+                kCellPrimeLimited = 6 };
 
 // Physical parameters of one instance.
 struct Phys {
