@@ -427,9 +427,12 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
     auto picard = [&](auto last_tag) {
       constexpr bool last = decltype(last_tag)::value;
 
+      // last iteration: the contraction is linear, so the time levels' fluxes
+      // are combined first (H = sum_l tw_l F_l) and contracted once
+      R Hx[V], Hy[V];
       if constexpr (last) {
 #pragma unroll
-        for (int v = 0; v < V; ++v) { Fh[0][v] = R(0); Fh[1][v] = R(0); }
+        for (int v = 0; v < V; ++v) { Fh[0][v] = R(0); Fh[1][v] = R(0); Hx[v] = R(0); Hy[v] = R(0); }
       }
 #pragma unroll
       for (int l = 0; l < P; ++l) {
@@ -440,15 +443,22 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
         } else {
           Sys::template pflux<R>(pc, q[l], Fx, Fy);
         }
-        vstore<R, V, VP>(cs + fidx(l, 0, 0), Fx);
-        vstore<R, V, VP>(cs + fidx(l, 1, 0), Fy);
-        if constexpr (last) {
+        if constexpr (!last) {
+          vstore<R, V, VP>(cs + fidx(l, 0, 0), Fx);
+          vstore<R, V, VP>(cs + fidx(l, 1, 0), Fy);
+        } else {
 #pragma unroll
           for (int v = 0; v < V; ++v) {
             Fh[0][v] = fma(op.w[l], Fx[v], Fh[0][v]);
             Fh[1][v] = fma(op.w[l], Fy[v], Fh[1][v]);
+            Hx[v] = fma(op.tw[l], Fx[v], Hx[v]);
+            Hy[v] = fma(op.tw[l], Fy[v], Hy[v]);
           }
         }
+      }
+      if constexpr (last) {
+        vstore<R, V, VP>(cs + fidx(0, 0, 0), Hx);
+        vstore<R, V, VP>(cs + fidx(0, 1, 0), Hy);
       }
       __syncthreads();
       if constexpr (!last) {
@@ -460,27 +470,46 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
 #pragma unroll
         for (int v = 0; v < V; ++v) { qh[v] = op.wg * u[v]; Sh[v] = R(0); }
       }
+      if constexpr (!last) {
 #pragma unroll
-      for (int l = 0; l < P; ++l) {
-        R b[V], ax, ay;
-        node_contract(l, b, ax, ay);
-        if constexpr (BN) {
-          R n[9];
-          BNSys::pncp<R>(pg[l], us[l], vs[l], ax, ay, n);
+        for (int l = 0; l < P; ++l) {
+          R b[V], ax, ay;
+          node_contract(l, b, ax, ay);
+          if constexpr (BN) {
+            R n[9];
+            BNSys::pncp<R>(pg[l], us[l], vs[l], ax, ay, n);
 #pragma unroll
-          for (int v = 0; v < V; ++v) {
-            b[v] = fma(rdt, n[v], b[v]);
-            if constexpr (last) Sh[v] = fma(-op.w[l], n[v], Sh[v]);
+            for (int v = 0; v < V; ++v) b[v] = fma(rdt, n[v], b[v]);
           }
-        }
-        if constexpr (!last) {
 #pragma unroll
           for (int lp = 0; lp < P; ++lp)
 #pragma unroll
             for (int v = 0; v < V; ++v) q[lp][v] = fma(-op.T[lp + P * l], b[v], q[lp][v]);
-        } else {
+        }
+      } else {
+        // qh = wg u - sum_l tw_l (D F_l + dt NCP_l) = wg u - D H - dt sum_l tw_l NCP_l
+        R b[V];
+        contract<C::VF, VP, P>(cs, 0, i, j, Dx, Dy, b);
 #pragma unroll
-          for (int v = 0; v < V; ++v) qh[v] = fma(-op.tw[l], b[v], qh[v]);
+        for (int v = 0; v < C::VF; ++v) qh[v] = qh[v] - b[v];
+        if constexpr (BN) {
+#pragma unroll
+          for (int l = 0; l < P; ++l) {
+            R ax = R(0), ay = R(0);
+#pragma unroll
+            for (int k = 0; k < P; ++k) {
+              ax = fma(Gx[k], as[l * P2 + k + P * j], ax);
+              ay = fma(Gy[k], as[l * P2 + i + P * k], ay);
+            }
+            R n[9];
+            BNSys::pncp<R>(pg[l], us[l], vs[l], ax, ay, n);
+            const R c = op.tw[l] * rdt;
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+              Sh[v] = fma(-op.w[l], n[v], Sh[v]);
+              qh[v] = fma(-c, n[v], qh[v]);
+            }
+          }
         }
       }
       __syncthreads();

@@ -109,7 +109,8 @@ def predictor_flops_per_cell(system, N, ad_fused=True):
         setup = 2 * P + 6
         it1 = cflux + contract + 3 * P * V
         mid = P * (cflux + contract + V + 2 * P * V)
-        last = P * (cflux + contract) + 2 * V * dot(P) + V * (1 + 2 * P)
+        # last: Fh and H = sum_l tw_l F_l accumulated, H contracted once, qh = wg u - D H
+        last = P * cflux + 4 * V * dot(P) + contract + 2 * V
         vol = V * (2 * dot(P) + 3)
         faces = 4 * P * V * 2 * dot(P)
     else:
@@ -120,7 +121,10 @@ def predictor_flops_per_cell(system, N, ad_fused=True):
         setup = 4 * P + 6
         it1 = cflux + contract + ncp + 3 * P * V
         mid = P * (cflux + contract + ncp + V + 2 * P * V)
-        last = P * (cflux + contract + ncp) + 2 * VF * dot(P) + VN * dot(P) + V * (1 + 2 * P)
+        # last: Fh and H, H contracted once, then per level the NCP term (grad alpha, NCP,
+        # tw_l dt, qh -= tw_l dt NCP_l) and Sh
+        last = (P * cflux + 4 * VF * dot(P) + contract + V + VF +
+                P * (2 * dot(P) + 9 + 1 + 2 * VN) + VN * dot(P))
         vol = (VF - 2) * (2 * dot(P) + 5) + 2 * (2 * dot(P) + 3) + 1
         faces = 4 * P * (V + VF) * dot(P)
     return P2 * (setup + it1 + mids * mid + last + vol) + faces

@@ -223,8 +223,10 @@ def predictor_cell(ops, system, N, u_nodes, dt, dx, dy, pc, fused):
             q[node] = [[g[l] * u[node][v] - ts[l] * b[v] for v in range(V)] for l in range(P)]
         for it in range(2, P + 1):
             last = it == P
+            H = [None] * P2
             for node in range(P2):
                 fh = [[ZERO] * V, [ZERO] * V]
+                hh = [[ZERO] * V, [ZERO] * V]
                 for l in range(P):
                     Fx, Fy, s = flux(pc, q[node][l])
                     F[l][0][node], F[l][1][node] = Fx, Fy
@@ -234,27 +236,38 @@ def predictor_cell(ops, system, N, u_nodes, dt, dx, dy, pc, fused):
                     if last:
                         fh = [[fma(w[l], Fx[v], fh[0][v]) for v in range(V)],
                               [fma(w[l], Fy[v], fh[1][v]) for v in range(V)]]
+                        hh = [[fma(tw[l], Fx[v], hh[0][v]) for v in range(V)],
+                              [fma(tw[l], Fy[v], hh[1][v]) for v in range(V)]]
                 if last:
                     Fh[0][node], Fh[1][node] = fh
+                    H[node] = hh
+            if last:
+                # the last iteration contracts the combined flux H = sum_l tw_l F_l once
+                for node in range(P2):
+                    F[0][0][node], F[0][1][node] = H[node]
             for node in range(P2):
                 if not last:
                     qn = [[g[l] * u[node][v] for v in range(V)] for l in range(P)]
+                    for l in range(P):
+                        b = contract(F, l, node)
+                        if BN:
+                            ax, ay = grad(A, l, node)
+                            n = bn_pncp(*ncp[l][node], ax, ay)
+                            b = [fma(dtc, n[v], b[v]) for v in range(V)]
+                        for lp in range(P):
+                            qn[lp] = [fma(-T[lp + P * l], b[v], qn[lp][v]) for v in range(V)]
                 else:
                     acc = [wg * u[node][v] for v in range(V)]
                     sh = [ZERO] * V
-                for l in range(P):
-                    b = contract(F, l, node)
+                    b = contract(F, 0, node)
+                    acc = [acc[v] - b[v] for v in range(V)]
                     if BN:
-                        ax, ay = grad(A, l, node)
-                        n = bn_pncp(*ncp[l][node], ax, ay)
-                        b = [fma(dtc, n[v], b[v]) for v in range(V)]
-                        if last:
+                        for l in range(P):
+                            ax, ay = grad(A, l, node)
+                            n = bn_pncp(*ncp[l][node], ax, ay)
+                            c = tw[l] * dtc
                             sh = [fma(-w[l], n[v], sh[v]) for v in range(V)]
-                    if not last:
-                        for lp in range(P):
-                            qn[lp] = [fma(-T[lp + P * l], b[v], qn[lp][v]) for v in range(V)]
-                    else:
-                        acc = [fma(-tw[l], b[v], acc[v]) for v in range(V)]
+                            acc = [fma(-c, n[v], acc[v]) for v in range(V)]
                 if not last:
                     q[node] = qn
                 else:
