@@ -328,6 +328,8 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
 #pragma unroll
       for (int l = 0; l < P; ++l) qs[l * P2 + node] = q[l][0];
       __syncthreads();
+      // last iteration: the time levels' fluxes combined (H = sum_l tw_l F_l) and contracted once
+      R hx = R(0), hy = R(0);
       if constexpr (last) { Fh[0][0] = Fh[1][0] = R(0); Gh[0] = Gh[1] = R(0); }
 #pragma unroll
       for (int l = 0; l < P; ++l) {
@@ -342,14 +344,21 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
           fx = fma(ccx, q[l][0], fx);
           fy = fma(ccy, q[l][0], fy);
         }
-        cs[fidx(l, 0, 0)] = fx;
-        cs[fidx(l, 1, 0)] = fy;
-        if constexpr (last) {
+        if constexpr (!last) {
+          cs[fidx(l, 0, 0)] = fx;
+          cs[fidx(l, 1, 0)] = fy;
+        } else {
           Fh[0][0] = fma(op.w[l], fx, Fh[0][0]);
           Fh[1][0] = fma(op.w[l], fy, Fh[1][0]);
           Gh[0] = fma(op.w[l], gx, Gh[0]);
           Gh[1] = fma(op.w[l], gy, Gh[1]);
+          hx = fma(op.tw[l], fx, hx);
+          hy = fma(op.tw[l], fy, hy);
         }
+      }
+      if constexpr (last) {
+        cs[fidx(0, 0, 0)] = hx;
+        cs[fidx(0, 1, 0)] = hy;
       }
       __syncthreads();
       if constexpr (!last) {
@@ -363,13 +372,9 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
           for (int lp = 0; lp < P; ++lp) q[lp][0] = fma(-op.T[lp + P * l], b[0], q[lp][0]);
         }
       } else {
-        qh[0] = op.wg * u[0];
-#pragma unroll
-        for (int l = 0; l < P; ++l) {
-          R b[1];
-          contract<1, VP, P>(cs, l, i, j, Dx, Dy, b);
-          qh[0] = fma(-op.tw[l], b[0], qh[0]);
-        }
+        R b[1];
+        contract<1, VP, P>(cs, 0, i, j, Dx, Dy, b);
+        qh[0] = op.wg * u[0] - b[0];
       }
       __syncthreads();
     };

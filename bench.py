@@ -100,7 +100,7 @@ def predictor_flops_per_cell(system, N, ad_fused=True):
         setup = 4 * P + 6             # Dx, Dy, Gx, Gy rows and scales, volume scales
         it1 = flux + contract + 3 * P  # q(l) = g u - ts b
         mid = P * (flux + 1 + contract + 2 * P)
-        last = P * flux + 4 * dot(P) + 1 + P * (contract + 2)
+        last = P * flux + 6 * dot(P) + contract + 2  # Fh, Gh, H; H contracted once
         vol = 2 * dot(P) + 3
         faces = 4 * P * 3 * dot(P)    # qbnd and the two gradQbnd components
     elif system == 1:

@@ -180,17 +180,24 @@ def predictor_cell(ops, system, N, u_nodes, dt, dx, dy, pc, fused):
             for node in range(P2):
                 for l in range(P):
                     A[l][node] = q[node][l][0]
+            H = [None] * P2
             for node in range(P2):
                 fh = [ZERO, ZERO]
                 gh = [ZERO, ZERO]
+                hh = [ZERO, ZERO]
                 for l in range(P):
                     gx, gy, fx, fy = ad_flux(l, node, q[node][l][0])
                     F[l][0][node], F[l][1][node] = [fx], [fy]
                     if last:
                         fh = [fma(w[l], fx, fh[0]), fma(w[l], fy, fh[1])]
                         gh = [fma(w[l], gx, gh[0]), fma(w[l], gy, gh[1])]
+                        hh = [fma(tw[l], fx, hh[0]), fma(tw[l], fy, hh[1])]
                 if last:
                     Fh[0][node], Fh[1][node], Gh[node] = [fh[0]], [fh[1]], gh
+                    H[node] = hh
+            if last:  # the combined flux H = sum_l tw_l F_l, contracted once
+                for node in range(P2):
+                    F[0][0][node], F[0][1][node] = [H[node][0]], [H[node][1]]
             for node in range(P2):
                 if not last:
                     qn = [[g[l] * u[node][0]] for l in range(P)]
@@ -200,11 +207,8 @@ def predictor_cell(ops, system, N, u_nodes, dt, dx, dy, pc, fused):
                             qn[lp][0] = fma(-T[lp + P * l], b[0], qn[lp][0])
                     q[node] = qn
                 else:
-                    acc = wg * u[node][0]
-                    for l in range(P):
-                        b = contract(F, l, node)
-                        acc = fma(-tw[l], b[0], acc)
-                    qh[node] = [acc]
+                    b = contract(F, 0, node)
+                    qh[node] = [wg * u[node][0] - b[0]]
     else:
         flux = bn_pflux if BN else euler_pflux
         ncp = [[None] * P2 for _ in range(P)]
