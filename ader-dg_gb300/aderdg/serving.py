@@ -105,6 +105,7 @@ class Server:
         pending = collections.deque(reqs)
         waiting = {g: collections.deque() for g in self.groups}
         running = {g: {} for g in self.groups}
+        inflight = {g: False for g in self.groups}  # a round of steps queued and not yet synced
         done = []
         t0 = time.perf_counter()
         clock = lambda: time.perf_counter() - t0  # noqa: E731
@@ -120,7 +121,6 @@ class Server:
             # admit in arrival order per group while there is room, and start the
             # group's steps before admitting into the next group, so that its
             # kernels overlap the next admissions
-            active = []
             for g, q in waiting.items():
                 b = self.groups[g]
                 while q:
@@ -143,9 +143,10 @@ class Server:
                     q.popleft()
                     r.slot, r.admitted = slot, clock()
                     running[g][slot] = r
-                if running[g]:
+                if running[g] and not inflight[g]:
                     b.launch(self.sync_every)
-                    active.append(g)
+                    inflight[g] = True
+            active = [g for g in self.groups if inflight[g]]
             if not active:
                 if pending:
                     time.sleep(max(0.0, min(pending[0].arrival - clock(), 0.01)))
@@ -155,6 +156,7 @@ class Server:
             for g in active:
                 b = self.groups[g]
                 b.sync()
+                inflight[g] = False
                 for slot in list(running[g]):
                     r = running[g][slot]
                     q = b.query(slot)
@@ -169,6 +171,11 @@ class Server:
                         b.release(slot)
                         del running[g][slot]
                         done.append(r)
+                # the group's next round right away (the GPU does not wait for the
+                # host's turn over the other groups), unless requests wait to join it
+                if running[g] and not waiting[g] and not (pending and pending[0].arrival <= clock()):
+                    b.launch(self.sync_every)
+                    inflight[g] = True
         makespan = clock()
         tts = np.array([r.finished - r.arrival for r in done])
         return {
