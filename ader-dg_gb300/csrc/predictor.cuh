@@ -42,11 +42,45 @@ struct PredCfg {
   static constexpr int VF = (Sys::ID == kSysBN && sizeof(R) == 4 && N <= 4) ? 8 : V;
   // FP32: pad to whole float4; FP64: double2 when VF is even
   static constexpr int VP = (VF == 1) ? 1 : (sizeof(R) == 4 ? ((VF + VEC - 1) / VEC) * VEC : VF);
-  // shared-memory elements per cell: flux buffer [P][2][P2][VP] (+ BN volume
-  // fraction [P][P2]; AD: flux [P][2][P2] + state [P][P2]), rounded to 16 bytes;
+  // Flux buffer layout.  FP64 and AD: [P][2][P2][VP], a node's variables
+  // contiguous.  FP32 Euler / Baer-Nunziato: each 16-byte chunk of the node
+  // vectors in a plane of its own, [chunk][P][2][P2] float4, so that the eight
+  // lanes of a quarter-warp (one 16-byte access each) address eight different
+  // bank groups; with the chunks interleaved, lanes j and j+1 of a row
+  // contraction met in the same group (2-way conflicts on Baer-Nunziato's
+  // stores and x contraction).  PC_PAD pads the planes and CE_PAD the cells
+  // (float4): the values that leave no conflict, or the fewest, in the
+  // stores and both contractions at this degree's cells-per-CTA.
+  static constexpr bool PLANAR = sizeof(R) == 4 && VF > 1;
+  static constexpr int NCH = PLANAR ? VP / 4 : 1;
+  // Row/column contraction (FP32 Euler / Baer-Nunziato, P >= 4): in the
+  // Picard iterations 2..N each thread also contracts one x row and one y
+  // column of one time level (the level its i names, the row / column its j
+  // names) in registers, in place, and the node's thread reads back the two
+  // contracted vectors per level: 8 P^2 accesses of 16 bytes per level and
+  // cell instead of (2P + 2) P^2 with every node reading its 2P neighbours.
+  // The x levels then the y levels, each level padded to XL / YL nodes; at
+  // P >= 5 the y pass takes level j and column i (the lanes of a quarter-warp
+  // then meet no bank group twice at these paddings).
+  static constexpr bool ROWCOL = PLANAR && P >= 4;
+  static constexpr int XL = ROWCOL ? P2 + ((P == 5) ? 0 : 1) : 2 * P2;  // nodes from x level to x level
+  static constexpr int YL = ROWCOL ? P2 + ((P == 5) ? 4 : 2) : 2 * P2;
+  static constexpr int Y0 = ROWCOL ? P * XL : P2;  // node offset of the y fluxes of level 0
+  static constexpr int PC_PAD = (PLANAR && !ROWCOL && Sys::ID == kSysBN) ? (P == 2 ? 1 : 0) : 0;
+  static constexpr int CE_PAD =
+      !PLANAR   ? 0
+      : ROWCOL  ? (P == 5 ? (Sys::ID == kSysBN ? 5 : 3) : (P == 6 && Sys::ID == kSysEuler) ? 2 : 0)
+                : (Sys::ID == kSysBN ? (P == 3 ? 1 : 0) : (P == 2 ? 4 : P == 3 ? 6 : 0));
+  static constexpr int PLANE = (ROWCOL ? Y0 + P * YL : 2 * P * P2) + PC_PAD;  // float4 per chunk plane
+  static constexpr int NS = PLANAR ? 4 : VP;            // elements from node to node
+  static constexpr int CS = PLANAR ? 4 * PLANE : VEC;   // elements from chunk to chunk of a node
+  static constexpr int FLUX_ELEMS = PLANAR ? 4 * NCH * PLANE : 2 * VP * P * P2;
+  // shared-memory elements per cell: flux buffer (+ BN volume fraction [P][P2];
+  // AD: flux [P][2][P2] + state [P][P2]), rounded to 16 bytes (+ CE_PAD);
   // the epilogue reuses it as [V][P2] x 3 (AD: x 5)
-  static constexpr int RAW = (Sys::ID == kSysAD) ? 3 * P * P2 : (2 * VP * P + (Sys::ID == kSysBN ? P : 0)) * P2;
-  static constexpr int CELL_ELEMS = ((RAW + VEC - 1) / VEC) * VEC;
+  static constexpr int RAW = (Sys::ID == kSysAD) ? 3 * P * P2 : FLUX_ELEMS + (Sys::ID == kSysBN ? P * P2 : 0);
+  static constexpr int CELL_ELEMS = ((RAW + VEC - 1) / VEC) * VEC + 4 * CE_PAD;
+  static_assert(CELL_ELEMS >= 3 * V * P2 && (Sys::ID != kSysAD || CELL_ELEMS >= 5 * P2), "epilogue layout");
   static constexpr int MAX_THREADS = 256;
   static constexpr int SMEM_BUDGET = 100 * 1024;
   static constexpr int CPB_T = MAX_THREADS / P2;
@@ -67,8 +101,9 @@ struct PredCfg {
   static constexpr int SMEM_BYTES = SLOTS * CELL_ELEMS * (int)sizeof(R);
 };
 
-// Loads the VP (padded) variables of one node with 16-byte vector loads.
-template <class R, int VP>
+// Loads the VP (padded) variables of one node with 16-byte vector loads;
+// chunk q of the node at p + q * CS.
+template <class R, int VP, int CS = 16 / (int)sizeof(R)>
 __device__ __forceinline__ void vload(const R* __restrict__ p, R* out) {
   if constexpr (VP % (16 / sizeof(R)) != 0) {
 #pragma unroll
@@ -76,22 +111,21 @@ __device__ __forceinline__ void vload(const R* __restrict__ p, R* out) {
   } else if constexpr (sizeof(R) == 4) {
 #pragma unroll
     for (int q = 0; q < VP / 4; ++q) {
-      const float4 t = reinterpret_cast<const float4*>(p)[q];
+      const float4 t = *reinterpret_cast<const float4*>(p + q * CS);
       out[4 * q] = t.x; out[4 * q + 1] = t.y; out[4 * q + 2] = t.z; out[4 * q + 3] = t.w;
     }
   } else {
 #pragma unroll
     for (int q = 0; q < VP / 2; ++q) {
-      const double2 t = reinterpret_cast<const double2*>(p)[q];
+      const double2 t = *reinterpret_cast<const double2*>(p + q * CS);
       out[2 * q] = t.x; out[2 * q + 1] = t.y;
     }
   }
 }
 
 // Stores V variables of one node as VP (padded) values with 16-byte vector
-// stores where VP allows (one vector per 4 floats / 2 doubles: no bank
-// conflicts between the lanes of a warp).
-template <class R, int V, int VP>
+// stores where VP allows; chunk q of the node at p + q * CS.
+template <class R, int V, int VP, int CS = 16 / (int)sizeof(R)>
 __device__ __forceinline__ void vstore(R* __restrict__ p, const R* in) {
   if constexpr (VP % (16 / sizeof(R)) != 0) {
 #pragma unroll
@@ -104,7 +138,7 @@ __device__ __forceinline__ void vstore(R* __restrict__ p, const R* in) {
       t.y = 4 * q + 1 < V ? in[4 * q + 1] : 0.0f;
       t.z = 4 * q + 2 < V ? in[4 * q + 2] : 0.0f;
       t.w = 4 * q + 3 < V ? in[4 * q + 3] : 0.0f;
-      reinterpret_cast<float4*>(p)[q] = t;
+      *reinterpret_cast<float4*>(p + q * CS) = t;
     }
   } else {
 #pragma unroll
@@ -112,32 +146,70 @@ __device__ __forceinline__ void vstore(R* __restrict__ p, const R* in) {
       double2 t;
       t.x = 2 * q + 0 < V ? in[2 * q + 0] : 0.0;
       t.y = 2 * q + 1 < V ? in[2 * q + 1] : 0.0;
-      reinterpret_cast<double2*>(p)[q] = t;
+      *reinterpret_cast<double2*>(p + q * CS) = t;
     }
   }
 }
 
-// Flux-derivative contraction of time level l into b[v]; flux buffer [P][2][P2][VP].
-template <int V, int VP, int P, class R>
+// Flux-derivative contraction of time level l into b[v]; the x fluxes of
+// level l start at node l*XL, the y fluxes at node Y0 + l*YL, nodes NS
+// elements apart, a node's chunks CS elements apart (default: [P][2][P2]).
+template <int V, int VP, int P, class R, int NS = VP, int CS = 16 / (int)sizeof(R), int XL = 2 * P * P,
+          int YL = 2 * P * P, int Y0 = P * P>
 __device__ __forceinline__ void contract(const R* __restrict__ cs, int l, int i, int j, const R* Dx, const R* Dy, R* b) {
-  constexpr int P2 = P * P;
-  const R* fx = cs + (size_t)(l * 2 + 0) * P2 * VP;
-  const R* fy = cs + (size_t)(l * 2 + 1) * P2 * VP;
+  const R* fx = cs + (size_t)l * XL * NS;
+  const R* fy = cs + ((size_t)Y0 + (size_t)l * YL) * NS;
 #pragma unroll
   for (int v = 0; v < V; ++v) b[v] = R(0);
 #pragma unroll
   for (int k = 0; k < P; ++k) {
     R f[VP];
-    vload<R, VP>(fx + (k + P * j) * VP, f);
+    vload<R, VP, CS>(fx + (k + P * j) * NS, f);
 #pragma unroll
     for (int v = 0; v < V; ++v) b[v] = fma(Dx[k], f[v], b[v]);
   }
 #pragma unroll
   for (int k = 0; k < P; ++k) {
     R f[VP];
-    vload<R, VP>(fy + (i + P * k) * VP, f);
+    vload<R, VP, CS>(fy + (i + P * k) * NS, f);
 #pragma unroll
     for (int v = 0; v < V; ++v) b[v] = fma(Dy[k], f[v], b[v]);
+  }
+}
+
+// Row/column pass of the Picard iterations 2..N (PredCfg::ROWCOL): the
+// thread of node (i, j) contracts x row j of time level i and y column c of
+// time level m in place (c = j, m = i for P = 4; c = i, m = j above),
+// X(o, j) <- sum_k Kxi(k, o) X(k, j) and Y(c, o) <- sum_k Kxi(k, o) Y(c, k),
+// each 16-byte chunk loaded once for all P outputs; the node's thread applies
+// dt/(dx w_i), dt/(dy w_j) when it reads the results back.
+template <class C, class Ops>
+__device__ __forceinline__ void rowcol_pass(float* __restrict__ cs, int i, int j, const Ops& op) {
+  constexpr int P = C::P;
+  auto line = [&](float* p, int stride) {
+    float4 f[P];
+#pragma unroll
+    for (int k = 0; k < P; ++k) f[k] = *reinterpret_cast<const float4*>(p + k * stride);
+#pragma unroll
+    for (int o = 0; o < P; ++o) {
+      const float m0 = op.Kxi[P * o];
+      float4 s = make_float4(m0 * f[0].x, m0 * f[0].y, m0 * f[0].z, m0 * f[0].w);
+#pragma unroll
+      for (int k = 1; k < P; ++k) {
+        const float m = op.Kxi[k + P * o];
+        s.x = fmaf(m, f[k].x, s.x);
+        s.y = fmaf(m, f[k].y, s.y);
+        s.z = fmaf(m, f[k].z, s.z);
+        s.w = fmaf(m, f[k].w, s.w);
+      }
+      *reinterpret_cast<float4*>(p + o * stride) = s;
+    }
+  };
+#pragma unroll
+  for (int c = 0; c < C::NCH; ++c) {
+    line(cs + c * C::CS + ((size_t)i * C::XL + P * j) * 4, 4);
+    const int m = P >= 5 ? j : i, col = P >= 5 ? i : j;
+    line(cs + c * C::CS + ((size_t)C::Y0 + (size_t)m * C::YL + col) * 4, 4 * P);
   }
 }
 
@@ -242,9 +314,10 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
 
   // per-thread contraction rows: Dx(i,k) = Kxi(k,i) dt/(dx w_i), Dy(j,k) likewise
   R Dx[P], Dy[P], Gx[P], Gy[P];
+  R cxw, cyw;  // dt/(dx w_i), dt/(dy w_j)
   {
     // FP32: the reciprocals 1/dx, 1/dy held in FP32 (no FP64 divisions per thread)
-    R idx, idy, cxw, cyw;
+    R idx, idy;
     if constexpr (sizeof(R) == 4) {
       idx = in.idxf;
       idy = in.idyf;
@@ -286,7 +359,9 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
   R Gh[2];      // AD: time-averaged gradient of the last iteration
   R qh[V];      // time-averaged state
 
-  auto fidx = [&](int l, int d, int v) { return ((size_t)(l * 2 + d) * P2 + node) * VP + v; };
+  auto fidx = [&](int l, int d, int v) {
+    return ((d == 0 ? (size_t)l * C::XL : (size_t)C::Y0 + (size_t)l * C::YL) + node) * C::NS + v;
+  };
 
   if constexpr (Sys::ID == kSysAD) {
     // -------------------------------------------------------------- AD
@@ -384,11 +459,30 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
   } else {
     // ------------------------------------------------- Euler / Baer-Nunziato
     constexpr bool BN = Sys::ID == kSysBN;
-    R* as = cs + (size_t)2 * VP * P * P2;  // BN volume fraction [P][P2]
+    R* as = cs + C::FLUX_ELEMS;            // BN volume fraction [P][P2]
     R pg[P], us[P], vs[P];                // BN: NCP scalars per time level
     // contraction of level l at this node: b = sum_k Dx Fx + sum_k Dy Fy (+ BN: ax, ay)
     auto node_contract = [&](int l, R* b, R& ax, R& ay) {
-      contract<C::VF, VP, P>(cs, l, i, j, Dx, Dy, b);
+      contract<C::VF, VP, P, R, C::NS, C::CS, C::XL, C::YL, C::Y0>(cs, l, i, j, Dx, Dy, b);
+      if constexpr (BN) {
+        ax = R(0);
+        ay = R(0);
+#pragma unroll
+        for (int k = 0; k < P; ++k) {
+          ax = fma(Gx[k], as[l * P2 + k + P * j], ax);
+          ay = fma(Gy[k], as[l * P2 + i + P * k], ay);
+        }
+      }
+#pragma unroll
+      for (int v = C::VF; v < V; ++v) b[v] = R(0);
+    };
+    // the same b from the row/column pass's results (PredCfg::ROWCOL)
+    auto node_gather = [&](int l, R* b, R& ax, R& ay) {
+      R bx[VP], by[VP];
+      vload<R, VP, C::CS>(cs + fidx(l, 0, 0), bx);
+      vload<R, VP, C::CS>(cs + fidx(l, 1, 0), by);
+#pragma unroll
+      for (int v = 0; v < C::VF; ++v) b[v] = fma(cxw, bx[v], cyw * by[v]);
       if constexpr (BN) {
         ax = R(0);
         ay = R(0);
@@ -410,8 +504,8 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
       } else {
         Sys::template pflux<R>(pc, u, Fx, Fy);
       }
-      vstore<R, V, VP>(cs + fidx(0, 0, 0), Fx);
-      vstore<R, V, VP>(cs + fidx(0, 1, 0), Fy);
+      vstore<R, V, VP, C::CS>(cs + fidx(0, 0, 0), Fx);
+      vstore<R, V, VP, C::CS>(cs + fidx(0, 1, 0), Fy);
       __syncthreads();
       R b[V], ax, ay;
       node_contract(0, b, ax, ay);
@@ -449,8 +543,8 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
           Sys::template pflux<R>(pc, q[l], Fx, Fy);
         }
         if constexpr (!last) {
-          vstore<R, V, VP>(cs + fidx(l, 0, 0), Fx);
-          vstore<R, V, VP>(cs + fidx(l, 1, 0), Fy);
+          vstore<R, V, VP, C::CS>(cs + fidx(l, 0, 0), Fx);
+          vstore<R, V, VP, C::CS>(cs + fidx(l, 1, 0), Fy);
         } else {
 #pragma unroll
           for (int v = 0; v < V; ++v) {
@@ -462,11 +556,15 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
         }
       }
       if constexpr (last) {
-        vstore<R, V, VP>(cs + fidx(0, 0, 0), Hx);
-        vstore<R, V, VP>(cs + fidx(0, 1, 0), Hy);
+        vstore<R, V, VP, C::CS>(cs + fidx(0, 0, 0), Hx);
+        vstore<R, V, VP, C::CS>(cs + fidx(0, 1, 0), Hy);
       }
       __syncthreads();
       if constexpr (!last) {
+        if constexpr (C::ROWCOL) {
+          rowcol_pass<C>(cs, i, j, op);
+          __syncthreads();
+        }
 #pragma unroll
         for (int l = 0; l < P; ++l)
 #pragma unroll
@@ -479,7 +577,10 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
 #pragma unroll
         for (int l = 0; l < P; ++l) {
           R b[V], ax, ay;
-          node_contract(l, b, ax, ay);
+          if constexpr (C::ROWCOL)
+            node_gather(l, b, ax, ay);
+          else
+            node_contract(l, b, ax, ay);
           if constexpr (BN) {
             R n[9];
             BNSys::pncp<R>(pg[l], us[l], vs[l], ax, ay, n);
@@ -494,7 +595,7 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
       } else {
         // qh = wg u - sum_l tw_l (D F_l + dt NCP_l) = wg u - D H - dt sum_l tw_l NCP_l
         R b[V];
-        contract<C::VF, VP, P>(cs, 0, i, j, Dx, Dy, b);
+        contract<C::VF, VP, P, R, C::NS, C::CS, C::XL, C::YL, C::Y0>(cs, 0, i, j, Dx, Dy, b);
 #pragma unroll
         for (int v = 0; v < C::VF; ++v) qh[v] = qh[v] - b[v];
         if constexpr (BN) {
