@@ -243,7 +243,13 @@ __device__ __forceinline__ unsigned long long seg_max(unsigned long long x) {
 template <class Sys, int N>
 struct CellCfg {
   static constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1, V = Sys::V;
-  static constexpr int CPB = (256 / P2) < 1 ? 1 : (256 / P2);
+  // small CTAs (the kernel waits on latency and barriers: smaller CTAs, more
+  // of them per SM, wait on fewer warps per barrier): 64 threads up to N = 3,
+  // 128 at N = 4 and 256 at N = 5, where the 25- and 36-thread cells fill
+  // smaller CTAs badly (measured: BN cylinder 0.559 -> 0.508 -> 0.487 ms,
+  // Riemann problem 0.344 -> 0.330 -> 0.324 ms for 256 -> 128 -> 64 threads)
+  static constexpr int CTA = N == 5 ? 256 : N == 4 ? 128 : 64;
+  static constexpr int CPB = (CTA / P2) < 1 ? 1 : (CTA / P2);
   static constexpr int THREADS = ((CPB * P2 + 31) / 32) * 32;
   // per cell: U [V][P2], LY [V][S][P], LB [V][P][P], red [2][V][P2] (FP64);
   // FP32-mixed: U64 [V][P2] then FP32 U [V][P2], LY, LB, red, |U| max [V]
@@ -253,11 +259,11 @@ struct CellCfg {
   static constexpr int OPS_DBL = S * P + P * P;  // uh2lim, uh2lob (FP64, then FP32 in the mixed mode)
   static constexpr int SMEM_BYTES = CPB * CELL_DBL * 8 + OPS_DBL * 12 + CPB * 8 /*cell max*/ + CPB * 4 /*flags*/ +
                                     CPB * V * 4 /*|U| max*/ + CPB * V * 4 /*FP32 reference state*/ + 16;
-  // blocks per SM the register allocation aims at: Euler's FP32-mixed cell
-  // kernel is latency-bound and gains from a fourth block; the other
-  // variants keep the allocation they reach unconstrained
+  // blocks per SM the register allocation aims at, in 256-thread units:
+  // Euler's FP32-mixed cell kernel is latency-bound and gains from a fourth;
+  // the other variants keep the allocation they reach unconstrained
   static constexpr int min_blocks(bool fast) {
-    return Sys::ID == kSysEuler ? (fast ? 4 : 3) : (Sys::ID == kSysBN ? 2 : 4);
+    return (Sys::ID == kSysEuler ? (fast ? 4 : 3) : (Sys::ID == kSysBN ? 2 : 4)) * (256 / CTA);
   }
 };
 
