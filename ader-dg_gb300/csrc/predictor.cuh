@@ -81,7 +81,10 @@ struct PredCfg {
   static constexpr int RAW = (Sys::ID == kSysAD) ? 3 * P * P2 : FLUX_ELEMS + (Sys::ID == kSysBN ? P * P2 : 0);
   static constexpr int CELL_ELEMS = ((RAW + VEC - 1) / VEC) * VEC + 4 * CE_PAD;
   static_assert(CELL_ELEMS >= 3 * V * P2 && (Sys::ID != kSysAD || CELL_ELEMS >= 5 * P2), "epilogue layout");
-  static constexpr int MAX_THREADS = 256;
+  // FP32 up to N = 4: CTAs of at most 128 threads, twice as many per SM (each
+  // Picard iteration's barriers then wait on fewer warps); N = 5 keeps 256,
+  // whose 36-thread cells fill 128 badly; FP64 is pipe-bound either way
+  static constexpr int MAX_THREADS = (sizeof(R) == 4 && N <= 4) ? 128 : 256;
   static constexpr int SMEM_BUDGET = 100 * 1024;
   static constexpr int CPB_T = MAX_THREADS / P2;
   static constexpr int CPB_S = SMEM_BUDGET / (CELL_ELEMS * (int)sizeof(R));
@@ -92,8 +95,8 @@ struct PredCfg {
   // contractions; Baer-Nunziato's time column does not fit in fewer
   // registers without spilling at N >= 3); FP64 is pipe-bound either way
   static constexpr int MIN_BLOCKS =
-      (sizeof(R) == 4 && THREADS > 128)
-          ? (Sys::ID == kSysAD ? 4 : Sys::ID == kSysEuler ? (N <= 3 ? 4 : 3) : (N <= 2 ? 3 : 2))
+      (sizeof(R) == 4 && THREADS > 64)
+          ? (Sys::ID == kSysAD ? 4 : Sys::ID == kSysEuler ? (N <= 3 ? 4 : 3) : (N <= 2 ? 3 : 2)) * (256 / MAX_THREADS)
           : 1;
   // threads past CPB*P2 (the tail of the last warp) take part in the barriers
   // and get a scratch slot of their own so they never touch a real cell's data

@@ -375,7 +375,7 @@ def run_mix(args, aderdg, dist, rank, ws, lr):
             "launch_ms": pred_ms, "dominant_phase": dominant,
             "phase_share": {k: v / sum(kern_ms.values()) for k, v in kern_ms.items()},
             "phase_ms_one_step": phase_tot, "traffic": None,
-            "limiter": ("FP32: shared-memory wavefronts of the flux contractions (73% of peak, FP32 pipe 43%, in the "
+            "limiter": ("FP32: shared-memory wavefronts of the flux contractions (79% of peak, FP32 pipe 46%, in the "
                         "ncu capture of profiles/k_predictor_k_cells_euler_vortex_256_N4.md); FP64: the FP64 pipe"
                         if mixed else "the FP64 pipe (90% busy in profiles/k_predictor_k_cells_euler_vortex_256_N4.md)")}
     try:

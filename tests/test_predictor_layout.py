@@ -42,7 +42,7 @@ def pred_cfg(system, N):
     flux = 4 * NCH * PLANE                     # floats
     raw = flux + (P * P2 if system == BN else 0)
     cell = (raw + 3) // 4 * 4 + 4 * CE         # floats
-    cpb = max(1, min(256 // P2, (100 * 1024) // (cell * 4)))
+    cpb = max(1, min((128 if N <= 4 else 256) // P2, (100 * 1024) // (cell * 4)))
     threads = (cpb * P2 + 31) // 32 * 32
     return dict(P=P, P2=P2, V=V, NCH=NCH, rowcol=rowcol, XL=XL, YL=YL, Y0=Y0, PLANE=PLANE, CELL4=cell // 4,
                 cell=cell, flux=flux, cpb=cpb, threads=threads)
