@@ -16,7 +16,10 @@ from . import builder as _build
 
 SYS_ADVDIFF, SYS_EULER, SYS_BN = 0, 1, 2
 NVAR = {SYS_ADVDIFF: 1, SYS_EULER: 4, SYS_BN: 9}
-FP64, FP32_MIXED = 0, 1
+# precision modes (aderdg_precision): FP64 throughout; FP32 contractions with
+# the FP64 split of the mixed mode; FP32-wide (faster, FP32 BN faces and subcell
+# re-solve, uncertified DMP comparisons)
+FP64, FP32_MIXED, FP32_WIDE = 0, 1, 2
 
 (A_UH, A_DUH, A_QHI, A_FHI, A_SHI, A_QBND, A_FBND, A_GRADQBND, A_FU, A_GU, A_FP, A_GP, A_LH, A_LMIN,
  A_LMAX, A_RECOMPUTE, A_STATUS) = range(17)
@@ -50,7 +53,7 @@ class _Config(ctypes.Structure):
 class _Info(ctypes.Structure):
     _fields_ = [("cells", ctypes.c_long), ("dofs", ctypes.c_long), ("device_bytes", ctypes.c_long),
                 ("steps", ctypes.c_long), ("time", ctypes.c_double), ("dt", ctypes.c_double),
-                ("n_recompute", ctypes.c_int), ("n_limited", ctypes.c_int)]
+                ("n_recompute", ctypes.c_int), ("n_limited", ctypes.c_int), ("n_settled", ctypes.c_int)]
 
 
 @dataclasses.dataclass
@@ -332,6 +335,13 @@ class Solver:
         st = np.ascontiguousarray(status, dtype=np.int32).ravel()
         lh = np.ascontiguousarray(lh, dtype=np.float64).ravel()
         self._ck(self.L.aderdg_upload_limiter(self.h, _ip(st), _dp(lh)))
+
+    def download_limiter(self):
+        """(status per cell, Lh(nVar, 2N+1, 2N+1, IMAX, JMAX)) of the current state."""
+        st = np.empty(self.cfg.cells, dtype=np.int32)
+        lh = np.empty(self.cfg.cells * self.cfg.S * self.cfg.S * self.cfg.nvar, dtype=np.float64)
+        self._ck(self.L.aderdg_download_limiter(self.h, _ip(st), _dp(lh)))
+        return st, lh
 
     def download(self):
         uh = np.empty(self.cfg.dofs, dtype=np.float64)

@@ -23,7 +23,8 @@ struct aderdg_ctx {
   aderdg_config cfg{};
   int V = 0, P = 0, S = 0;
   long long ncells = 0, nfx = 0, nfy = 0;
-  bool limiter = false, fp32 = false;
+  bool limiter = false, fp32 = false;  // fp32: FP32 predictor and intermediates (both FP32 modes)
+  int prec = ADERDG_FP64;
   aderdg::HostOps ops;
   std::vector<unsigned char> ops64, ops32;
   const KernelTable* kt = nullptr;
@@ -94,7 +95,8 @@ int validate(const aderdg_config* c, std::string* why) {
   if ((long long)c->imax * c->jmax > (1ll << 31) / 64) return *why = "grid too large", ADERDG_EINVAL;
   if (!(c->xr[0] > c->xl[0]) || !(c->xr[1] > c->xl[1])) return *why = "empty domain", ADERDG_EINVAL;
   if (!(c->cfl > 0.0)) return *why = "cfl must be positive", ADERDG_EINVAL;
-  if (c->precision != ADERDG_FP64 && c->precision != ADERDG_FP32_MIXED) return *why = "bad precision", ADERDG_EINVAL;
+  if (c->precision != ADERDG_FP64 && c->precision != ADERDG_FP32_MIXED && c->precision != ADERDG_FP32_WIDE)
+    return *why = "bad precision", ADERDG_EINVAL;
   if (c->bc_mode != 0 && !(c->bc_mode == 1 && c->system == ADERDG_SYS_EULER))
     return *why = "bc_mode 1 (double Mach reflection) is Euler only", ADERDG_EINVAL;
   for (int s = 0; s < 4; ++s) {
@@ -154,12 +156,12 @@ int set_clock(aderdg_ctx* c, double time, double tend) {
 int launch_step(aderdg_ctx* c) {
   CK(c, control(c, aderdg::kCtlBegin));
   CK(c, c->kt->predictor(c->args, pred_ops(c), c->fp32 ? 1 : 0, false, c->stream));
-  CK(c, c->kt->faces(c->args, c->fc, c->fp32 ? 1 : 0, c->stream));
+  CK(c, aderdg::launch_faces(c->kt, c->args, c->fc, c->prec, c->stream));
   int r = cells(c, aderdg::kCellFused);
   if (r) return r;
   if (c->limiter) {
     CK(c, c->kt->mark(c->args, c->stream));
-    CK(c, c->kt->subcell(c->args, c->ops64.data(), c->fc, c->subcell_grid, c->fp32, c->stream));
+    CK(c, c->kt->subcell(c->args, c->ops64.data(), c->fc, c->subcell_grid, aderdg::subcell_fp32(c->prec), c->stream));
   }
   CK(c, control(c, aderdg::kCtlEnd));
   return ADERDG_OK;
@@ -296,7 +298,8 @@ int aderdg_create(const aderdg_config* cfg, aderdg_ctx** out) {
   c->nfx = (long long)(cfg->imax + 1) * cfg->jmax;
   c->nfy = (long long)cfg->imax * (cfg->jmax + 1);
   c->limiter = cfg->limiter != 0 && cfg->system != ADERDG_SYS_ADVDIFF;
-  c->fp32 = cfg->precision == ADERDG_FP32_MIXED;
+  c->fp32 = cfg->precision != ADERDG_FP64;
+  c->prec = cfg->precision;
   if (!aderdg::build_ops(cfg->N, c->ops, &why)) {
     delete c;
     return fail(nullptr, ADERDG_EINVAL, why);
@@ -346,6 +349,8 @@ int aderdg_create(const aderdg_config* cfg, aderdg_ctx** out) {
     if (!r) r = dalloc(c, &a.lh[1], nc * S * S * V);
     if (!r) r = dalloc(c, &a.mm[0], nc * 2 * V);
     if (!r) r = dalloc(c, &a.mm[1], nc * 2 * V);
+    if (!r && c->prec == ADERDG_FP32_MIXED) r = dalloc(c, &a.mme[0], nc * V);
+    if (!r && c->prec == ADERDG_FP32_MIXED) r = dalloc(c, &a.mme[1], nc * V);
     if (!r) r = dalloc(c, &a.lminmax, nc * 2 * V);
     if (!r) r = dalloc(c, &a.troubled, nc);
     if (!r) r = dalloc(c, &a.recompute, nc);
@@ -376,7 +381,7 @@ int aderdg_create(const aderdg_config* cfg, aderdg_ctx** out) {
     c->ops32.assign(kt->ops32_size, 0);
     kt->make_ops32(c->ops, c->ops32.data());
   }
-  if (c->limiter) c->subcell_grid = kt->subcell_grid(c->num_sms, c->fp32);
+  if (c->limiter) c->subcell_grid = kt->subcell_grid(c->num_sms, aderdg::subcell_fp32(c->prec));
   // set kernel attributes now, outside any later stream capture
   {
     BatchArgs z = a;
@@ -613,7 +618,7 @@ int aderdg_volume_integral(aderdg_ctx* c) {
 
 int aderdg_riemann_problem(aderdg_ctx* c) {
   if (!c) return fail(c, ADERDG_EINVAL, "null context");
-  CK(c, c->kt->faces(c->args, c->fc, c->fp32 ? 1 : 0, c->stream));
+  CK(c, aderdg::launch_faces(c->kt, c->args, c->fc, c->prec, c->stream));
   return ADERDG_OK;
 }
 
@@ -643,7 +648,7 @@ int aderdg_limiter(aderdg_ctx* c) {
   if (!c->pending) return fail(c, ADERDG_ESTATE, "run aderdg_element_update first");
   CK(c, cudaMemsetAsync(c->args.list_count, 0, sizeof(int), c->stream));
   CK(c, c->kt->mark(c->args, c->stream));
-  CK(c, c->kt->subcell(c->args, c->ops64.data(), c->fc, c->subcell_grid, c->fp32, c->stream));
+  CK(c, c->kt->subcell(c->args, c->ops64.data(), c->fc, c->subcell_grid, aderdg::subcell_fp32(c->prec), c->stream));
   CK(c, control(c, aderdg::kCtlEnd));
   c->pending = false;
   return pull_state(c);
@@ -769,14 +774,15 @@ int aderdg_profile_step(aderdg_ctx* c, double* time, double tend, double* phase_
   CK(c, cudaEventRecord(ev[1], c->stream));
   CK(c, c->kt->predictor(c->args, pred_ops(c), c->fp32 ? 1 : 0, false, c->stream));
   CK(c, cudaEventRecord(ev[2], c->stream));
-  CK(c, c->kt->faces(c->args, c->fc, c->fp32 ? 1 : 0, c->stream));
+  CK(c, aderdg::launch_faces(c->kt, c->args, c->fc, c->prec, c->stream));
   CK(c, cudaEventRecord(ev[3], c->stream));
   r = cells(c, aderdg::kCellFused);
   if (r) return r;
   CK(c, cudaEventRecord(ev[4], c->stream));
   if (c->limiter) CK(c, c->kt->mark(c->args, c->stream));
   CK(c, cudaEventRecord(ev[5], c->stream));
-  if (c->limiter) CK(c, c->kt->subcell(c->args, c->ops64.data(), c->fc, c->subcell_grid, c->fp32, c->stream));
+  if (c->limiter)
+    CK(c, c->kt->subcell(c->args, c->ops64.data(), c->fc, c->subcell_grid, aderdg::subcell_fp32(c->prec), c->stream));
   CK(c, cudaEventRecord(ev[6], c->stream));
   CK(c, control(c, aderdg::kCtlEnd));
   CK(c, cudaEventRecord(ev[7], c->stream));
@@ -957,6 +963,7 @@ int aderdg_get_info(aderdg_ctx* c, aderdg_info* info) {
   info->time = c->h_st->time;
   info->dt = c->h_st->dt;
   info->n_recompute = c->h_st->n_recompute;
+  info->n_settled = c->h_st->n_settled;
   info->n_limited = 0;
   if (c->limiter) {
     std::vector<int> st((size_t)c->ncells);

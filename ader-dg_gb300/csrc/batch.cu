@@ -91,12 +91,14 @@ int nvar(int sys) { return sys == ADERDG_SYS_ADVDIFF ? 1 : sys == ADERDG_SYS_EUL
 // bytes per unit of every per-cell array of a batch
 long long unit_bytes(int system, int N, int precision, int limiter) {
   const long long V = nvar(system), P = N + 1, S = 2 * N + 1;
-  const long long rb = precision == ADERDG_FP32_MIXED ? 4 : 8;
+  const long long rb = precision != ADERDG_FP64 ? 4 : 8;
   long long b = 8 * V * P * P * 2 + rb * V * P * P;                 // uh[2], duh
   b += rb * P * 4 * V * (system == ADERDG_SYS_ADVDIFF ? 3 : 2);     // qbnd, fbnd / gradQbnd
   b += rb * P * V * (system == ADERDG_SYS_BN ? 4 : 2);              // face fluxes
-  if (limiter && system != ADERDG_SYS_ADVDIFF)
+  if (limiter && system != ADERDG_SYS_ADVDIFF) {
     b += 8 * V * S * S * 2 + 4 * 2 + 8 * 2 * V * 2 + 1 + 4 + 4 + 8;  // Lh[2], status[2], mm[2], flags, list, denom
+    if (precision == ADERDG_FP32_MIXED) b += 4 * V * 2;               // mme[2]
+  }
   return b;
 }
 
@@ -205,11 +207,11 @@ int blaunch_step(aderdg_batch* b) {
   const int fp32 = b->precision ? 1 : 0;
   BK(b, bcontrol(b, aderdg::kCtlBegin, -1));
   BK(b, b->kt->predictor(a, bpred_ops(b), fp32, false, b->stream));
-  BK(b, b->kt->faces(a, b->fc, fp32, b->stream));
+  BK(b, aderdg::launch_faces(b->kt, a, b->fc, b->precision, b->stream));
   BK(b, b->kt->cells(a, b->ops64.data(), fp32, b->stream));
   if (b->limiter) {
     BK(b, b->kt->mark(a, b->stream));
-    BK(b, b->kt->subcell(a, b->ops64.data(), b->fc, b->subcell_grid, b->precision ? 1 : 0, b->stream));
+    BK(b, b->kt->subcell(a, b->ops64.data(), b->fc, b->subcell_grid, aderdg::subcell_fp32(b->precision), b->stream));
   }
   BK(b, bcontrol(b, aderdg::kCtlEnd, -1));
   return ADERDG_OK;
@@ -280,7 +282,7 @@ int aderdg_batch_create(int system, int N, int precision, int limiter, long capa
   if (!out) return bfail(nullptr, ADERDG_EINVAL, "null output pointer");
   *out = nullptr;
   if (system < 0 || system > 2 || N < 1 || N > 5 || capacity_units < 4 || max_instances < 1 ||
-      (precision != ADERDG_FP64 && precision != ADERDG_FP32_MIXED))
+      (precision != ADERDG_FP64 && precision != ADERDG_FP32_MIXED && precision != ADERDG_FP32_WIDE))
     return bfail(nullptr, ADERDG_EINVAL, "bad batch parameters");
   const aderdg::KernelTable* kt = aderdg::kernel_table(system, N);
   if (!kt) return bfail(nullptr, ADERDG_EUNSUPPORTED, "no kernels built for this (system, N)");
@@ -340,6 +342,8 @@ int aderdg_batch_create(int system, int N, int precision, int limiter, long capa
     if (!r) r = balloc(b, &a.lh[1], U * S * S * V);
     if (!r) r = balloc(b, &a.mm[0], U * 2 * V);
     if (!r) r = balloc(b, &a.mm[1], U * 2 * V);
+    if (!r && precision == ADERDG_FP32_MIXED) r = balloc(b, &a.mme[0], U * V);
+    if (!r && precision == ADERDG_FP32_MIXED) r = balloc(b, &a.mme[1], U * V);
     // no lminmax: the neighbourhood bounds are an introspection output of
     // the single-simulation API only
     if (!r) r = balloc(b, &a.troubled, U);
@@ -367,7 +371,7 @@ int aderdg_batch_create(int system, int N, int precision, int limiter, long capa
     b->ops32.assign(kt->ops32_size, 0);
     kt->make_ops32(b->ops, b->ops32.data());
   }
-  if (b->limiter) b->subcell_grid = kt->subcell_grid(b->num_sms, b->precision ? 1 : 0);
+  if (b->limiter) b->subcell_grid = kt->subcell_grid(b->num_sms, aderdg::subcell_fp32(b->precision));
   {  // kernel attributes before any capture
     BatchArgs z = a;
     z.ncells = z.nfx = z.nfy = 0;
@@ -687,13 +691,14 @@ int aderdg_batch_profile(aderdg_batch* b, double* phase_ms) {
   BK(b, cudaEventRecord(ev[1], b->stream));
   BK(b, b->kt->predictor(a, bpred_ops(b), fp32, false, b->stream));
   BK(b, cudaEventRecord(ev[2], b->stream));
-  BK(b, b->kt->faces(a, b->fc, fp32, b->stream));
+  BK(b, aderdg::launch_faces(b->kt, a, b->fc, b->precision, b->stream));
   BK(b, cudaEventRecord(ev[3], b->stream));
   BK(b, b->kt->cells(a, b->ops64.data(), fp32, b->stream));
   BK(b, cudaEventRecord(ev[4], b->stream));
   if (b->limiter) BK(b, b->kt->mark(a, b->stream));
   BK(b, cudaEventRecord(ev[5], b->stream));
-  if (b->limiter) BK(b, b->kt->subcell(a, b->ops64.data(), b->fc, b->subcell_grid, b->precision ? 1 : 0, b->stream));
+  if (b->limiter)
+    BK(b, b->kt->subcell(a, b->ops64.data(), b->fc, b->subcell_grid, aderdg::subcell_fp32(b->precision), b->stream));
   BK(b, cudaEventRecord(ev[6], b->stream));
   BK(b, bcontrol(b, aderdg::kCtlEnd, -1));
   BK(b, cudaEventRecord(ev[7], b->stream));

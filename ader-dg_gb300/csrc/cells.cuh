@@ -137,43 +137,53 @@ struct Proj {
   // min/max are of the projected deviations.  A subcell whose FP32 value
   // ubar + proj(d) is not clearly admissible (err = the error bound of
   // proj(d), plus the rounding of ubar to FP32) is projected again in FP64
-  // from U64 and tested exactly.
+  // from U64, in the reference's order (y pass, then x), and tested exactly:
+  // the value and the decision are those of the FP64 path bit for bit.
   template <class Sys>
   __device__ static void xpass_minmax_f32(const float* LY, const float* LB, const float* lim, const float* lob,
-                                          const double* U64, const DevOps<N, double>& op,
+                                          const double* U64, const double* lim64,
                                           const typename Sys::FConst& fc, const float* err, const float* ubf,
                                           const Phys& ph, int r, int nr, float* mn, float* mx, bool& posfail) {
     float val[V], q[V], e[V];
 #pragma unroll
     for (int v = 0; v < V; ++v) e[v] = err[v] + 2.5e-7f * fabsf(ubf[v]);
-    for (int idx = r; idx < S * S; idx += nr) {
-      const int s1 = idx % S, s2 = idx / S;
-      subcell<true>(LY, lim, s1, s2, val);
+    unsigned open = 0u;  // bit it: the it-th subcell of this thread needs the FP64 test
+    int it = 0;
+    for (int idx = r; idx < S * S; idx += nr, ++it) {
+      subcell<true>(LY, lim, idx % S, idx / S, val);
 #pragma unroll
       for (int v = 0; v < V; ++v) { mn[v] = fminf(mn[v], val[v]); mx[v] = fmaxf(mx[v], val[v]); }
       if constexpr (Sys::ID != kSysAD) {
 #pragma unroll
         for (int v = 0; v < V; ++v) q[v] = ubf[v] + val[v];
-        if (!Sys::admissible_box_f32(fc, q, e)) {
-          double q[V];
-#pragma unroll
-          for (int v = 0; v < V; ++v) {
-            double acc = 0.0;
-            for (int l = 0; l < P; ++l) {
-              double row = 0.0;
-              for (int k = 0; k < P; ++k) row = fma(U64[v * P2 + k + P * l], op.uh2lim[s1 + S * k], row);
-              acc = fma(row, op.uh2lim[s2 + S * l], acc);
-            }
-            q[v] = acc;
-          }
-          if (!Sys::positive(ph, q)) posfail = true;
-        }
+        if (!Sys::admissible_box_f32(fc, q, e)) open |= 1u << it;
       }
     }
     for (int idx = r; idx < P * P; idx += nr) {
       lobatto<true>(LB, lob, idx % P, idx / P, val);
 #pragma unroll
       for (int v = 0; v < V; ++v) { mn[v] = fminf(mn[v], val[v]); mx[v] = fmaxf(mx[v], val[v]); }
+    }
+    // the subcells left open, in FP64 in the reference's order (the y pass
+    // of get_subcell_data, then x; lim64 = uh2lim (s,k) at [s + S*k]): the
+    // FP64 path's value and decision bit for bit
+    if constexpr (Sys::ID != kSysAD) while (open) {
+      const int idx = r + (__ffs(open) - 1) * nr;
+      open &= open - 1u;
+      const int s1 = idx % S, s2 = idx / S;
+      double qd[V];
+#pragma unroll 1
+      for (int v = 0; v < V; ++v) {
+        double acc = 0.0;
+#pragma unroll 1
+        for (int k = 0; k < P; ++k) {
+          double ly = 0.0;
+          for (int m = 0; m < P; ++m) ly = ly + U64[v * P2 + k + P * m] * lim64[s2 + S * m];
+          acc = acc + ly * lim64[s1 + S * k];
+        }
+        qd[v] = acc;
+      }
+      if (!Sys::positive(ph, qd)) posfail = true;
     }
   }
 };
@@ -267,6 +277,117 @@ struct CellCfg {
   }
 };
 
+// FP32-mixed K3: the DMP decisions the FP32 bounds left open (bit 4 of the
+// cell's flag and no other failure), settled from FP64 reference-order values:
+// the cell's own projections of its new state U, and (not for the initial
+// DMP, whose bounds are the cell's nodal values) the min/max of every
+// neighbour whose stored min/max carries an error bound, recomputed from its
+// start-of-step state uh_in.  The decision is then the FP64 path's on this
+// state, bit for bit.  Called by every thread of the CTA (barriers inside);
+// the threads of a cell to settle pass redo = true.
+template <class Sys, int N>
+__device__ __forceinline__ void cell_dmp_settle(const double* uh_in, const double* mm_in, const float* mme_in,
+                                             const int* status, double* mm_out, float* mme_out, double* lminmax,
+                                             const InstDesc* in, long long cell, int ci, int cj, int mode, bool redo,
+                                             int node, double* U, double* LY, double* LB, double* RED,
+                                             const double* opsm, int* cflag, int* n_settled) {
+  constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1, V = Sys::V;
+  if (redo && node == 0) atomicAdd(n_settled, 1);
+  if (redo) Proj<N, V, double>::template ypass<false>(U, LY, LB, opsm, opsm + S * P, node, P2);
+  __syncthreads();
+  bool pdummy = false;  // positivity was decided exactly above
+  if (redo) {
+    double mn[V], mx[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) { mn[v] = kInf; mx[v] = -kInf; }
+    Proj<N, V, double>::template xpass_minmax<Sys, false>(U, LY, LB, opsm, opsm + S * P, in->ph, node, P2, mn,
+                                                          mx, pdummy);
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      RED[v * P2 + node] = mn[v];
+      RED[(V + v) * P2 + node] = mx[v];
+    }
+  }
+  __syncthreads();
+  double rmn = 0.0, rmx = 0.0, elmin = kInf, elmax = -kInf;
+  if (redo && node < V) {
+    const int v = node;
+    rmn = RED[v * P2];
+    rmx = RED[(V + v) * P2];
+    for (int k = 1; k < P2; ++k) { rmn = fmin(rmn, RED[v * P2 + k]); rmx = fmax(rmx, RED[(V + v) * P2 + k]); }
+    if (mode == kCellInitDmp) {
+      for (int k = 0; k < P2; ++k) { elmin = fmin(elmin, U[v * P2 + k]); elmax = fmax(elmax, U[v * P2 + k]); }
+    }
+  }
+  if (mode != kCellInitDmp) {
+    __syncthreads();  // U and RED are reused for the neighbours
+    for (int n = 0; n < 9; ++n) {
+      const int in_ = nb_index(ci, n % 3 - 1, in->imax, in->bc[0], in->bc[1]);
+      const int jn_ = nb_index(cj, n / 3 - 1, in->jmax, in->bc[2], in->bc[3]);
+      const long long nc = in->cell_base + in_ + (long long)in->imax * jn_;
+      // limited neighbours' min/max come from Lh (exact); others are
+      // recomputed when their stored values carry an error bound
+      bool comp = false;
+      if (redo && status[nc] == 0) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) comp = comp || mme_in[(size_t)nc * V + v] > 0.0f;
+      }
+      if (comp) {
+        const double* un = uh_in + ((size_t)nc * P2 + node) * V;
+#pragma unroll
+        for (int v = 0; v < V; ++v) U[v * P2 + node] = un[v];
+      }
+      __syncthreads();
+      if (comp) Proj<N, V, double>::template ypass<false>(U, LY, LB, opsm, opsm + S * P, node, P2);
+      __syncthreads();
+      if (comp) {
+        double mn[V], mx[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) { mn[v] = kInf; mx[v] = -kInf; }
+        Proj<N, V, double>::template xpass_minmax<Sys, false>(U, LY, LB, opsm, opsm + S * P, in->ph, node, P2,
+                                                              mn, mx, pdummy);
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          RED[v * P2 + node] = mn[v];
+          RED[(V + v) * P2 + node] = mx[v];
+        }
+      }
+      __syncthreads();
+      if (redo && node < V) {
+        const int v = node;
+        double nmn, nmx;
+        if (comp) {
+          nmn = RED[v * P2];
+          nmx = RED[(V + v) * P2];
+          for (int k = 1; k < P2; ++k) { nmn = fmin(nmn, RED[v * P2 + k]); nmx = fmax(nmx, RED[(V + v) * P2 + k]); }
+        } else {
+          nmn = mm_in[(size_t)nc * 2 * V + v];
+          nmx = mm_in[(size_t)nc * 2 * V + V + v];
+        }
+        elmin = fmin(elmin, nmn);
+        elmax = fmax(elmax, nmx);
+      }
+      __syncthreads();
+    }
+  }
+  if (redo && node < V) {
+    const int v = node;
+    const double argmax = mode == kCellInitDmp ? 1.0e-1 : 0.0;
+    const double ldiff = fmax(fmax(1.0e-4, 1.0e-3 * (elmax - elmin)), argmax);
+    if (rmn < elmin - ldiff || rmx > elmax + ldiff) atomicOr(cflag, 2);
+    if (mode != kCellInitDmp) {
+      mm_out[(size_t)cell * 2 * V + v] = rmn;
+      mm_out[(size_t)cell * 2 * V + V + v] = rmx;
+      mme_out[(size_t)cell * V + v] = 0.0f;
+      if (lminmax) {
+        lminmax[(size_t)cell * 2 * V + v] = elmin;
+        lminmax[(size_t)cell * 2 * V + V + v] = elmax;
+      }
+    }
+  }
+  __syncthreads();
+}
+
 template <class Sys, int N, bool kFast>
 __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min_blocks(kFast))
     k_cells(BatchArgs a, DevOps<N, double> op) {
@@ -317,6 +438,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
   // thread v < V of a cell folds its 3x3 Voronoi neighbourhood now, so the
   // global loads overlap the update and the projections
   double nlmin = 0.0, nlmax = 0.0;
+  float nen = 0.0f;  // FP32-mixed: largest error bound of the folded min/max
   if (limiter && act && node < V && (mode == kCellFused || mode == kCellUpdate)) {
     const int v = node;
     const double* mmi = a.mm[par];
@@ -325,6 +447,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
     if constexpr (kFast) {
       // integer-key min/max (the integer pipe, not FP64)
       long long kmn = okey(nlmin), kmx = okey(nlmax);
+      const float* mei = a.mme[par];
 #pragma unroll
       for (int jj = -1; jj <= 1; ++jj)
 #pragma unroll
@@ -334,6 +457,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
           const long long nc = in.cell_base + in_ + (long long)in.imax * jn_;
           kmn = min(kmn, okey(mmi[(size_t)nc * 2 * V + v]));
           kmx = max(kmx, okey(mmi[(size_t)nc * 2 * V + V + v]));
+          if (mei) nen = fmaxf(nen, mei[(size_t)nc * V + v]);
         }
       nlmin = okey_inv(kmn);
       nlmax = okey_inv(kmx);
@@ -522,7 +646,8 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
       __syncthreads();
       // FP32 projections of the deviations when their error bound stays
       // within the DMP's absolute tolerance (1e-4) for every variable;
-      // otherwise this cell takes the FP64 projections.
+      // otherwise this cell takes the FP64 projections in the reference's
+      // order (the FP64 path's values bit for bit).
       float err[V];
       bool f32ok = true;
 #pragma unroll
@@ -533,7 +658,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
       }
       if (act && !from_lh) {
         if (f32ok) Proj<N, V, float>::template ypass<true>(Uf, LYf, LBf, opsf, opsf + S * P, node, P2);
-        else Proj<N, V, double>::template ypass<true>(U, LY, LB, opsm, opsm + S * P, node, P2);
+        else Proj<N, V, double>::template ypass<false>(U, LY, LB, opsm, opsm + S * P, node, P2);
       }
       __syncthreads();
       bool posfail = false;
@@ -555,7 +680,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
           float mn[V], mx[V];
 #pragma unroll
           for (int v = 0; v < V; ++v) { mn[v] = du[v]; mx[v] = du[v]; }
-          Proj<N, V, float>::template xpass_minmax_f32<Sys>(LYf, LBf, opsf, opsf + S * P, U, op,
+          Proj<N, V, float>::template xpass_minmax_f32<Sys>(LYf, LBf, opsf, opsf + S * P, U, opsm,
                                                             typename Sys::FConst(in.ph), err, ubf, in.ph, node, P2,
                                                             mn, mx, posfail);
 #pragma unroll
@@ -567,8 +692,8 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
           double mn[V], mx[V];
 #pragma unroll
           for (int v = 0; v < V; ++v) { mn[v] = kInf; mx[v] = -kInf; }
-          Proj<N, V, double>::template xpass_minmax<Sys, true>(U, LY, LB, opsm, opsm + S * P, in.ph, node, P2, mn, mx,
-                                                               posfail);
+          Proj<N, V, double>::template xpass_minmax<Sys, false>(U, LY, LB, opsm, opsm + S * P, in.ph, node, P2, mn, mx,
+                                                                posfail);
 #pragma unroll
           for (int v = 0; v < V; ++v) {
             RED[v * P2 + node] = mn[v];
@@ -613,6 +738,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
     if (act && node < V) {
       const int v = node;
       double cmn, cmx;
+      double eself = 0.0;  // bound on |cmn - FP64 value| and |cmx - FP64 value|
       if (f32red) {
         float fmn = REDf[v * P2], fmx = REDf[(V + v) * P2];
 #pragma unroll
@@ -620,6 +746,11 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
         const double ubar = (double)ubs[v];
         cmn = ubar + (double)fmn;
         cmx = ubar + (double)fmx;
+        // the projections' bound (as formed above), plus the FP64 rounding of
+        // the reference-order values
+        const float am = __uint_as_float(amax[v]);
+        const float e32 = op.perr * am + op.pdev * (fabsf(ubs[v]) + 2.0f * am);
+        eself = (double)e32 + 1.0e-13 * (fabs(ubar) + (double)am);
       } else {
         cmn = RED[v * P2];
         cmx = RED[(V + v) * P2];
@@ -629,8 +760,10 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
       if (mode == kCellPrime || mode == kCellPrimeLimited) {
         a.mm[par][(size_t)cell * 2 * V + v] = cmn;
         a.mm[par][(size_t)cell * 2 * V + V + v] = cmx;
+        if (a.mme[0]) a.mme[par][(size_t)cell * V + v] = __double2float_ru(eself);
       } else {
         double lmin, lmax, argmax;
+        float en = 0.0f;
         if (mode == kCellInitDmp) {
           // Euler/initialize.f90:291-294: the cell's own nodal min/max
           lmin = U[v * P2];
@@ -641,6 +774,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
           // get_min_max step 2: the neighbourhood bounds folded at the start
           lmin = nlmin;
           lmax = nlmax;
+          en = nen;
           argmax = 0.0;
           if (a.lminmax) {
             a.lminmax[(size_t)cell * 2 * V + v] = lmin;
@@ -649,15 +783,43 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
           // candidate min/max for the next step (status 0)
           a.mm[par ^ 1][(size_t)cell * 2 * V + v] = cmn;
           a.mm[par ^ 1][(size_t)cell * 2 * V + V + v] = cmx;
+          if (a.mme[0]) a.mme[par ^ 1][(size_t)cell * V + v] = __double2float_ru(eself);
         }
         // Euler/limiter.f90:210-220
         const double ldiff = fmax(fmax(1.0e-4, 1.0e-3 * (lmax - lmin)), argmax);
-        if (cmn < lmin - ldiff || cmx > lmax + ldiff) atomicOr(&cflag[lc], 2);
+        if (a.mme[0] == nullptr || (eself == 0.0 && en == 0.0f)) {
+          // FP64 values (FP32-wide mode: FP32 projections taken as they are)
+          if (cmn < lmin - ldiff || cmx > lmax + ldiff) atomicOr(&cflag[lc], 2);
+        } else {
+          // FP32-mixed: |lmin - its FP64 value| <= en and likewise lmax, so the
+          // threshold moves by at most en (1 + 2e-3); a comparison decides here
+          // only when it holds with that margin plus the own bound, otherwise
+          // the cell is settled below from FP64 values (bit 4)
+          const double M = eself + 1.002 * (double)en + 1.0e-13 * (fabs(lmin) + fabs(lmax) + fabs(cmn) + fabs(cmx));
+          if (cmn < lmin - ldiff - M || cmx > lmax + ldiff + M) atomicOr(&cflag[lc], 2);
+          else if (!(cmn >= lmin - ldiff + M) || !(cmx <= lmax + ldiff - M)) atomicOr(&cflag[lc], 4);
+        }
       }
     }
     __syncthreads();
+    if constexpr (kFast) {
+      if (a.mme[0] != nullptr && (mode == kCellFused || mode == kCellUpdate || mode == kCellInitDmp)) {
+        // FP32-mixed: DMP decisions the FP32 bounds left open (no other
+        // failure of the cell decided it), from FP64 reference-order values:
+        // the cell's own projections of its new state, and (not for the
+        // initial DMP, whose bounds are the cell's nodal values) the min/max
+        // of every neighbour whose stored min/max carries an error bound,
+        // from its start-of-step state.  The decision is then the FP64
+        // path's on this state, bit for bit.
+        const bool redo = act && (cflag[lc] & 7) == 4;
+        if (__syncthreads_or(redo))
+          cell_dmp_settle<Sys, N>(a.uh[par], a.mm[par], a.mme[par], a.status[par], a.mm[par ^ 1], a.mme[par ^ 1],
+                                  a.lminmax, &in, cell, ci, cj, mode, redo, node, U, LY, LB, RED, opsm, &cflag[lc],
+                                  &a.st[kc].n_settled);
+      }
+    }
     if (act && mode != kCellPrime && mode != kCellPrimeLimited) {
-      const bool bad = cflag[lc] != 0;
+      const bool bad = (cflag[lc] & 3) != 0;
       if (mode == kCellInitDmp) {
         if (bad) {
           // Euler/initialize.f90:296-317: status 1, Lh = NewLh = initial subcell data

@@ -60,6 +60,7 @@ struct InstState {
   unsigned long long denom_next;     // accumulator for the next step
   int active;                        // 1 while time < tend
   int n_recompute;                   // troubled cells of the last step (nRecompute)
+  int n_settled;                     // FP32-mixed: DMP decisions of the last step settled from FP64 values
   int n_list;                        // cells with recompute > 0
   int nonfinite;                     // set when dt came out non-finite
   long long steps;
@@ -133,6 +134,11 @@ struct BatchArgs {
   int* status[2];                    // limiter status per cell
   double* lh[2];                     // subcell data [cell][S*S][V]
   double* mm[2];                     // per-cell min/max [cell][2][V] (lmin_old/lmax_old)
+  // FP32-mixed mode only (null otherwise): a bound on |mm - the FP64
+  // reference-order min/max| per cell and variable [cell][V], 0 where mm holds
+  // the FP64 value itself; double-buffered like mm.  The DMP decisions use it
+  // to settle each comparison exactly (see k_cells / k_subcell).
+  float* mme[2];
   double* lminmax;                   // neighbourhood lmin/lmax used by the DMP [cell][2][V]
   unsigned char* troubled;           // DMP failed after the update
   int* recompute;                    // 0, 1, 2

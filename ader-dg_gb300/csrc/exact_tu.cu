@@ -51,14 +51,15 @@ __global__ void __launch_bounds__(256) k_volume(BatchArgs a, DevOps<N, double> o
   }
 }
 
+// fp32 = 1: FP32 storage and FP32 arithmetic; 0: FP64 in reference order
 cudaError_t faces(const BatchArgs& a, const FaceConst& fc, int fp32, cudaStream_t s) {
   const long long n = (a.nfx + a.nfy) * P;
   if (n <= 0) return cudaSuccess;
   const unsigned grid = (unsigned)((n + 255) / 256);
   if (fp32)
-    k_faces<Sys, N, float><<<grid, 256, 0, s>>>(a, fc);
+    k_faces<Sys, N, float, float><<<grid, 256, 0, s>>>(a, fc);
   else
-    k_faces<Sys, N, double><<<grid, 256, 0, s>>>(a, fc);
+    k_faces<Sys, N, double, double><<<grid, 256, 0, s>>>(a, fc);
   return cudaGetLastError();
 }
 
@@ -78,8 +79,8 @@ cudaError_t launch_cells(const BatchArgs& a, const void* ops, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-// fast = 1 (FP32-mixed precision): FP64 with fused multiply-adds in the DMP
-// projections and a reciprocal mass matrix; fast = 0: reference order
+// fast = 1 (the FP32 modes): FP32 surface integral and DMP projections, the
+// FP64 update as one fused multiply-add; fast = 0: FP64 in reference order
 cudaError_t cells(const BatchArgs& a, const void* ops, int fast, cudaStream_t s) {
   return fast ? launch_cells<true>(a, ops, s) : launch_cells<false>(a, ops, s);
 }

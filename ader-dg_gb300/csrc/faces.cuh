@@ -6,13 +6,15 @@
 // (path-conservative Rusanov fluctuations Dm/Dp), and
 // Advection-Diffusion/riemann_problem.f90:8-113 (viscous LLF).  One thread per
 // (face, point); the x faces of all instances come first, then the y faces.
-// Compiled with --fmad=false: every value agrees bit for bit with the
-// reference expression evaluated in FP64 from the same face states.  In the
-// FP32-mixed mode (R = float) the fluxes are stored in FP32, and the Euler
-// and Baer-Nunziato fluxes are computed in FP32.
+// R is the storage type of the face states and fluxes, CT the compute type.
+// FP64 (R = CT = double) is compiled with --fmad=false: every value agrees bit
+// for bit with the reference expression evaluated in FP64 from the same face
+// states.  The FP32 modes store states and fluxes in FP32; Euler and
+// advection-diffusion compute in FP32, and Baer-Nunziato computes its
+// path-conservative flux (Roe-matrix path integral included) in FP64 in the
+// FP32-mixed mode (CT = double, instantiated with fused multiply-adds in
+// predictor_tu.cu) and in FP32 in the FP32-wide mode.
 #pragma once
-
-#include <type_traits>
 
 #include "common.cuh"
 #include "physics.cuh"
@@ -147,7 +149,7 @@ __device__ void faces_euler_fp32(const BatchArgs& a, const FaceConst& fc, const 
   for (int v = 0; v < V; ++v) dst[v] = 0.5f * (FL[v] + FR[v]) - 0.5f * smax * (QR[v] - QL[v]);
 }
 
-template <class Sys, int N, class R>
+template <class Sys, int N, class R, class CT>
 __global__ void __launch_bounds__(256) k_faces(BatchArgs a, FaceConst fc) {
   constexpr int P = N + 1, V = Sys::V;
   const long long nx = a.nfx * P, ny = a.nfy * P;
@@ -192,14 +194,14 @@ __global__ void __launch_bounds__(256) k_faces(BatchArgs a, FaceConst fc) {
   const int fl = xdir ? 0 : 2, fr = xdir ? 1 : 3;  // left/bottom and right/top face ids
   const size_t out = ((size_t)face * P + l) * V;
   if constexpr (Sys::ID == kSysEuler && sizeof(R) == 4) {
+    static_assert(sizeof(CT) == 4, "Euler's FP32-storage faces compute in FP32");
     faces_euler_fp32<N>(a, fc, in, k, xdir, i, j, l, face);
     return;
   }
 
   if constexpr (Sys::ID == kSysAD) {
     // Advection-Diffusion/riemann_problem.f90 with PDEViscLLFRiemannSolver (pde.f90:121-152);
-    // compute type: FP64 (reference order), FP32 in the mixed mode
-    using CT = typename std::conditional<sizeof(R) == 4, float, double>::type;
+    // compute type: FP64 (reference order), FP32 in the FP32 modes
     CT QL[1], QR[1], gL[2], gR[2];
     auto get = [&](long long c, int f, CT* Q, CT* gq) {
       const size_t o = (((size_t)c * 4 + f) * P + l);
@@ -257,8 +259,7 @@ __global__ void __launch_bounds__(256) k_faces(BatchArgs a, FaceConst fc) {
     R* dst = reinterpret_cast<R*>(xdir ? a.fu : a.gu);
     dst[out] = (R)(CT(0.5) * ((FL0 + FR0) * nv0 + (FL1 + FR1) * nv1) - CT(0.5) * smax * (QR[0] - QL[0]));
   } else {
-    // compute type: FP64 (reference order), FP32 for Baer-Nunziato in the mixed mode
-    using CT = typename std::conditional<sizeof(R) == 4, float, double>::type;
+    // Euler (FP64) and Baer-Nunziato (FP64 or FP32 compute, see above)
     const PhysC<CT> pc(ph);
     CT QL[V], QR[V], FL[V], FR[V];
     const bool is_dmr = (Sys::ID == kSysEuler) && in.bc_mode == 1;

@@ -8,8 +8,10 @@
 //     cell, persistent over the list; then put_subcell_data, the DMP of
 //     recompute = 2 cells, the next step's min/max and CFL contribution.
 //     update_limiter (Lh = NewLh) is the parity flip of the Lh buffers.
-// Compiled with --fmad=false, reference operation order throughout; the
-// FP32-mixed mode runs the subcell re-solve (K4b) in FP32.
+// Compiled with --fmad=false, reference operation order throughout.  The FP64
+// and FP32-mixed modes run K4b in FP64 (T = double); the FP32-mixed mode adds
+// the settling of DMP comparisons against neighbourhood bounds that carry an
+// FP32 error bound.  The FP32-wide mode runs the re-solve in FP32 (T = float).
 #pragma once
 
 #include "cells.cuh"
@@ -138,7 +140,7 @@ __device__ __forceinline__ void warp_minmax_store(R* mn, R* mx, R* red, int t) {
 }
 
 // T = double: the reference's FP64 arithmetic in its order (bit for bit).
-// T = float: the FP32-mixed mode; the subcell re-solve, the DMP projections
+// T = float: the FP32-wide mode; the subcell re-solve, the DMP projections
 // of the new polynomial (while their error bound allows) and the CFL
 // eigenvalues (where the FP32 pressure is settled) in FP32; the state, Lh
 // and min/max in FP64.
@@ -465,7 +467,7 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
         float ubf[V];
 #pragma unroll
         for (int v = 0; v < V; ++v) ubf[v] = (float)UN[v * P2];
-        Proj<N, V, float>::template xpass_minmax_f32<Sys>(LYf, LBf, limT, lobT, UN, op, typename Sys::FConst(ph), err,
+        Proj<N, V, float>::template xpass_minmax_f32<Sys>(LYf, LBf, limT, lobT, UN, opsm, typename Sys::FConst(ph), err,
                                                           ubf, ph, t, NT, fmn, fmx, posfail);
       }
       warp_minmax_store<float, V, NW>(fmn, fmx, redf, t);
@@ -514,6 +516,7 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
       if (rec == 2) {
         const double* mmi = a.mm[par];
         double lmin = mmi[(size_t)c * 2 * V + v], lmax = mmi[(size_t)c * 2 * V + V + v];
+        float en = 0.0f;  // FP32-mixed: largest error bound of the folded min/max
         for (int jj = -1; jj <= 1; ++jj)
           for (int ii = -1; ii <= 1; ++ii) {
             const int in_ = nb_index(ci, ii, in.imax, in.bc[0], in.bc[1]);
@@ -521,14 +524,79 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
             const long long nc = in.cell_base + in_ + (long long)in.imax * jn_;
             lmin = fmin(lmin, mmi[(size_t)nc * 2 * V + v]);
             lmax = fmax(lmax, mmi[(size_t)nc * 2 * V + V + v]);
+            if (a.mme[0]) en = fmaxf(en, a.mme[par][(size_t)nc * V + v]);
           }
         const double ldiff = fmax(fmax(1.0e-4, 1.0e-3 * (lmax - lmin)), 0.0);
-        if (cmn < lmin - ldiff || cmx > lmax + ldiff) atomicOr(&flag[0], 2);
+        if (en == 0.0f) {
+          if (cmn < lmin - ldiff || cmx > lmax + ldiff) atomicOr(&flag[0], 2);
+        } else {
+          // FP32-mixed: the own values are FP64; the neighbourhood bounds
+          // carry at most en, so the threshold moves by at most en (1 + 2e-3).
+          // Comparisons inside that margin are settled below (bit 4).
+          const double M = 1.002 * (double)en + 1.0e-13 * (fabs(lmin) + fabs(lmax) + fabs(cmn) + fabs(cmx));
+          if (cmn < lmin - ldiff - M || cmx > lmax + ldiff + M) atomicOr(&flag[0], 2);
+          else if (!(cmn >= lmin - ldiff + M) || !(cmx <= lmax + ldiff - M)) atomicOr(&flag[0], 4);
+        }
       }
     }
     __syncthreads();
+    if constexpr (sizeof(T) == 8) {
+      if (rec == 2 && a.mme[0] != nullptr && (flag[0] & 7) == 4) {
+        // FP32-mixed, a recompute = 2 DMP the bounds left open: the min/max
+        // of every neighbour whose stored values carry an error bound are
+        // recomputed from its start-of-step state in FP64 reference order,
+        // so that the decision is the FP64 path's on this state
+        if (t == 0) atomicAdd(&a.st[k].n_settled, 1);
+        double elmin = kInf, elmax = -kInf;
+        for (int n = 0; n < 9; ++n) {
+          const long long nc = nbc[n];
+          bool comp = false;
+          if (nbs[n] == 0) {
+#pragma unroll
+            for (int v = 0; v < V; ++v) comp = comp || a.mme[par][(size_t)nc * V + v] > 0.0f;
+          }
+          if (comp) {
+            const double* un = a.uh[par] + (size_t)nc * P2 * V;
+            for (int p = t; p < P2 * V; p += NT) {
+              const int node = p / V, v = p - node * V;
+              UN[v * P2 + node] = un[p];
+            }
+          }
+          __syncthreads();
+          if (comp) Proj<N, V, double>::ypass(UN, LY, LB, opsm, opsm + S * P, t, NT);
+          __syncthreads();
+          double nmn[V], nmx[V];
+#pragma unroll
+          for (int v = 0; v < V; ++v) { nmn[v] = kInf; nmx[v] = -kInf; }
+          bool pdummy = false;
+          if (comp) Proj<N, V, double>::template xpass_minmax<Sys>(UN, LY, LB, opsm, opsm + S * P, ph, t, NT, nmn, nmx, pdummy);
+          warp_minmax_store<double, V, NW>(nmn, nmx, red, t);
+          __syncthreads();
+          if (t < V) {
+            const int v = t;
+            double lo, hi;
+            if (comp) {
+              lo = red[v * NW];
+              hi = red[(V + v) * NW];
+              for (int q = 1; q < NW; ++q) { lo = fmin(lo, red[v * NW + q]); hi = fmax(hi, red[(V + v) * NW + q]); }
+            } else {
+              lo = a.mm[par][(size_t)nc * 2 * V + v];
+              hi = a.mm[par][(size_t)nc * 2 * V + V + v];
+            }
+            elmin = fmin(elmin, lo);
+            elmax = fmax(elmax, hi);
+          }
+          __syncthreads();
+        }
+        if (t < V) {
+          const double ldiff = fmax(fmax(1.0e-4, 1.0e-3 * (elmax - elmin)), 0.0);
+          if (dmn < elmin - ldiff || dmx > elmax + ldiff) atomicOr(&flag[0], 2);
+        }
+        __syncthreads();
+      }
+    }
     // status: recompute 1 -> limited; recompute 2 -> limited only when the DMP fails
-    const bool limited = rec == 1 || (rec == 2 && flag[0] != 0);
+    const bool limited = rec == 1 || (rec == 2 && (flag[0] & 3) != 0);
     // min/max over the new subcell data (get_min_max of the next step), in T
     T* redt = reinterpret_cast<T*>(red);
     if (limited) {
@@ -559,6 +627,7 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
       }
       mmo[v] = cmn;
       mmo[V + v] = cmx;
+      if (a.mme[0]) a.mme[par ^ 1][(size_t)c * V + v] = 0.0f;  // FP64 values
     }
     if (t == 0) {
       a.status[par ^ 1][c] = limited ? 1 : 0;

@@ -4,6 +4,7 @@
 // chains; its results agree with the reference to rounding, not bit for bit).
 #include <cmath>
 
+#include "faces.cuh"
 #include "predictor.cuh"
 #include "tables.h"
 
@@ -121,6 +122,18 @@ cudaError_t predictor(const BatchArgs& a, const void* ops, int fp32, bool phase,
   return phase ? launch_pred<double, true>(a, ops, s) : launch_pred<double, false>(a, ops, s);
 }
 
+#if ADERDG_SYS == 2
+// FP32-mixed faces of Baer-Nunziato: FP32 face states and fluxes, the
+// path-conservative Rusanov flux and its Roe-matrix path integral in FP64
+// (compiled here, with fused multiply-adds, not in the reference-order unit)
+cudaError_t faces_mixed(const BatchArgs& a, const FaceConst& fc, cudaStream_t s) {
+  const long long n = (a.nfx + a.nfy) * (N + 1);
+  if (n <= 0) return cudaSuccess;
+  k_faces<Sys, N, float, double><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, fc);
+  return cudaGetLastError();
+}
+#endif
+
 }  // namespace
 
 #define ADERDG_CAT2(a, b, c) a##b##_##c
@@ -137,6 +150,9 @@ void ADERDG_CAT(register_predictor_, ADERDG_SYS, ADERDG_N)(KernelTable& t) {
   t.pred_cells_per_cta[1] = PredCfg<Sys, N, float>::CPB;
   t.pred_threads[0] = PredCfg<Sys, N, double>::THREADS;
   t.pred_threads[1] = PredCfg<Sys, N, float>::THREADS;
+#if ADERDG_SYS == 2
+  t.faces_mixed = &faces_mixed;
+#endif
 }
 
 }  // namespace aderdg

@@ -25,6 +25,9 @@ struct KernelTable {
   cudaError_t (*predictor)(const BatchArgs&, const void* ops, int fp32, bool phase, cudaStream_t) = nullptr;
   int pred_cells_per_cta[2] = {0, 0};
   int pred_threads[2] = {0, 0};
+  // FP32-mixed faces where they differ from the FP32 faces (Baer-Nunziato:
+  // FP64 arithmetic on FP32 storage); null: use faces(..., fp32 = 1, ...)
+  cudaError_t (*faces_mixed)(const BatchArgs&, const FaceConst&, cudaStream_t) = nullptr;
   // exact translation unit
   cudaError_t (*faces)(const BatchArgs&, const FaceConst&, int fp32, cudaStream_t) = nullptr;
   cudaError_t (*cells)(const BatchArgs&, const void* ops64, int fast, cudaStream_t) = nullptr;
@@ -55,5 +58,14 @@ cudaError_t launch_error_norms(const aderdg_config& cfg, const double* uh, int i
 
 // Returns the table for (sys, N) or nullptr when that pair was not built.
 const KernelTable* kernel_table(int sys, int N);
+
+// The face kernel of a precision mode (aderdg_precision).
+inline cudaError_t launch_faces(const KernelTable* kt, const BatchArgs& a, const FaceConst& fc, int precision,
+                                cudaStream_t s) {
+  if (precision == ADERDG_FP32_MIXED && kt->faces_mixed) return kt->faces_mixed(a, fc, s);
+  return kt->faces(a, fc, precision != ADERDG_FP64 ? 1 : 0, s);
+}
+// The subcell re-solve runs in FP32 in the FP32-wide mode only.
+inline int subcell_fp32(int precision) { return precision == ADERDG_FP32_WIDE ? 1 : 0; }
 
 }  // namespace aderdg

@@ -42,7 +42,21 @@ enum aderdg_status {
 };
 
 enum aderdg_system { ADERDG_SYS_ADVDIFF = 0, ADERDG_SYS_EULER = 1, ADERDG_SYS_BN = 2 };
-enum aderdg_precision { ADERDG_FP64 = 0, ADERDG_FP32_MIXED = 1 };
+/* ADERDG_FP64: every phase in FP64 (the reference's arithmetic).
+ * ADERDG_FP32_MIXED: the predictor, volume and surface contractions and the
+ *   Euler / advection-diffusion face fluxes in FP32 with FP32 accumulation;
+ *   FP64 for the update of the state (conservation), the Baer-Nunziato
+ *   path-conservative face flux with its Roe-matrix path integral, the
+ *   subcell finite-volume re-solve, the CFL maximum and dt.  The DMP and
+ *   positivity decisions are those of an FP64 evaluation of the same state:
+ *   FP32 projections decide where their error bound settles the comparison,
+ *   FP64 reference-order projections decide the rest.
+ * ADERDG_FP32_WIDE: as ADERDG_FP32_MIXED, but the Baer-Nunziato face flux and
+ *   the subcell re-solve in FP32 too, and DMP decisions from the FP32
+ *   projections whenever their error bound is within the DMP's 1e-4 floor,
+ *   without settling comparisons closer than that bound (faster; decisions
+ *   near the thresholds may differ from FP64's). */
+enum aderdg_precision { ADERDG_FP64 = 0, ADERDG_FP32_MIXED = 1, ADERDG_FP32_WIDE = 2 };
 
 /* Configuration: what the reference reads from params.ini
  * (Euler/initialize.f90:21-38, Baer-Nunziato/initialize.f90:21-41,
@@ -210,6 +224,8 @@ typedef struct aderdg_info {
   double dt;
   int n_recompute;      /* last step */
   int n_limited;        /* cells with status != 0 after the last step */
+  int n_settled;        /* FP32-mixed: DMP decisions of the last step that the FP32
+                           error bounds left open and FP64 values settled */
 } aderdg_info;
 int aderdg_get_info(aderdg_ctx* ctx, aderdg_info* info);
 
