@@ -159,7 +159,7 @@ def load(build_if_missing=False):
         "aderdg_batch_admit": (i, [vp, cfgp, dp, dp, d, ctypes.c_long, ip]),
         "aderdg_batch_release": (i, [vp, i]), "aderdg_batch_launch": (i, [vp, i]), "aderdg_batch_sync": (i, [vp, ip]),
         "aderdg_batch_query": (i, [vp, i, dp, dp, ctypes.POINTER(ctypes.c_long), ip]),
-        "aderdg_batch_download": (i, [vp, i, dp]),
+        "aderdg_batch_download": (i, [vp, i, dp]), "aderdg_batch_download_status": (i, [vp, i, ip]),
         "aderdg_batch_info": (i, [vp, ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long),
                                   ctypes.POINTER(ctypes.c_long), ip]),
         "aderdg_batch_last_error": (ctypes.c_char_p, [vp]), "aderdg_batch_profile": (i, [vp, dp]),
@@ -186,7 +186,7 @@ EXPORTED = ("aderdg_create", "aderdg_destroy", "aderdg_upload", "aderdg_init_lim
             "aderdg_operator", "aderdg_step_host", "aderdg_time_steps", "aderdg_profile_step",
             "aderdg_batch_unit_bytes", "aderdg_batch_create", "aderdg_batch_destroy", "aderdg_batch_admit",
             "aderdg_batch_release", "aderdg_batch_launch", "aderdg_batch_sync", "aderdg_batch_query",
-            "aderdg_batch_download", "aderdg_batch_info", "aderdg_batch_last_error", "aderdg_batch_profile",
+            "aderdg_batch_download", "aderdg_batch_download_status", "aderdg_batch_info", "aderdg_batch_last_error", "aderdg_batch_profile",
             "aderdg_batch_run_timed", "aderdg_initial_condition", "aderdg_batch_admit_ic",
             "aderdg_cell_averages", "aderdg_batch_cell_averages", "aderdg_error_norms", "aderdg_host_alloc",
             "aderdg_host_free")
@@ -543,6 +543,12 @@ class Batch:
             uh = out[: cfg.dofs]
         self._ck(self.L.aderdg_batch_download(self.h, slot, _dp(uh)))
         return uh
+
+    def download_status(self, slot):
+        """The simulation's limiter status per cell (1: limited by its last step)."""
+        st = np.empty(self.cfgs[slot].cells, dtype=np.int32)
+        self._ck(self.L.aderdg_batch_download_status(self.h, slot, _ip(st)))
+        return st
 
     def cell_averages(self, slot, primitive=True):
         cfg = self.cfgs[slot]

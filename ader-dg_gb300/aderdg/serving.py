@@ -11,7 +11,11 @@ the device at admission (device_setup=True, only the request's parameters
 cross to the device), or projected on a host thread pool and copied in.
 
 Reported per run: aggregate DOF-updates/s over the makespan and the p50/p99
-time-to-solution (arrival to result on the host) of the requests.
+time-to-solution (arrival to result on the host) of the requests.  A request
+whose time step became non-finite (the batch reports ADERDG_ENONFINITE for it;
+its neighbours in the batch are unaffected) is released and reported failed:
+it counts neither towards the throughput nor the time-to-solution
+percentiles.
 """
 import collections
 import concurrent.futures
@@ -21,12 +25,15 @@ import time
 import numpy as np
 
 from .core import FP64, SYS_ADVDIFF, Batch, PinnedArray, project_initial_condition
+
+ENONFINITE = -5  # aderdg_status: the simulation's time step became non-finite
 from . import workloads
 
 
 class Request:
     __slots__ = ("rid", "name", "N", "side", "params", "tend", "max_steps", "arrival", "cfg", "ic", "prepared",
-                 "admitted", "finished", "steps", "dofs", "group", "slot", "result", "time")
+                 "admitted", "finished", "steps", "dofs", "group", "slot", "result", "time", "failed", "uh",
+                 "lh")
 
     def __init__(self, rid, spec, arrival, precision, max_steps):
         self.rid = rid
@@ -43,6 +50,10 @@ class Request:
         self.slot = None
         self.result = None
         self.time = 0.0
+        self.failed = False
+        # optional host initial state (admitted as given instead of the initial field)
+        self.uh = spec.get("uh")
+        self.lh = spec.get("lh")
 
 
 def poisson_arrivals(n, rate, seed):
@@ -85,6 +96,8 @@ class Server:
 
     @staticmethod
     def _prepare(req):
+        if req.uh is not None:
+            return req.uh, req.lh
         uh, lh = project_initial_condition(req.cfg, req.ic, req.params)
         return uh, (lh if req.cfg.limiter and req.cfg.system != SYS_ADVDIFF else None)
 
@@ -115,7 +128,7 @@ class Server:
             now = clock()
             while pending and pending[0].arrival <= now:
                 r = pending.popleft()
-                if not self.device_setup:
+                if not self.device_setup or r.uh is not None:
                     futures[r.rid] = self.pool.submit(self._prepare, r)
                 waiting[r.group].append(r)
             # admit in arrival order per group while there is room, and start the
@@ -125,7 +138,7 @@ class Server:
                 b = self.groups[g]
                 while q:
                     r = q[0]
-                    if self.device_setup:
+                    if self.device_setup and r.uh is None:
                         slot = b.admit_ic(r.cfg, r.ic, r.params, r.tend, r.max_steps)
                         if slot is None:
                             break
@@ -161,13 +174,15 @@ class Server:
                     r = running[g][slot]
                     q = b.query(slot)
                     if q["done"]:
-                        if self.download_results:
+                        r.failed = q["status"] == ENONFINITE
+                        if self.download_results and not r.failed:
                             res = b.download(slot, out=None if stage is None else stage.array)
                             self.d2h_bytes += res.nbytes
                             if self.keep_results:
                                 r.result = res
                         r.steps, r.time, r.finished = q["steps"], q["time"], clock()
-                        total_steps_dofs += r.steps * r.dofs
+                        if not r.failed:
+                            total_steps_dofs += r.steps * r.dofs
                         b.release(slot)
                         del running[g][slot]
                         done.append(r)
@@ -177,9 +192,12 @@ class Server:
                     b.launch(self.sync_every)
                     inflight[g] = True
         makespan = clock()
-        tts = np.array([r.finished - r.arrival for r in done])
+        ok = [r for r in done if not r.failed]
+        tts = np.array([r.finished - r.arrival for r in ok]) if ok else np.array([math.nan])
         return {
-            "requests": len(done),
+            "requests": len(ok),
+            "failed": len(done) - len(ok),
+            "failed_ids": [r.rid for r in done if r.failed],
             "dof_updates": int(total_steps_dofs),
             "makespan_s": makespan,
             "dof_updates_per_s": total_steps_dofs / makespan if makespan > 0 else math.nan,

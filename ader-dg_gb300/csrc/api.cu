@@ -129,6 +129,9 @@ int cur_par(aderdg_ctx* c) { return (int)(c->h_st->steps & 1); }
 int cells(aderdg_ctx* c, int mode) {
   c->args.mode = mode;
   CK(c, c->kt->cells(c->args, c->ops64.data(), c->fp32 ? 1 : 0, c->stream));
+  // FP32-mixed: the DMP decisions the FP32 bounds left open
+  if (c->args.settle && (mode == aderdg::kCellFused || mode == aderdg::kCellUpdate || mode == aderdg::kCellInitDmp))
+    CK(c, c->kt->settle(c->args, c->ops64.data(), c->num_sms, c->stream));
   return ADERDG_OK;
 }
 
@@ -161,7 +164,7 @@ int launch_step(aderdg_ctx* c) {
   if (r) return r;
   if (c->limiter) {
     CK(c, c->kt->mark(c->args, c->stream));
-    CK(c, c->kt->subcell(c->args, c->ops64.data(), c->fc, c->subcell_grid, aderdg::subcell_fp32(c->prec), c->stream));
+    CK(c, aderdg::launch_subcell(c->kt, c->args, c->ops64.data(), c->fc, c->subcell_grid, c->prec, c->stream));
   }
   CK(c, control(c, aderdg::kCtlEnd));
   return ADERDG_OK;
@@ -341,7 +344,7 @@ int aderdg_create(const aderdg_config* cfg, aderdg_ctx** out) {
   if (!r) r = dalloc(c, &a.gu, stor((size_t)c->nfy * P * V));
   if (!r && cfg->system == ADERDG_SYS_BN) r = dalloc(c, &a.fp, stor((size_t)c->nfx * P * V));
   if (!r && cfg->system == ADERDG_SYS_BN) r = dalloc(c, &a.gp, stor((size_t)c->nfy * P * V));
-  if (!r) r = dalloc(c, &a.list_count, 1);
+  if (!r) r = dalloc(c, &a.list_count, 2);
   if (c->limiter) {
     if (!r) r = dalloc(c, &a.status[0], nc);
     if (!r) r = dalloc(c, &a.status[1], nc);
@@ -351,6 +354,7 @@ int aderdg_create(const aderdg_config* cfg, aderdg_ctx** out) {
     if (!r) r = dalloc(c, &a.mm[1], nc * 2 * V);
     if (!r && c->prec == ADERDG_FP32_MIXED) r = dalloc(c, &a.mme[0], nc * V);
     if (!r && c->prec == ADERDG_FP32_MIXED) r = dalloc(c, &a.mme[1], nc * V);
+    if (!r && c->prec == ADERDG_FP32_MIXED) r = dalloc(c, &a.settle, nc);
     if (!r) r = dalloc(c, &a.lminmax, nc * 2 * V);
     if (!r) r = dalloc(c, &a.troubled, nc);
     if (!r) r = dalloc(c, &a.recompute, nc);
@@ -381,7 +385,7 @@ int aderdg_create(const aderdg_config* cfg, aderdg_ctx** out) {
     c->ops32.assign(kt->ops32_size, 0);
     kt->make_ops32(c->ops, c->ops32.data());
   }
-  if (c->limiter) c->subcell_grid = kt->subcell_grid(c->num_sms, aderdg::subcell_fp32(c->prec));
+  if (c->limiter) c->subcell_grid = aderdg::subcell_grid_of(kt, c->num_sms, c->prec);
   // set kernel attributes now, outside any later stream capture
   {
     BatchArgs z = a;
@@ -648,7 +652,7 @@ int aderdg_limiter(aderdg_ctx* c) {
   if (!c->pending) return fail(c, ADERDG_ESTATE, "run aderdg_element_update first");
   CK(c, cudaMemsetAsync(c->args.list_count, 0, sizeof(int), c->stream));
   CK(c, c->kt->mark(c->args, c->stream));
-  CK(c, c->kt->subcell(c->args, c->ops64.data(), c->fc, c->subcell_grid, aderdg::subcell_fp32(c->prec), c->stream));
+  CK(c, aderdg::launch_subcell(c->kt, c->args, c->ops64.data(), c->fc, c->subcell_grid, c->prec, c->stream));
   CK(c, control(c, aderdg::kCtlEnd));
   c->pending = false;
   return pull_state(c);
@@ -782,7 +786,7 @@ int aderdg_profile_step(aderdg_ctx* c, double* time, double tend, double* phase_
   if (c->limiter) CK(c, c->kt->mark(c->args, c->stream));
   CK(c, cudaEventRecord(ev[5], c->stream));
   if (c->limiter)
-    CK(c, c->kt->subcell(c->args, c->ops64.data(), c->fc, c->subcell_grid, aderdg::subcell_fp32(c->prec), c->stream));
+    CK(c, aderdg::launch_subcell(c->kt, c->args, c->ops64.data(), c->fc, c->subcell_grid, c->prec, c->stream));
   CK(c, cudaEventRecord(ev[6], c->stream));
   CK(c, control(c, aderdg::kCtlEnd));
   CK(c, cudaEventRecord(ev[7], c->stream));

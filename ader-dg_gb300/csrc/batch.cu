@@ -97,7 +97,7 @@ long long unit_bytes(int system, int N, int precision, int limiter) {
   b += rb * P * V * (system == ADERDG_SYS_BN ? 4 : 2);              // face fluxes
   if (limiter && system != ADERDG_SYS_ADVDIFF) {
     b += 8 * V * S * S * 2 + 4 * 2 + 8 * 2 * V * 2 + 1 + 4 + 4 + 8;  // Lh[2], status[2], mm[2], flags, list, denom
-    if (precision == ADERDG_FP32_MIXED) b += 4 * V * 2;               // mme[2]
+    if (precision == ADERDG_FP32_MIXED) b += 4 * V * 2 + 4;           // mme[2], settle list
   }
   return b;
 }
@@ -209,9 +209,10 @@ int blaunch_step(aderdg_batch* b) {
   BK(b, b->kt->predictor(a, bpred_ops(b), fp32, false, b->stream));
   BK(b, aderdg::launch_faces(b->kt, a, b->fc, b->precision, b->stream));
   BK(b, b->kt->cells(a, b->ops64.data(), fp32, b->stream));
+  if (a.settle) BK(b, b->kt->settle(a, b->ops64.data(), b->num_sms, b->stream));
   if (b->limiter) {
     BK(b, b->kt->mark(a, b->stream));
-    BK(b, b->kt->subcell(a, b->ops64.data(), b->fc, b->subcell_grid, aderdg::subcell_fp32(b->precision), b->stream));
+    BK(b, aderdg::launch_subcell(b->kt, a, b->ops64.data(), b->fc, b->subcell_grid, b->precision, b->stream));
   }
   BK(b, bcontrol(b, aderdg::kCtlEnd, -1));
   return ADERDG_OK;
@@ -249,6 +250,7 @@ int bcells_one(aderdg_batch* b, int pos, int mode, const double* lh_ic) {
   a.only_inst = pos;
   a.lh_ic = lh_ic;
   BK(b, b->kt->cells(a, b->ops64.data(), b->precision ? 1 : 0, b->stream));
+  if (a.settle && mode == aderdg::kCellInitDmp) BK(b, b->kt->settle(a, b->ops64.data(), b->num_sms, b->stream));
   return ADERDG_OK;
 }
 
@@ -334,7 +336,7 @@ int aderdg_batch_create(int system, int N, int precision, int limiter, long capa
   if (!r) r = balloc(b, &a.gu, stor(U * P * V));
   if (!r && system == ADERDG_SYS_BN) r = balloc(b, &a.fp, stor(U * P * V));
   if (!r && system == ADERDG_SYS_BN) r = balloc(b, &a.gp, stor(U * P * V));
-  if (!r) r = balloc(b, &a.list_count, 1);
+  if (!r) r = balloc(b, &a.list_count, 2);
   if (b->limiter) {
     if (!r) r = balloc(b, &a.status[0], U);
     if (!r) r = balloc(b, &a.status[1], U);
@@ -344,6 +346,7 @@ int aderdg_batch_create(int system, int N, int precision, int limiter, long capa
     if (!r) r = balloc(b, &a.mm[1], U * 2 * V);
     if (!r && precision == ADERDG_FP32_MIXED) r = balloc(b, &a.mme[0], U * V);
     if (!r && precision == ADERDG_FP32_MIXED) r = balloc(b, &a.mme[1], U * V);
+    if (!r && precision == ADERDG_FP32_MIXED) r = balloc(b, &a.settle, U);
     // no lminmax: the neighbourhood bounds are an introspection output of
     // the single-simulation API only
     if (!r) r = balloc(b, &a.troubled, U);
@@ -371,7 +374,7 @@ int aderdg_batch_create(int system, int N, int precision, int limiter, long capa
     b->ops32.assign(kt->ops32_size, 0);
     kt->make_ops32(b->ops, b->ops32.data());
   }
-  if (b->limiter) b->subcell_grid = kt->subcell_grid(b->num_sms, aderdg::subcell_fp32(b->precision));
+  if (b->limiter) b->subcell_grid = aderdg::subcell_grid_of(kt, b->num_sms, b->precision);
   {  // kernel attributes before any capture
     BatchArgs z = a;
     z.ncells = z.nfx = z.nfy = 0;
@@ -628,6 +631,25 @@ int aderdg_batch_query(aderdg_batch* b, int slot, double* time, double* dt, long
   return ADERDG_OK;
 }
 
+int aderdg_batch_download_status(aderdg_batch* b, int slot, int* status) {
+  if (!b || !status || slot < 0 || slot >= b->max_inst || b->pos_of[slot] < 0)
+    return bfail(b, ADERDG_EINVAL, "bad slot");
+  int r = pull_states(b);
+  if (r) return r;
+  const int pos = b->pos_of[slot];
+  const InstDesc& in = b->h_inst[pos];
+  const size_t cells = (size_t)in.imax * in.jmax;
+  if (!b->limiter) {
+    std::memset(status, 0, cells * sizeof(int));
+    return ADERDG_OK;
+  }
+  const int par = (int)(b->h_st[pos].steps & 1);
+  BK(b, cudaMemcpyAsync(status, b->args.status[par] + in.cell_base, cells * sizeof(int), cudaMemcpyDeviceToHost,
+                        b->stream));
+  BK(b, cudaStreamSynchronize(b->stream));
+  return ADERDG_OK;
+}
+
 int aderdg_batch_download(aderdg_batch* b, int slot, double* uh) {
   if (!b || !uh || slot < 0 || slot >= b->max_inst || b->pos_of[slot] < 0) return bfail(b, ADERDG_EINVAL, "bad slot");
   int r = pull_states(b);
@@ -694,11 +716,12 @@ int aderdg_batch_profile(aderdg_batch* b, double* phase_ms) {
   BK(b, aderdg::launch_faces(b->kt, a, b->fc, b->precision, b->stream));
   BK(b, cudaEventRecord(ev[3], b->stream));
   BK(b, b->kt->cells(a, b->ops64.data(), fp32, b->stream));
+  if (a.settle) BK(b, b->kt->settle(a, b->ops64.data(), b->num_sms, b->stream));
   BK(b, cudaEventRecord(ev[4], b->stream));
   if (b->limiter) BK(b, b->kt->mark(a, b->stream));
   BK(b, cudaEventRecord(ev[5], b->stream));
   if (b->limiter)
-    BK(b, b->kt->subcell(a, b->ops64.data(), b->fc, b->subcell_grid, aderdg::subcell_fp32(b->precision), b->stream));
+    BK(b, aderdg::launch_subcell(b->kt, a, b->ops64.data(), b->fc, b->subcell_grid, b->precision, b->stream));
   BK(b, cudaEventRecord(ev[6], b->stream));
   BK(b, bcontrol(b, aderdg::kCtlEnd, -1));
   BK(b, cudaEventRecord(ev[7], b->stream));

@@ -52,6 +52,9 @@ struct Proj {
   template <bool kFast>
   __device__ __forceinline__ static T madd(T acc, T a, T b) {
     if constexpr (kFast) return fma(a, b, acc);
+    // reference order: a rounded product, then a rounded sum, also in the
+    // translation units compiled with fused multiply-adds
+    else if constexpr (sizeof(T) == 8) return __dadd_rn(acc, __dmul_rn(a, b));
     else return acc + a * b;
   }
   // y pass: LY[v][s][i] = sum_k U[v][i + P k] uh2lim(s,k); LB[v][s][i] likewise with uh2lob
@@ -276,117 +279,6 @@ struct CellCfg {
     return (Sys::ID == kSysEuler ? (fast ? 4 : 3) : (Sys::ID == kSysBN ? 2 : 4)) * (256 / CTA);
   }
 };
-
-// FP32-mixed K3: the DMP decisions the FP32 bounds left open (bit 4 of the
-// cell's flag and no other failure), settled from FP64 reference-order values:
-// the cell's own projections of its new state U, and (not for the initial
-// DMP, whose bounds are the cell's nodal values) the min/max of every
-// neighbour whose stored min/max carries an error bound, recomputed from its
-// start-of-step state uh_in.  The decision is then the FP64 path's on this
-// state, bit for bit.  Called by every thread of the CTA (barriers inside);
-// the threads of a cell to settle pass redo = true.
-template <class Sys, int N>
-__device__ __forceinline__ void cell_dmp_settle(const double* uh_in, const double* mm_in, const float* mme_in,
-                                             const int* status, double* mm_out, float* mme_out, double* lminmax,
-                                             const InstDesc* in, long long cell, int ci, int cj, int mode, bool redo,
-                                             int node, double* U, double* LY, double* LB, double* RED,
-                                             const double* opsm, int* cflag, int* n_settled) {
-  constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1, V = Sys::V;
-  if (redo && node == 0) atomicAdd(n_settled, 1);
-  if (redo) Proj<N, V, double>::template ypass<false>(U, LY, LB, opsm, opsm + S * P, node, P2);
-  __syncthreads();
-  bool pdummy = false;  // positivity was decided exactly above
-  if (redo) {
-    double mn[V], mx[V];
-#pragma unroll
-    for (int v = 0; v < V; ++v) { mn[v] = kInf; mx[v] = -kInf; }
-    Proj<N, V, double>::template xpass_minmax<Sys, false>(U, LY, LB, opsm, opsm + S * P, in->ph, node, P2, mn,
-                                                          mx, pdummy);
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-      RED[v * P2 + node] = mn[v];
-      RED[(V + v) * P2 + node] = mx[v];
-    }
-  }
-  __syncthreads();
-  double rmn = 0.0, rmx = 0.0, elmin = kInf, elmax = -kInf;
-  if (redo && node < V) {
-    const int v = node;
-    rmn = RED[v * P2];
-    rmx = RED[(V + v) * P2];
-    for (int k = 1; k < P2; ++k) { rmn = fmin(rmn, RED[v * P2 + k]); rmx = fmax(rmx, RED[(V + v) * P2 + k]); }
-    if (mode == kCellInitDmp) {
-      for (int k = 0; k < P2; ++k) { elmin = fmin(elmin, U[v * P2 + k]); elmax = fmax(elmax, U[v * P2 + k]); }
-    }
-  }
-  if (mode != kCellInitDmp) {
-    __syncthreads();  // U and RED are reused for the neighbours
-    for (int n = 0; n < 9; ++n) {
-      const int in_ = nb_index(ci, n % 3 - 1, in->imax, in->bc[0], in->bc[1]);
-      const int jn_ = nb_index(cj, n / 3 - 1, in->jmax, in->bc[2], in->bc[3]);
-      const long long nc = in->cell_base + in_ + (long long)in->imax * jn_;
-      // limited neighbours' min/max come from Lh (exact); others are
-      // recomputed when their stored values carry an error bound
-      bool comp = false;
-      if (redo && status[nc] == 0) {
-#pragma unroll
-        for (int v = 0; v < V; ++v) comp = comp || mme_in[(size_t)nc * V + v] > 0.0f;
-      }
-      if (comp) {
-        const double* un = uh_in + ((size_t)nc * P2 + node) * V;
-#pragma unroll
-        for (int v = 0; v < V; ++v) U[v * P2 + node] = un[v];
-      }
-      __syncthreads();
-      if (comp) Proj<N, V, double>::template ypass<false>(U, LY, LB, opsm, opsm + S * P, node, P2);
-      __syncthreads();
-      if (comp) {
-        double mn[V], mx[V];
-#pragma unroll
-        for (int v = 0; v < V; ++v) { mn[v] = kInf; mx[v] = -kInf; }
-        Proj<N, V, double>::template xpass_minmax<Sys, false>(U, LY, LB, opsm, opsm + S * P, in->ph, node, P2,
-                                                              mn, mx, pdummy);
-#pragma unroll
-        for (int v = 0; v < V; ++v) {
-          RED[v * P2 + node] = mn[v];
-          RED[(V + v) * P2 + node] = mx[v];
-        }
-      }
-      __syncthreads();
-      if (redo && node < V) {
-        const int v = node;
-        double nmn, nmx;
-        if (comp) {
-          nmn = RED[v * P2];
-          nmx = RED[(V + v) * P2];
-          for (int k = 1; k < P2; ++k) { nmn = fmin(nmn, RED[v * P2 + k]); nmx = fmax(nmx, RED[(V + v) * P2 + k]); }
-        } else {
-          nmn = mm_in[(size_t)nc * 2 * V + v];
-          nmx = mm_in[(size_t)nc * 2 * V + V + v];
-        }
-        elmin = fmin(elmin, nmn);
-        elmax = fmax(elmax, nmx);
-      }
-      __syncthreads();
-    }
-  }
-  if (redo && node < V) {
-    const int v = node;
-    const double argmax = mode == kCellInitDmp ? 1.0e-1 : 0.0;
-    const double ldiff = fmax(fmax(1.0e-4, 1.0e-3 * (elmax - elmin)), argmax);
-    if (rmn < elmin - ldiff || rmx > elmax + ldiff) atomicOr(cflag, 2);
-    if (mode != kCellInitDmp) {
-      mm_out[(size_t)cell * 2 * V + v] = rmn;
-      mm_out[(size_t)cell * 2 * V + V + v] = rmx;
-      mme_out[(size_t)cell * V + v] = 0.0f;
-      if (lminmax) {
-        lminmax[(size_t)cell * 2 * V + v] = elmin;
-        lminmax[(size_t)cell * 2 * V + V + v] = elmax;
-      }
-    }
-  }
-  __syncthreads();
-}
 
 template <class Sys, int N, bool kFast>
 __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min_blocks(kFast))
@@ -738,19 +630,21 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
     if (act && node < V) {
       const int v = node;
       double cmn, cmx;
-      double eself = 0.0;  // bound on |cmn - FP64 value| and |cmx - FP64 value|
+      // FP32 projections: the cell's deviation min/max from its FP32 reference
+      // state ubar, and a bound on |ubar + fmn - FP64 value| (and fmx): the
+      // projections' bound as formed above (rounded up), plus the FP64
+      // roundings of the reference-order values (generously 1e-12 relative)
+      float fmn = 0.0f, fmx = 0.0f, ecell = 0.0f;
       if (f32red) {
-        float fmn = REDf[v * P2], fmx = REDf[(V + v) * P2];
+        fmn = REDf[v * P2];
+        fmx = REDf[(V + v) * P2];
 #pragma unroll
         for (int k = 1; k < P2; ++k) { fmn = fminf(fmn, REDf[v * P2 + k]); fmx = fmaxf(fmx, REDf[(V + v) * P2 + k]); }
         const double ubar = (double)ubs[v];
         cmn = ubar + (double)fmn;
         cmx = ubar + (double)fmx;
-        // the projections' bound (as formed above), plus the FP64 rounding of
-        // the reference-order values
         const float am = __uint_as_float(amax[v]);
-        const float e32 = op.perr * am + op.pdev * (fabsf(ubs[v]) + 2.0f * am);
-        eself = (double)e32 + 1.0e-13 * (fabs(ubar) + (double)am);
+        ecell = (op.perr * am + op.pdev * (fabsf(ubs[v]) + 2.0f * am)) * 1.0001f + 1.0e-12f * (fabsf(ubs[v]) + am);
       } else {
         cmn = RED[v * P2];
         cmx = RED[(V + v) * P2];
@@ -760,7 +654,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
       if (mode == kCellPrime || mode == kCellPrimeLimited) {
         a.mm[par][(size_t)cell * 2 * V + v] = cmn;
         a.mm[par][(size_t)cell * 2 * V + V + v] = cmx;
-        if (a.mme[0]) a.mme[par][(size_t)cell * V + v] = __double2float_ru(eself);
+        if (a.mme[0]) a.mme[par][(size_t)cell * V + v] = ecell;
       } else {
         double lmin, lmax, argmax;
         float en = 0.0f;
@@ -783,40 +677,46 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
           // candidate min/max for the next step (status 0)
           a.mm[par ^ 1][(size_t)cell * 2 * V + v] = cmn;
           a.mm[par ^ 1][(size_t)cell * 2 * V + V + v] = cmx;
-          if (a.mme[0]) a.mme[par ^ 1][(size_t)cell * V + v] = __double2float_ru(eself);
+          if (a.mme[0]) a.mme[par ^ 1][(size_t)cell * V + v] = ecell;
         }
-        // Euler/limiter.f90:210-220
-        const double ldiff = fmax(fmax(1.0e-4, 1.0e-3 * (lmax - lmin)), argmax);
-        if (a.mme[0] == nullptr || (eself == 0.0 && en == 0.0f)) {
-          // FP64 values (FP32-wide mode: FP32 projections taken as they are)
+        if (a.mme[0] == nullptr || (!f32red && en == 0.0f)) {
+          // FP64 values (FP32-wide mode: FP32 projections taken as they are);
+          // Euler/limiter.f90:210-220
+          const double ldiff = fmax(fmax(1.0e-4, 1.0e-3 * (lmax - lmin)), argmax);
           if (cmn < lmin - ldiff || cmx > lmax + ldiff) atomicOr(&cflag[lc], 2);
         } else {
-          // FP32-mixed: |lmin - its FP64 value| <= en and likewise lmax, so the
-          // threshold moves by at most en (1 + 2e-3); a comparison decides here
-          // only when it holds with that margin plus the own bound, otherwise
-          // the cell is settled below from FP64 values (bit 4)
-          const double M = eself + 1.002 * (double)en + 1.0e-13 * (fabs(lmin) + fabs(lmax) + fabs(cmn) + fabs(cmx));
-          if (cmn < lmin - ldiff - M || cmx > lmax + ldiff + M) atomicOr(&cflag[lc], 2);
-          else if (!(cmn >= lmin - ldiff + M) || !(cmx <= lmax + ldiff - M)) atomicOr(&cflag[lc], 4);
+          // FP32-mixed: the same comparisons in FP32, in the deviation space
+          // of the cell's FP32 reference state ub (FP64 work is the costly
+          // part of this kernel).  |own - FP64 value| <= ecell; |lmin - its
+          // FP64 value| <= en and likewise lmax, so the thresholds move by at
+          // most en (1 + 2e-3); the FP32 forms of lmin - ub, lmax - ub, ldiff,
+          // the thresholds and the differences add at most 2.5e-7 of the
+          // magnitudes involved, and the FP32 constants 1e-4 and 0.1 differ
+          // from their FP64 values by less than 1e-11 and 1e-8 of themselves.
+          // A comparison decides here only when it holds by that margin;
+          // otherwise k_settle decides the cell from FP64 values (bit 4).
+          const double ub = (double)ubs[v];
+          const float Lmin = (float)(lmin - ub), Lmax = (float)(lmax - ub);
+          const float ld = fmaxf(fmaxf(1.0e-4f, 1.0e-3f * (Lmax - Lmin)), (float)argmax);
+          const float dl = Lmin - ld, dh = Lmax + ld;
+          const float xl = f32red ? fmn : (float)(cmn - ub), xh = f32red ? fmx : (float)(cmx - ub);
+          const float e = ecell + 1.002f * en + 2.5e-7f * (fabsf(Lmin) + fabsf(Lmax) + ld) + 1.0e-11f +
+                          1.0e-12f * fabsf(ubs[v]);
+          const float ml = e + 1.2e-7f * fabsf(xl), mh = e + 1.2e-7f * fabsf(xh);
+          const float gl = xl - dl, gh = dh - xh;  // >= 0: not below lmin - ldiff / not above lmax + ldiff
+          if (gl < -ml || gh < -mh) atomicOr(&cflag[lc], 2);
+          else if (!(gl >= ml) || !(gh >= mh)) atomicOr(&cflag[lc], 4);
         }
       }
     }
     __syncthreads();
     if constexpr (kFast) {
-      if (a.mme[0] != nullptr && (mode == kCellFused || mode == kCellUpdate || mode == kCellInitDmp)) {
-        // FP32-mixed: DMP decisions the FP32 bounds left open (no other
-        // failure of the cell decided it), from FP64 reference-order values:
-        // the cell's own projections of its new state, and (not for the
-        // initial DMP, whose bounds are the cell's nodal values) the min/max
-        // of every neighbour whose stored min/max carries an error bound,
-        // from its start-of-step state.  The decision is then the FP64
-        // path's on this state, bit for bit.
-        const bool redo = act && (cflag[lc] & 7) == 4;
-        if (__syncthreads_or(redo))
-          cell_dmp_settle<Sys, N>(a.uh[par], a.mm[par], a.mme[par], a.status[par], a.mm[par ^ 1], a.mme[par ^ 1],
-                                  a.lminmax, &in, cell, ci, cj, mode, redo, node, U, LY, LB, RED, opsm, &cflag[lc],
-                                  &a.st[kc].n_settled);
-      }
+      // FP32-mixed: a cell whose DMP the error bounds left open (bit 4) and
+      // that nothing else marked goes on the list k_settle decides from FP64
+      // values; here it counts as not troubled
+      if (act && node == 0 && a.settle && (cflag[lc] & 7) == 4 &&
+          (mode == kCellFused || mode == kCellUpdate || mode == kCellInitDmp))
+        a.settle[atomicAdd(&a.list_count[1], 1)] = (int)cell;
     }
     if (act && mode != kCellPrime && mode != kCellPrimeLimited) {
       const bool bad = (cflag[lc] & 3) != 0;
@@ -865,5 +765,6 @@ __global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min
     atomicMax(&a.st[kc].denom_next, m);
   }
 }
+
 
 }  // namespace aderdg

@@ -143,7 +143,9 @@ struct BatchArgs {
   unsigned char* troubled;           // DMP failed after the update
   int* recompute;                    // 0, 1, 2
   int* list;                         // cells with recompute > 0
-  int* list_count;
+  int* list_count;                   // [0]: entries of list, [1]: entries of settle
+  int* settle;                       // FP32-mixed only (null otherwise): cells whose DMP
+                                     // decision k_settle takes from FP64 values
   double* denom;                     // per-cell CFL denominator
   const double* lh_ic;               // initial-limiter candidates
   int mode;                          // kernel mode switch

@@ -30,7 +30,10 @@ __device__ __forceinline__ double dt_from_denom(double cfl_pnpm, double maxd) {
 // only >= 0: the priming modes (reset, commit) act on that instance alone
 static __global__ void k_control(InstDesc* inst, InstState* st, int ninst, int* list_count, int mode, int only) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k == 0 && list_count && (mode == kCtlBegin || (mode == kCtlPrimeReset && only < 0))) *list_count = 0;
+  if (k == 0 && list_count && (mode == kCtlBegin || (mode == kCtlPrimeReset && only < 0))) list_count[0] = 0;
+  // the settle list serves one cell-kernel pass at a time: every pass that
+  // fills it follows a begin or a priming reset on the same stream
+  if (k == 0 && list_count && (mode == kCtlBegin || mode == kCtlPrimeReset)) list_count[1] = 0;
   if (k >= ninst) return;
   if (only >= 0 && k != only) return;
   InstState& s = st[k];

@@ -129,6 +129,11 @@ cudaError_t subcell_t(const BatchArgs& a, const void* ops, const FaceConst& fc, 
 cudaError_t subcell(const BatchArgs& a, const void* ops, const FaceConst& fc, int grid, int fp32, cudaStream_t s) {
   return fp32 ? subcell_t<float>(a, ops, fc, grid, s) : subcell_t<double>(a, ops, fc, grid, s);
 }
+
+cudaError_t settle(const BatchArgs& a, const void* ops, int grid, cudaStream_t s) {
+  k_settle<Sys, N><<<grid, 128, 0, s>>>(a, *reinterpret_cast<const DevOps<N, double>*>(ops));
+  return cudaGetLastError();
+}
 #endif
 
 }  // namespace
@@ -143,6 +148,7 @@ void ADERDG_CAT(register_exact_, ADERDG_SYS, ADERDG_N)(KernelTable& t) {
   t.mark = &mark;
   t.subcell = &subcell;
   t.subcell_grid = &subcell_grid;
+  t.settle = &settle;
 #endif
 }
 

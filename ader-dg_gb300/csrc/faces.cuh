@@ -302,12 +302,17 @@ __global__ void __launch_bounds__(256) k_faces(BatchArgs a, FaceConst fc) {
       load_face_state<V, R>(qb, fb, cL, P, l, fr, QL, FL);
       load_face_state<V, R>(qb, fb, cR, P, l, fl, QR, FR);
     }
+    // FP32-mixed Baer-Nunziato: FP64 with the reciprocal-sharing forms
+    constexpr bool kRcp = sizeof(R) == 4 && sizeof(CT) == 8;
     // Rusanov: smax from both sides' eigenvalues (Euler/pde.f90:97-114)
-    const CT smax = tmax(Sys::max_eig(pc, QL, d), Sys::max_eig(pc, QR, d));
+    CT smax;
+    if constexpr (kRcp) smax = tmax(Sys::max_eig_r(pc, QL, d), Sys::max_eig_r(pc, QR, d));
+    else smax = tmax(Sys::max_eig(pc, QL, d), Sys::max_eig(pc, QR, d));
     if constexpr (Sys::ID == kSysBN) {
       // path-conservative fluctuations, Baer-Nunziato/pde.f90:326-353
       CT D[9];
-      BNSys::roe_times_jump(pc, QL, QR, d, D);
+      if constexpr (kRcp) BNSys::roe_times_jump_r(pc, QL, QR, d, D);
+      else BNSys::roe_times_jump(pc, QL, QR, d, D);
       R* dm = reinterpret_cast<R*>(xdir ? a.fu : a.gu);
       R* dp = reinterpret_cast<R*>(xdir ? a.fp : a.gp);
 #pragma unroll

@@ -105,19 +105,30 @@ __device__ __forceinline__ T minmod(T a, T b) {
   return (tabs(a) < tabs(b)) ? a : b;
 }
 
-// Subgrid Rusanov flux (Euler/limiter.f90:361-378; BN :359-383 adds D = B~ dQ)
-template <class Sys, class T>
+// Subgrid Rusanov flux (Euler/limiter.f90:361-378; BN :359-383 adds D = B~ dQ);
+// kRcp: the reciprocal-sharing physics forms (FP32-mixed mode)
+template <class Sys, class T, bool kRcp = false>
 __device__ __forceinline__ void rusanov_s(const PhysC<T>& pc, const T* QL, const T* QR, int d, T* F, T* D) {
   constexpr int V = Sys::V;
-  const T smax = tmax(Sys::max_eig(pc, QL, d), Sys::max_eig(pc, QR, d));
-  T FLf[2 * V], FRf[2 * V];
-  Sys::flux(pc, QL, FLf);
-  Sys::flux(pc, QR, FRf);
+  T FLf[2 * V], FRf[2 * V], smax;
+  if constexpr (kRcp) {
+    T eL, eR;
+    Sys::flux_eig_r(pc, QL, d, FLf, eL);
+    Sys::flux_eig_r(pc, QR, d, FRf, eR);
+    smax = tmax(eL, eR);
+  } else {
+    smax = tmax(Sys::max_eig(pc, QL, d), Sys::max_eig(pc, QR, d));
+    Sys::flux(pc, QL, FLf);
+    Sys::flux(pc, QR, FRf);
+  }
   const T nv0 = d == 0 ? T(1) : T(0), nv1 = d == 0 ? T(0) : T(1);
 #pragma unroll
   for (int v = 0; v < V; ++v)
     F[v] = T(0.5) * ((FLf[v] + FRf[v]) * nv0 + (FLf[V + v] + FRf[V + v]) * nv1) - T(0.5) * smax * (QR[v] - QL[v]);
-  if constexpr (Sys::ID == kSysBN) BNSys::roe_times_jump(pc, QL, QR, d, D);
+  if constexpr (Sys::ID == kSysBN) {
+    if constexpr (kRcp) BNSys::roe_times_jump_r(pc, QL, QR, d, D);
+    else BNSys::roe_times_jump(pc, QL, QR, d, D);
+  }
 }
 
 // Warp-wide min/max of V values per lane (butterfly), then lane 0 of warp w
@@ -139,12 +150,16 @@ __device__ __forceinline__ void warp_minmax_store(R* mn, R* mx, R* red, int t) {
     }
 }
 
-// T = double: the reference's FP64 arithmetic in its order (bit for bit).
+// T = double: the reference's FP64 arithmetic in its order (bit for bit),
+// or, with kRcp (the FP32-mixed mode, instantiated with fused multiply-adds in
+// predictor_tu.cu), FP64 with the reciprocal-sharing physics forms and
+// multiplications by 1/ldx in place of divisions; the DMP projections keep
+// the reference order in both.
 // T = float: the FP32-wide mode; the subcell re-solve, the DMP projections
 // of the new polynomial (while their error bound allows) and the CFL
 // eigenvalues (where the FP32 pressure is settled) in FP32; the state, Lh
 // and min/max in FP64.
-template <class Sys, int N, class T>
+template <class Sys, int N, class T, bool kRcp = false>
 __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>::MIN_BLOCKS) k_subcell(BatchArgs a, DevOps<N, double> op, FaceConst fc) {
   using C = SubCfg<Sys, N, T>;
   constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1, V = Sys::V, R = C::R, H = C::H, NT = C::THREADS, NE = C::NE;
@@ -208,6 +223,16 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
     const int rec = a.recompute[c];
     const T dt = (T)st.dt;
     const T ldx0 = (T)(in.dx / (double)S), ldx1 = (T)(in.dy / (double)S);
+    const T ix0 = T(1) / ldx0, ix1 = T(1) / ldx1;  // kRcp only
+    auto divx = [&](T q) -> T { if constexpr (kRcp) return q * ix0; else return q / ldx0; };
+    auto divy = [&](T q) -> T { if constexpr (kRcp) return q * ix1; else return q / ldx1; };
+    auto flux = [&](const T* Q, T* F) { if constexpr (kRcp) Sys::flux_r(pc, Q, F); else Sys::flux(pc, Q, F); };
+    auto ncp = [&](const T* Q, T ax, T ay, T* Sr) {
+      if constexpr (Sys::ID == kSysBN) {
+        if constexpr (kRcp) BNSys::src_ncp_r(pc, Q, ax, ay, Sr);
+        else BNSys::src_ncp(pc, Q, ax, ay, Sr);
+      }
+    };
     const bool dmr = (Sys::ID == kSysEuler) && in.bc_mode == 1;
 
     // ---- gather the subcell data of the 3x3 neighbourhood (only the strip
@@ -312,19 +337,19 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
       T src[V];
       if constexpr (BN) {
         // Baer-Nunziato/limiter.f90:494-497
-        BNSys::src_ncp(pc, q0, slx[hx(8, ii, jj)] / ldx0, sly[hx(8, ii, jj)] / ldx1, src);
+        ncp(q0, divx(slx[hx(8, ii, jj)]), divy(sly[hx(8, ii, jj)]), src);
       }
 #pragma unroll
       for (int v = 0; v < V; ++v) {
         wl[v] = q0[v] - T(0.5) * slx[hx(v, ii, jj)];
         wr[v] = q0[v] + T(0.5) * slx[hx(v, ii, jj)];
       }
-      Sys::flux(pc, wl, FLx);
-      Sys::flux(pc, wr, FRx);
+      flux(wl, FLx);
+      flux(wr, FRx);
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        if constexpr (BN) Qt[v] = src[v] - (FRx[v] - FLx[v]) / ldx0;
-        else Qt[v] = -(FRx[v] - FLx[v]) / ldx0;
+        if constexpr (BN) Qt[v] = src[v] - divx(FRx[v] - FLx[v]);
+        else Qt[v] = -divx(FRx[v] - FLx[v]);
         wLx[hx(v, ii, jj)] = wl[v];
         wRx[hx(v, ii, jj)] = wr[v];
       }
@@ -333,11 +358,11 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
         wl[v] = q0[v] - T(0.5) * sly[hx(v, ii, jj)];
         wr[v] = q0[v] + T(0.5) * sly[hx(v, ii, jj)];
       }
-      Sys::flux(pc, wl, FLy);
-      Sys::flux(pc, wr, FRy);
+      flux(wl, FLy);
+      flux(wr, FRy);
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        Qt[v] = Qt[v] - (FRy[V + v] - FLy[V + v]) / ldx1;
+        Qt[v] = Qt[v] - divy(FRy[V + v] - FLy[V + v]);
         slt[hx(v, ii, jj)] = Qt[v];
         wLx[hx(v, ii, jj)] = wLx[hx(v, ii, jj)] + T(0.5) * dt * Qt[v];
         wRx[hx(v, ii, jj)] = wRx[hx(v, ii, jj)] + T(0.5) * dt * Qt[v];
@@ -365,7 +390,7 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
           QL[v] = xd ? wRx[hx(v, ii - 1, jj)] : wRy[hx(v, ii, jj - 1)];
           QR[v] = xd ? wLx[hx(v, ii, jj)] : wLy[hx(v, ii, jj)];
         }
-        rusanov_s<Sys>(pc, QL, QR, xd ? 0 : 1, F, Dd);
+        rusanov_s<Sys, T, kRcp>(pc, QL, QR, xd ? 0 : 1, F, Dd);
         T* dst = xd ? EX : EY;
 #pragma unroll
         for (int v = 0; v < V; ++v) dst[v * NE + q] = F[v];
@@ -383,19 +408,19 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
           // first-order FV update, Euler/limiter.f90:592-597
 #pragma unroll
           for (int v = 0; v < V; ++v)
-            sub1[v * S * S + p] = SU(v, ii, jj) - dt / ldx0 * (EX[v * NE + xp] - EX[v * NE + xm]) -
-                                  dt / ldx1 * (EY[v * NE + yp] - EY[v * NE + ym]);
+            sub1[v * S * S + p] = SU(v, ii, jj) - divx(dt) * (EX[v * NE + xp] - EX[v * NE + xm]) -
+                                  divy(dt) * (EY[v * NE + yp] - EY[v * NE + ym]);
         } else {
           T qh[V], src[V];
 #pragma unroll
           for (int v = 0; v < V; ++v) qh[v] = SU(v, ii, jj) + T(0.5) * dt * slt[hx(v, ii, jj)];
-          BNSys::src_ncp(pc, qh, slx[hx(8, ii, jj)] / ldx0, sly[hx(8, ii, jj)] / ldx1, src);
+          ncp(qh, divx(slx[hx(8, ii, jj)]), divy(sly[hx(8, ii, jj)]), src);
 #pragma unroll
           for (int v = 0; v < V; ++v)
-            sub1[v * S * S + p] = SU(v, ii, jj) - dt / ldx0 * (EX[v * NE + xp] - EX[v * NE + xm]) -
-                                  dt / ldx1 * (EY[v * NE + yp] - EY[v * NE + ym]) -
-                                  dt / ldx0 * T(0.5) * (EX[(V + v) * NE + xp] + EX[(V + v) * NE + xm]) -
-                                  dt / ldx1 * T(0.5) * (EY[(V + v) * NE + yp] + EY[(V + v) * NE + ym]) +
+            sub1[v * S * S + p] = SU(v, ii, jj) - divx(dt) * (EX[v * NE + xp] - EX[v * NE + xm]) -
+                                  divy(dt) * (EY[v * NE + yp] - EY[v * NE + ym]) -
+                                  divx(dt) * T(0.5) * (EX[(V + v) * NE + xp] + EX[(V + v) * NE + xm]) -
+                                  divy(dt) * T(0.5) * (EY[(V + v) * NE + yp] + EY[(V + v) * NE + ym]) +
                                   dt * src[v];
         }
       }
@@ -634,6 +659,129 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
       atomicMax(&a.st[k].denom_next, *cmaxp);
     }
     __syncthreads();
+  }
+}
+
+
+// FP32-mixed: the DMP decisions k_cells left open (a.settle, a.list_count[1]
+// entries), from FP64 values in the reference's order.  One CTA per listed
+// cell, persistent over the list.  The cell's own subcell / Gauss-Lobatto /
+// nodal min and max come from its new state (fused step: uh[par ^ 1]; initial
+// DMP: uh[par]); the neighbourhood bounds (get_min_max, Euler/limiter.f90:
+// 104-171) from the stored min/max where they are FP64 values (error bound 0,
+// or limited cells, whose min/max come from Lh) and from the neighbour's
+// start-of-step state otherwise.  The decision (Euler/limiter.f90:206-220) is
+// then the FP64 path's on this state, bit for bit; a troubled cell is marked
+// as k_cells marks it, and the cell's min/max for the next step become the
+// FP64 values.  The initial DMP compares against the cell's own nodal
+// min/max with argmax 0.1 (Euler/initialize.f90:287-307).
+template <class Sys, int N>
+__global__ void __launch_bounds__(128) k_settle(BatchArgs a, DevOps<N, double> op) {
+  constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1, V = Sys::V, NT = 128, NW = NT / 32;
+  __shared__ double U[V * P2], LY[V * S * P], LB[V * P * P], red[2 * V * NW], ops[S * P + P * P];
+  __shared__ int flag;
+  const int t = threadIdx.x;
+  const int count = a.list_count[1];
+  if (count == 0) return;
+  for (int k = t; k < S * P + P * P; k += NT) ops[k] = k < S * P ? op.uh2lim[k] : op.uh2lob[k - S * P];
+  const bool init = a.mode == kCellInitDmp;
+  // FP64 min/max of the projections of the state U (all threads take part)
+  auto minmax = [&](const Phys& ph, double* lo, double* hi) {
+    __syncthreads();
+    Proj<N, V, double>::ypass(U, LY, LB, ops, ops + S * P, t, NT);
+    __syncthreads();
+    double mn[V], mx[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) { mn[v] = kInf; mx[v] = -kInf; }
+    bool pdummy = false;  // positivity was decided by k_cells, exactly
+    Proj<N, V, double>::template xpass_minmax<Sys>(U, LY, LB, ops, ops + S * P, ph, t, NT, mn, mx, pdummy);
+    warp_minmax_store<double, V, NW>(mn, mx, red, t);
+    __syncthreads();
+    if (t < V) {
+      double l = red[t * NW], h = red[(V + t) * NW];
+      for (int q = 1; q < NW; ++q) { l = fmin(l, red[t * NW + q]); h = fmax(h, red[(V + t) * NW + q]); }
+      *lo = l;
+      *hi = h;
+    }
+  };
+  for (int li = blockIdx.x; li < count; li += gridDim.x) {
+    const long long cell = a.settle[li];
+    const int k = find_inst_cell(a.inst, a.ninst, cell);
+    const InstDesc& in = a.inst[k];
+    const int par = parity(a.st[k]);
+    const long long lc = cell - in.cell_base;
+    const int ci = (int)(lc % in.imax), cj = (int)(lc / in.imax);
+    const double* un = (init ? a.uh[par] : a.uh[par ^ 1]) + (size_t)cell * P2 * V;
+    __syncthreads();  // the previous cell's readers of U are done
+    for (int p = t; p < P2 * V; p += NT) U[(p % V) * P2 + p / V] = un[p];
+    double cmn = 0.0, cmx = 0.0, lmin = kInf, lmax = -kInf;
+    minmax(in.ph, &cmn, &cmx);
+    if (init) {
+      if (t < V)
+        for (int q = 0; q < P2; ++q) { lmin = fmin(lmin, U[t * P2 + q]); lmax = fmax(lmax, U[t * P2 + q]); }
+    } else {
+      for (int n = 0; n < 9; ++n) {
+        const int in_ = nb_index(ci, n % 3 - 1, in.imax, in.bc[0], in.bc[1]);
+        const int jn_ = nb_index(cj, n / 3 - 1, in.jmax, in.bc[2], in.bc[3]);
+        const long long nc = in.cell_base + in_ + (long long)in.imax * jn_;
+        bool comp = false;
+        if (a.status[par][nc] == 0) {
+#pragma unroll
+          for (int v = 0; v < V; ++v) comp = comp || a.mme[par][(size_t)nc * V + v] > 0.0f;
+        }
+        double lo = 0.0, hi = 0.0;
+        if (comp) {  // uniform over the CTA
+          __syncthreads();
+          const double* nu = a.uh[par] + (size_t)nc * P2 * V;
+          for (int p = t; p < P2 * V; p += NT) U[(p % V) * P2 + p / V] = nu[p];
+          minmax(in.ph, &lo, &hi);
+        } else if (t < V) {
+          lo = a.mm[par][(size_t)nc * 2 * V + t];
+          hi = a.mm[par][(size_t)nc * 2 * V + V + t];
+        }
+        if (t < V) {
+          lmin = fmin(lmin, lo);
+          lmax = fmax(lmax, hi);
+        }
+      }
+    }
+    if (t == 0) flag = 0;
+    __syncthreads();
+    if (t < V) {
+      const double ldiff = fmax(fmax(1.0e-4, 1.0e-3 * (lmax - lmin)), init ? 1.0e-1 : 0.0);
+      if (cmn < lmin - ldiff || cmx > lmax + ldiff) atomicOr(&flag, 1);
+      if (!init) {
+        a.mm[par ^ 1][(size_t)cell * 2 * V + t] = cmn;
+        a.mm[par ^ 1][(size_t)cell * 2 * V + V + t] = cmx;
+        a.mme[par ^ 1][(size_t)cell * V + t] = 0.0f;
+        if (a.lminmax) {
+          a.lminmax[(size_t)cell * 2 * V + t] = lmin;
+          a.lminmax[(size_t)cell * 2 * V + V + t] = lmax;
+        }
+      }
+    }
+    __syncthreads();
+    if (t == 0) atomicAdd(&a.st[k].n_settled, 1);
+    if (flag) {
+      if (init) {
+        // as k_cells' initial limiter: status 1, Lh = the initial subcell data
+        if (t == 0) {
+          a.status[0][cell] = 1;
+          a.status[1][cell] = 1;
+          atomicAdd(&a.st[k].n_recompute, 1);
+        }
+        if (a.lh_ic) {
+          const size_t o = (size_t)cell * S * S * V;
+          for (int q = t; q < S * S * V; q += NT) {
+            a.lh[0][o + q] = a.lh_ic[o + q];
+            a.lh[1][o + q] = a.lh_ic[o + q];
+          }
+        }
+      } else if (t == 0) {
+        a.troubled[cell] = 1;
+        atomicAdd(&a.st[k].n_recompute, 1);
+      }
+    }
   }
 }
 

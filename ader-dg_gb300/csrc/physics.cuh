@@ -80,6 +80,40 @@ struct EulerSys {
     ex = fmax(fmax(fabs(u - c), fabs(u)), fabs(u + c));
     ey = fmax(fmax(fabs(v - c), fabs(v)), fabs(v + c));
   }
+  // Flux F[d*V + v] and maxval(abs(Lambda)) along axis d of one state with a
+  // single reciprocal of the density: algebraically Euler/pde.f90:46-91, used
+  // by the FP32-mixed mode's FP64 subcell re-solve (compiled with fused
+  // multiply-adds; its values agree with the reference order to rounding).
+  template <class T>
+  __device__ static void flux_eig_r(const PhysC<T>& pc, const T* Q, int d, T* F, T& eig) {
+    const T irho = T(1) / Q[0];
+    const T u = Q[1] * irho, v = Q[2] * irho;
+    const T p = pc.gm1 * (Q[3] - T(0.5) * (Q[1] * u + Q[2] * v));
+    if (F) {
+      F[0] = Q[1];
+      F[1] = Q[1] * u + p;
+      F[2] = Q[1] * v;
+      F[3] = u * (Q[3] + p);
+      F[4] = Q[2];
+      F[5] = Q[2] * u;
+      F[6] = Q[2] * v + p;
+      F[7] = v * (Q[3] + p);
+    }
+    const T un = d == 0 ? u : v;
+    const T c = tsqrt(pc.gamma * p * irho);
+    eig = tmax(tabs(un - c), tabs(un + c));
+  }
+  template <class T>
+  __device__ static void flux_r(const PhysC<T>& pc, const T* Q, T* F) {
+    T e;
+    flux_eig_r(pc, Q, 0, F, e);
+  }
+  template <class T>
+  __device__ static T max_eig_r(const PhysC<T>& pc, const T* Q, int d) {
+    T e;
+    flux_eig_r<T>(pc, Q, d, nullptr, e);
+    return e;
+  }
   // Constants of the FP32-mixed cell kernel (CFL eigenvalues, admissibility pre-test).
   struct FConst {
     float gm1, gamma;
@@ -338,6 +372,97 @@ struct BNSys {
   }
   __device__ static void roe_times_jump(const Phys& ph, const double* QL, const double* QR, int d, double* D) {
     roe_times_jump<double>(PhysC<double>(ph), QL, QR, d, D);
+  }
+  // Reciprocal-sharing forms for the FP32-mixed mode's FP64 face flux and
+  // subcell re-solve (compiled with fused multiply-adds; values agree with the
+  // reference order to rounding).  Algebraically the reference expressions of
+  // Baer-Nunziato/pde.f90 with phi = alpha_s (Q8), phi_g = 1 - phi:
+  //   phi p_s = (gamma_s - 1) (Q3 - (Q1^2 + Q2^2) / (2 Q0)) - gamma_s pi_s phi,
+  //   phi rho_s u_s = Q1, (p_s + pi_s) / rho_s = (phi p_s + pi_s phi) / Q0,
+  // and likewise for the gas with Q4..Q7 and phi_g; so a state needs 1/Q0
+  // and 1/Q4 only, both from one reciprocal of Q0 Q4.
+  // Flux F[d*V + v] (pde.f90:74-119) and maxval(abs(Lambda)) along axis d (:125-144).
+  template <class T>
+  __device__ static void flux_eig_r(const PhysC<T>& pc, const T* Q, int d, T* F, T& eig) {
+    const T r = T(1) / (Q[0] * Q[4]);
+    const T i0 = Q[4] * r, i4 = Q[0] * r;
+    const T u_s = Q[1] * i0, v_s = Q[2] * i0, u_g = Q[5] * i4, v_g = Q[6] * i4;
+    const T phi_s = Q[8], phi_g = T(1) - Q[8];
+    const T pps = pc.gs1 * (Q[3] - T(0.5) * (Q[1] * u_s + Q[2] * v_s)) - pc.gsps * phi_s;  // phi p_s
+    const T ppg = pc.gg1 * (Q[7] - T(0.5) * (Q[5] * u_g + Q[6] * v_g)) - pc.ggpg * phi_g;  // phi_g p_g
+    if (F) {
+      F[0] = Q[1]; F[1] = Q[1] * u_s + pps; F[2] = Q[1] * v_s; F[3] = u_s * (Q[3] + pps);
+      F[4] = Q[5]; F[5] = Q[5] * u_g + ppg; F[6] = Q[5] * v_g; F[7] = u_g * (Q[7] + ppg); F[8] = T(0);
+      F[9] = Q[2]; F[10] = Q[2] * u_s; F[11] = Q[2] * v_s + pps; F[12] = v_s * (Q[3] + pps);
+      F[13] = Q[6]; F[14] = Q[6] * u_g; F[15] = Q[6] * v_g + ppg; F[16] = v_g * (Q[7] + ppg); F[17] = T(0);
+    }
+    const T a_s = tsqrt(pc.gs * (pps + pc.ps * phi_s) * i0);
+    const T a_g = tsqrt(pc.gg * (ppg + pc.pg * phi_g) * i4);
+    const T us = d == 0 ? u_s : v_s, ug = d == 0 ? u_g : v_g;
+    eig = tmax(tmax(tabs(ug - a_g), tabs(ug + a_g)), tmax(tabs(us - a_s), tabs(us + a_s)));
+  }
+  template <class T>
+  __device__ static void flux_r(const PhysC<T>& pc, const T* Q, T* F) {
+    T e;
+    flux_eig_r(pc, Q, 0, F, e);
+  }
+  template <class T>
+  __device__ static T max_eig_r(const PhysC<T>& pc, const T* Q, int d) {
+    T e;
+    flux_eig_r<T>(pc, Q, d, nullptr, e);
+    return e;
+  }
+  // p_g = (gamma_g - 1) (Q7 Q4 - (Q5^2 + Q6^2) / 2) / (Q4 phi_g) - gamma_g pi_g
+  // and u_n = qn / Q0 (qn = n . (Q1, Q2)) from one reciprocal of Q0 Q4 phi_g
+  template <class T>
+  __device__ static void p_gas_un_r(const PhysC<T>& pc, const T* Q, T qn, T& p_g, T& un) {
+    const T b = Q[4] * (T(1) - Q[8]);
+    const T r = T(1) / (b * Q[0]);
+    p_g = pc.gg1 * (Q[7] * Q[4] - T(0.5) * (Q[5] * Q[5] + Q[6] * Q[6])) * (Q[0] * r) - pc.ggpg;
+    un = qn * (b * r);
+  }
+  // roe_times_jump with column 9 of B from p_g and u_n of p_gas_un_r
+  template <class T>
+  __device__ static void roe_times_jump_r(const PhysC<T>& pc, const T* QL, const T* QR, int d, T* D) {
+    const double sq = sqrt(15.0) / 10.;
+    const T sGP[3] = {T(0.5 - sq), T(0.5), T(0.5 + sq)};
+    const T wGP[3] = {T(5. / 18.0), T(8. / 18.), T(5. / 18.)};
+    T bp = T(0), bu = T(0), bpu = T(0);  // path integrals of p_g, u_n and p_g u_n
+#pragma unroll
+    for (int g = 0; g < 3; ++g) {
+      T Q[9];
+#pragma unroll
+      for (int v = 0; v < 9; ++v) Q[v] = QL[v] + sGP[g] * (QR[v] - QL[v]);
+      T p, un;
+      p_gas_un_r(pc, Q, d == 0 ? Q[1] : Q[2], p, un);
+      bp = bp + wGP[g] * p;
+      bu = bu + wGP[g] * un;
+      bpu = bpu + wGP[g] * (p * un);
+    }
+    const T dq9 = QR[8] - QL[8];
+    D[0] = T(0);
+    D[1] = d == 0 ? -bp * dq9 : T(0);
+    D[2] = d == 1 ? -bp * dq9 : T(0);
+    D[3] = -bpu * dq9;
+    D[4] = T(0);
+    D[5] = d == 0 ? bp * dq9 : T(0);
+    D[6] = d == 1 ? bp * dq9 : T(0);
+    D[7] = bpu * dq9;
+    D[8] = bu * dq9;
+  }
+  template <class T>
+  __device__ static void src_ncp_r(const PhysC<T>& pc, const T* Q, T ax, T ay, T* S) {
+    T p_g, un;
+    p_gas_un_r(pc, Q, Q[1] * ax + Q[2] * ay, p_g, un);
+    S[0] = T(0);
+    S[1] = p_g * ax;
+    S[2] = p_g * ay;
+    S[3] = p_g * un;
+    S[4] = T(0);
+    S[5] = -(p_g * ax);
+    S[6] = -(p_g * ay);
+    S[7] = -(p_g * un);
+    S[8] = -un;
   }
   // -NCP, Baer-Nunziato/pde.f90:192-231 and :277-290; only the volume-fraction gradient enters
   template <class T>

@@ -5,6 +5,7 @@
 #include <cmath>
 
 #include "faces.cuh"
+#include "limiter.cuh"
 #include "predictor.cuh"
 #include "tables.h"
 
@@ -122,6 +123,34 @@ cudaError_t predictor(const BatchArgs& a, const void* ops, int fp32, bool phase,
   return phase ? launch_pred<double, true>(a, ops, s) : launch_pred<double, false>(a, ops, s);
 }
 
+#if ADERDG_SYS != 0
+// FP32-mixed subcell re-solve: FP64 with the reciprocal-sharing physics forms,
+// compiled here with fused multiply-adds (k_subcell's DMP projections keep
+// the reference order through rounded intrinsics)
+using SubMixed = SubCfg<Sys, N, double>;
+int subcell_grid_mixed(int num_sms) {
+  int per_sm = 0;
+  cudaFuncSetAttribute(k_subcell<Sys, N, double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       SubMixed::SMEM_BYTES);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_subcell<Sys, N, double, true>, SubMixed::THREADS,
+                                                    SubMixed::SMEM_BYTES) != cudaSuccess)
+    per_sm = 1;
+  return (per_sm < 1 ? 1 : per_sm) * num_sms;
+}
+cudaError_t subcell_mixed(const BatchArgs& a, const void* ops, const FaceConst& fc, int grid, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_subcell<Sys, N, double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         SubMixed::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  k_subcell<Sys, N, double, true><<<grid, SubMixed::THREADS, SubMixed::SMEM_BYTES, s>>>(
+      a, *reinterpret_cast<const DevOps<N, double>*>(ops), fc);
+  return cudaGetLastError();
+}
+#endif
+
 #if ADERDG_SYS == 2
 // FP32-mixed faces of Baer-Nunziato: FP32 face states and fluxes, the
 // path-conservative Rusanov flux and its Roe-matrix path integral in FP64
@@ -152,6 +181,10 @@ void ADERDG_CAT(register_predictor_, ADERDG_SYS, ADERDG_N)(KernelTable& t) {
   t.pred_threads[1] = PredCfg<Sys, N, float>::THREADS;
 #if ADERDG_SYS == 2
   t.faces_mixed = &faces_mixed;
+#endif
+#if ADERDG_SYS != 0
+  t.subcell_mixed = &subcell_mixed;
+  t.subcell_grid_mixed = &subcell_grid_mixed;
 #endif
 }
 

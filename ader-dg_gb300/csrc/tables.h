@@ -28,6 +28,10 @@ struct KernelTable {
   // FP32-mixed faces where they differ from the FP32 faces (Baer-Nunziato:
   // FP64 arithmetic on FP32 storage); null: use faces(..., fp32 = 1, ...)
   cudaError_t (*faces_mixed)(const BatchArgs&, const FaceConst&, cudaStream_t) = nullptr;
+  // FP32-mixed subcell re-solve (FP64, reciprocal-sharing physics, fused
+  // multiply-adds) and its persistent grid; null for advection-diffusion
+  cudaError_t (*subcell_mixed)(const BatchArgs&, const void* ops64, const FaceConst&, int grid, cudaStream_t) = nullptr;
+  int (*subcell_grid_mixed)(int num_sms) = nullptr;
   // exact translation unit
   cudaError_t (*faces)(const BatchArgs&, const FaceConst&, int fp32, cudaStream_t) = nullptr;
   cudaError_t (*cells)(const BatchArgs&, const void* ops64, int fast, cudaStream_t) = nullptr;
@@ -35,6 +39,9 @@ struct KernelTable {
   cudaError_t (*mark)(const BatchArgs&, cudaStream_t) = nullptr;
   cudaError_t (*subcell)(const BatchArgs&, const void* ops64, const FaceConst&, int grid, int fp32, cudaStream_t) = nullptr;
   int (*subcell_grid)(int num_sms, int fp32) = nullptr;
+  // FP32-mixed: DMP decisions k_cells left open, from FP64 values (k_settle);
+  // grid CTAs persistent over the list
+  cudaError_t (*settle)(const BatchArgs&, const void* ops64, int grid, cudaStream_t) = nullptr;
 };
 
 // On-device initial field of one simulation (initial.cu): uh at the
@@ -65,7 +72,18 @@ inline cudaError_t launch_faces(const KernelTable* kt, const BatchArgs& a, const
   if (precision == ADERDG_FP32_MIXED && kt->faces_mixed) return kt->faces_mixed(a, fc, s);
   return kt->faces(a, fc, precision != ADERDG_FP64 ? 1 : 0, s);
 }
-// The subcell re-solve runs in FP32 in the FP32-wide mode only.
+// The subcell re-solve of a precision mode: FP32 in the FP32-wide mode, FP64
+// with the reciprocal-sharing physics in the FP32-mixed mode, FP64 in the
+// reference's order otherwise.
 inline int subcell_fp32(int precision) { return precision == ADERDG_FP32_WIDE ? 1 : 0; }
+inline cudaError_t launch_subcell(const KernelTable* kt, const BatchArgs& a, const void* ops64, const FaceConst& fc,
+                                  int grid, int precision, cudaStream_t s) {
+  if (precision == ADERDG_FP32_MIXED && kt->subcell_mixed) return kt->subcell_mixed(a, ops64, fc, grid, s);
+  return kt->subcell(a, ops64, fc, grid, subcell_fp32(precision), s);
+}
+inline int subcell_grid_of(const KernelTable* kt, int num_sms, int precision) {
+  if (precision == ADERDG_FP32_MIXED && kt->subcell_grid_mixed) return kt->subcell_grid_mixed(num_sms);
+  return kt->subcell_grid(num_sms, subcell_fp32(precision));
+}
 
 }  // namespace aderdg

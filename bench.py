@@ -9,36 +9,40 @@ Default workload ("mix"): the seeded request mix -- each request draws its
 system uniformly from {advection-diffusion, Euler vortex, Euler 2D Riemann
 problem, Baer-Nunziato cylinder}, N uniformly from {2,3,4,5}, a square grid
 side log-uniformly from [32, 512] and initial-field parameters jittered by
-+-10% (workloads.request_mix, seed 0); the first --requests of the 1024
-requests, each advanced --steps steps (fixed K).  One bench "step" is one time
-step of every request.
++-10% (workloads.request_mix, seed 0).  One bench "step" is one time step of
+every request.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
                     [--workload mix|euler_vortex|euler_rp2d|bn_cylinder|ad_sine]
 
-Ours:
-  value       batched FP32-mixed throughput, all requests resident in HBM in
-              their (system, N) batches, the batches stepping concurrently on
-              their own streams (wall clock between fully synchronised points;
-              the state, ~tens of GB, is far larger than L2);
-  plain_fp64  the plain single-instance FP64 GPU path on the same requests
-              (one simulation at a time, CUDA events per step, L2 flushed);
-  e2e         the served run through the public API with every request
-              submitted at once: admission with the initial field evaluated on
-              the device (the request's parameters copied host->device), the
-              batched steps, each result copied device->host when its request
-              ends; a second served run with Poisson arrivals at --rate req/s
-              gives the p50/p99 time-to-solution (latency_s);
-  roofline    the dominant kernel of the batched step (k_predictor) against
-              the FP32 (mixed mode) or FP64 FMA peak, from its CUDA-event
-              durations measured live and the flop model
-              predictor_flops_per_cell; in the mixed mode it is bound by the
-              shared-memory wavefronts of its contractions, not by the pipe;
-  cpu_baseline the FP64 CPU restatement of the reference (oracle/), one thread,
-              on a bounded sample of the same requests.
-The reference arm times the same restatement on the host (the Fortran
-reference cannot be built on these machines).  Multi-GPU: requests are
-independent, so N GPUs serve N replicas of the mix (weak scaling).
+Ours (FP32-mixed: the precision split of include/aderdg_gpu.h's
+ADERDG_FP32_MIXED):
+  value        batched throughput of the first --requests requests, all
+               resident in HBM in their (system, N) batches, the batches
+               stepping concurrently on their own streams; K steps timed on the
+               device (the state, tens of GB, is far larger than L2);
+  error_vs_fp64  every one of those requests against its own run on the plain
+               FP64 path after the same W + K steps: relative L1 / L-infinity
+               of uh and the limited-cell counts;
+  fp32_wide    the same for the ADERDG_FP32_WIDE split, labelled separately;
+  plain_fp64   the plain single-instance FP64 GPU path on the same requests
+               (one simulation at a time, CUDA events per step, L2 flushed);
+  e2e          the served run through the public API, --serve-requests (1024)
+               requests of K steps submitted at once: admission with the
+               initial field evaluated on the device (the request's parameters
+               copied host->device), the batched steps, each result copied
+               device->host when its request ends; e2e.rates / latency_s: the
+               same requests arriving as Poisson processes at each --rates
+               rate, with throughput and p50/p99 time-to-solution;
+  roofline     the predictor (k_predictor) of the batched step against the
+               FP32 FMA peak, from its CUDA-event duration measured live and
+               the flop model predictor_flops_per_cell;
+  cpu_baseline the reference arm's sample on one host core.
+The reference arm (--impl reference) times the FP64 CPU restatement of the
+reference (oracle/; the Fortran cannot be built on these machines) on all host
+cores with one wall clock around the timed steps.  Multi-GPU: requests are
+independent, so rank r serves requests r, r + N, ... (weak scaling; no
+collective beyond the barrier and the timing reductions).
 """
 import argparse
 import json
@@ -60,19 +64,21 @@ NVAR = {0: 1, 1: 4, 2: 9}
 
 def parse():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--gpus", type=int, default=1, help="ranks (launch with torchrun for more than one)")
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="mix")
-    ap.add_argument("--requests", type=int, default=128)
-    ap.add_argument("--rate", type=float, default=100.0)
+    ap.add_argument("--requests", type=int, default=128, help="resident requests per rank (value)")
+    ap.add_argument("--serve-requests", type=int, default=1024, help="served requests in total (e2e, rates)")
+    ap.add_argument("--rates", default="10,30,100,300,500", help="Poisson arrival rates swept, requests/s")
     ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32"])
     ap.add_argument("--side", type=int, default=0)
     ap.add_argument("--hbm-budget-gb", type=float, default=160.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-wide", action="store_true", help="skip the FP32-wide comparison run")
     ap.add_argument("--host-setup", action="store_true", help="serve with host-projected initial fields")
     ap.add_argument("--to-tend", action="store_true",
                     help="single workload: also run it from t=0 to its end time (time-to-solution, exact-solution error)")
@@ -211,9 +217,12 @@ def allmax(dist, x):
     return float(t.item())
 
 
-def mix_specs(n):
+def mix_specs(n, rank=0, ws=1):
+    """Rank `rank`'s shard of the first n * ws requests of the seeded mix
+    (requests r, r + ws, ...): the ranks serve disjoint requests."""
     import aderdg
-    return aderdg.workloads.request_mix(1024, seed=0)[:n]
+    total = n * ws
+    return aderdg.workloads.request_mix(max(total, 1024), seed=0)[:total][rank::ws]
 
 
 def spec_config(aderdg, spec, precision):
@@ -221,94 +230,120 @@ def spec_config(aderdg, spec, precision):
     return cfg, ic
 
 
-def oracle_rate(specs, budget_s=20.0, side_cap=48, steps=1):
-    """DOF-updates/s of the FP64 oracle, one thread, over `specs` with grid
-    sides capped at side_cap (same N, system and cell count per side; the
-    cost per DOF does not depend on the number of cells), bounded by budget_s."""
+# ---------------------------------------------------------------- CPU arms
+CPU_SIDE_CAP = 32  # grid side cap of the CPU samples (the cost per DOF does not depend on the cell count)
+
+
+def _cpu_oracle(spec, side_cap):
+    """An oracle on the projected initial field (and initial limiter) of one
+    request with its grid side capped; returns (oracle, DOFs per step)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import aderdg
     import pyoracle as po
-    dofs, el, used = 0, 0.0, 0
-    for spec in specs:
-        if el > budget_s:
-            break
-        cfg, ic, _, _ = aderdg.workloads.make(spec["name"], side=min(spec["side"], side_cap), N=spec["N"])
-        oc = po.make_config(cfg.system, cfg.N, cfg.imax, cfg.jmax, xl=cfg.xl, xr=cfg.xr, bc=cfg.bc, cfl=cfg.cfl,
-                            gamma=cfg.gamma, gamma_s=cfg.gamma_s, gamma_g=cfg.gamma_g, pi_s=cfg.pi_s,
-                            pi_g=cfg.pi_g, cx=cfg.cx, cy=cfg.cy, a=cfg.a, ad_flux_mode=cfg.ad_flux_mode,
-                            limiter=cfg.limiter)
-        o = po.Oracle(oc)
-        uh, lh = o.project_ic(ic, spec["params"])
-        o.set(po.UH, uh)
-        if cfg.limiter and cfg.system != 0:
-            o.init_limiter(lh)
-        t = 0.0
-        t0 = time.perf_counter()
-        for _ in range(steps):
-            t, _, _ = o.step(t, spec["tend"])
-        el += time.perf_counter() - t0
-        dofs += cfg.dofs * steps
-        used += 1
-    return dofs / el, used, el
+    cfg, ic, _, _ = aderdg.workloads.make(spec["name"], side=min(spec["side"], side_cap), N=spec["N"])
+    oc = po.make_config(cfg.system, cfg.N, cfg.imax, cfg.jmax, xl=cfg.xl, xr=cfg.xr, bc=cfg.bc, cfl=cfg.cfl,
+                        gamma=cfg.gamma, gamma_s=cfg.gamma_s, gamma_g=cfg.gamma_g, pi_s=cfg.pi_s, pi_g=cfg.pi_g,
+                        cx=cfg.cx, cy=cfg.cy, a=cfg.a, ad_flux_mode=cfg.ad_flux_mode, limiter=cfg.limiter)
+    o = po.Oracle(oc)
+    uh, lh = o.project_ic(ic, spec["params"])
+    o.set(po.UH, uh)
+    if cfg.limiter and cfg.system != 0:
+        o.init_limiter(lh)
+    return o, cfg.dofs
+
+
+def _cpu_worker(job):
+    """One host core of a CPU arm: set up its requests' oracles and take the
+    warm-up steps (untimed), wait for the other cores, then take `steps` steps
+    of each request; returns (start, end, DOF-updates) of the timed part.
+    perf_counter is CLOCK_MONOTONIC, comparable across processes."""
+    specs, side_cap, warmup, steps, barrier = job
+    sims = [_cpu_oracle(s, side_cap) + (s["tend"],) for s in specs]
+    t = [0.0] * len(sims)
+    for k, (o, _, tend) in enumerate(sims):
+        for _ in range(warmup):
+            t[k], _, _ = o.step(t[k], tend)
+    if barrier is not None:
+        barrier.wait()
+    t0 = time.perf_counter()
+    dofs = 0
+    for _ in range(steps):
+        for k, (o, d, tend) in enumerate(sims):
+            t[k], _, _ = o.step(t[k], tend)
+            dofs += d
+    t1 = time.perf_counter()
+    if barrier is not None:
+        barrier.wait()
+    return t0, t1, dofs
+
+
+CPU_SET = 8       # requests every core steps (the first of the mix)
+
+
+def cpu_arm(specs, cores, side_cap, warmup, steps):
+    """The FP64 CPU restatement of the reference (oracle/) on `cores` host
+    cores, every core stepping its own copy of the requests `specs` (the same
+    work on every core, so that no core idles while another finishes); one
+    wall clock from the first core's start to the last core's end, after every
+    core has built its oracles and taken its warm-up steps.  Returns
+    (DOF-updates/s, wall seconds, DOF-updates)."""
+    import multiprocessing as mp
+    shards = [list(specs) for _ in range(cores)]
+    if len(shards) == 1:
+        t0, t1, dofs = _cpu_worker((shards[0], side_cap, warmup, steps, None))
+        return dofs / (t1 - t0), t1 - t0, dofs
+    ctx = mp.get_context("spawn")
+    with ctx.Manager() as mgr:
+        bar = mgr.Barrier(len(shards))
+        with ctx.Pool(len(shards)) as pool:
+            res = pool.map(_cpu_worker, [(sh, side_cap, warmup, steps, bar) for sh in shards])
+    wall = max(r[1] for r in res) - min(r[0] for r in res)
+    dofs = sum(r[2] for r in res)
+    return dofs / wall, wall, dofs
 
 
 # ---------------------------------------------------------------- arms
-def _oracle_worker(job):
-    """One process of the reference arm: oracle steps of one request."""
-    spec, side_cap, steps = job
-    rate, _, el = oracle_rate([spec], budget_s=1e9, side_cap=side_cap, steps=steps)
-    return rate
-
-
 def run_reference(args):
-    """The FP64 CPU restatement on all host cores: one process per core, each
-    stepping one request of the mix (requests are independent)."""
-    import multiprocessing as mp
-    dist, rank, ws, _ = dist_init()
+    """The reference's CPU path: the FP64 restatement of the Fortran solvers
+    (oracle/; the Fortran cannot be compiled on these machines) on all host
+    cores, one request per core from the mix, grid sides capped at 32.  A bench
+    step is one time step of every core's request; value = DOF-updates over the
+    wall clock of the timed steps."""
+    dist, rank, ws, _ = dist_init("gloo")
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        if args.workload == "mix":
-            specs = mix_specs(args.requests)
-            jobs = lambda k: [(specs[(cores * k + q) % len(specs)], 40, 2) for q in range(cores)]  # noqa: E731
-            sample = ("per step: two oracle steps of each of %d requests of the mix at once (one per core, rotating "
-                      "through the first %d), grid sides capped at 40; FP64" % (cores, args.requests))
-            cfg_desc = {"workload": "mix", "requests": args.requests, "steps_per_request": args.steps}
-        else:
-            import aderdg
-            cfg, ic, params, tend = aderdg.workloads.make(args.workload, side=args.side or None)
-            spec = dict(name=args.workload, N=cfg.N, side=cfg.imax, params=params, tend=tend)
-            jobs = lambda k: [(spec, 64, 2)] * cores  # noqa: E731
-            sample = "per step: two oracle steps of a 64x64 grid of the workload on each of %d cores; FP64" % cores
-            cfg_desc = {"workload": args.workload, "N": cfg.N, "grid": [cfg.imax, cfg.jmax]}
-        for k in range(args.warmup):
-            pool.map(_oracle_worker, [(j[0], 16, 1) for j in jobs(k)])
-        rates = []
-        t0 = time.perf_counter()
-        for k in range(args.steps):
-            # cores step their requests at once: the aggregate rate is the sum of theirs
-            rates.append(sum(pool.map(_oracle_worker, jobs(k))))
-        el = time.perf_counter() - t0
-    val = float(np.mean(rates))
+    if args.workload == "mix":
+        specs = mix_specs(CPU_SET)
+        sample = ("on each of %d cores, the first %d requests of the mix (request_mix seed 0) with grid sides capped "
+                  "at %d; %d untimed warm-up steps, then %d timed steps of every request; FP64"
+                  % (cores, CPU_SET, CPU_SIDE_CAP, args.warmup, args.steps))
+        cfg_desc = {"workload": "mix (served/batched request mix): the first %d requests, grid sides capped at %d, "
+                                "on every host core" % (CPU_SET, CPU_SIDE_CAP), "requests": CPU_SET * cores}
+    else:
+        import aderdg
+        cfg, ic, params, tend = aderdg.workloads.make(args.workload, side=args.side or None)
+        specs = [dict(name=args.workload, N=cfg.N, side=cfg.imax, params=params, tend=tend)]
+        sample = ("the workload on a %dx%d grid on each of %d cores; %d warm-up + %d timed steps; FP64"
+                  % (CPU_SIDE_CAP, CPU_SIDE_CAP, cores, args.warmup, args.steps))
+        cfg_desc = {"workload": args.workload, "N": cfg.N, "grid": [CPU_SIDE_CAP, CPU_SIDE_CAP]}
+    val, wall, dofs = cpu_arm(specs, cores, CPU_SIDE_CAP, args.warmup, args.steps)
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": el / max(args.steps, 1) * 1e3, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": wall / max(args.steps, 1) * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: projected initial fields of the seeded request mix (deterministic)",
-            "config": cfg_desc,
+            "config": cfg_desc, "dof_updates_per_step": dofs / max(args.steps, 1),
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def run_mix(args, aderdg, dist, rank, ws, lr):
-    prec = aderdg.FP32_MIXED if args.precision == "fp32" else aderdg.FP64
-    specs = mix_specs(args.requests)
-    K, W = args.steps, args.warmup
-    # ---- batched, resident: every request admitted into its (system, N) batch
-    groups, members = {}, []
-    need = {}
+def _resident(aderdg, specs, prec, W, K):
+    """Every request of `specs` admitted into its (system, N) batch (initial
+    field evaluated on the device), W untimed steps, then K steps of all the
+    batches concurrently, timed on the device.  Returns (groups, slots,
+    seconds, DOF-updates in the timed steps, DOFs per step)."""
+    groups, members, need = {}, [], {}
     for spec in specs:
         cfg, ic = spec_config(aderdg, spec, prec)
         key = (cfg.system, cfg.N)
@@ -318,112 +353,100 @@ def run_mix(args, aderdg, dist, rank, ws, lr):
         lim = 0 if key[0] == aderdg.SYS_ADVDIFF else 1
         groups[key] = aderdg.Batch(key[0], key[1], prec, lim, capacity_units=units + 16,
                                    max_instances=sum(1 for m in members if m[3] == key) + 1)
-    total_dofs = 0
-    bytes_in = 0
-    slots = []
+    slots, total_dofs = [], 0
     for spec, cfg, ic, key in members:
-        uh, lh = aderdg.project_initial_condition(cfg, ic, spec["params"])
-        lim = cfg.limiter and cfg.system != aderdg.SYS_ADVDIFF
-        slot = groups[key].admit(cfg, uh, lh if lim else None, spec["tend"], W + K + 1)
+        # W + K steps, one more for the per-launch profile afterwards
+        slot = groups[key].admit_ic(cfg, ic, spec["params"], spec["tend"], W + K + 1)
         assert slot is not None
-        slots.append((key, slot, cfg.dofs))
+        slots.append((key, slot, cfg))
         total_dofs += cfg.dofs
-        bytes_in += uh.nbytes + (lh.nbytes if lim else 0)
     for g in groups.values():
         g.launch(W)
     for g in groups.values():
         g.sync()
     steps0 = [groups[key].query(slot)["steps"] for key, slot, _ in slots]
-    barrier(dist)
-    with ClockSampler(lr) as clk:
-        # CUDA events on a timing stream that every group's stream waits for
-        # and that waits for all of them (the groups run concurrently)
-        batched_s = aderdg.Batch.run_timed(list(groups.values()), K) * 1e-3
+    secs = aderdg.Batch.run_timed(list(groups.values()), K) * 1e-3
     for g in groups.values():
         g.sync()
-    batched_s = allmax(dist, batched_s)
-    barrier(dist)
-    # DOF-updates actually done in the timed region (a request that reaches its end time stops early)
-    updates = sum(d * (groups[key].query(slot)["steps"] - s0) for (key, slot, d), s0 in zip(slots, steps0))
-    value = updates * ws / batched_s
-    # dominant kernel: per-launch device times of one more (eager) step of every group
-    phase_tot = {}
-    pred_flops = 0.0
-    for key, g in groups.items():
-        ph = g.profile()
-        for k, v in ph.items():
-            phase_tot[k] = phase_tot.get(k, 0.0) + v
-    for spec, cfg, ic, key in members:
-        pred_flops += predictor_flops_per_cell(cfg.system, cfg.N, ad_fused=cfg.ad_flux_mode != 0) * cfg.cells
-    dev_bytes = sum(g.info()["device_bytes"] for g in groups.values())
+    updates = sum(cfg.dofs * (groups[key].query(slot)["steps"] - s0) for (key, slot, cfg), s0 in zip(slots, steps0))
+    return groups, slots, secs, updates, total_dofs
+
+
+def _profile_groups(groups):
+    """Per-launch device ms of one more (eager) step of every group, summed."""
+    tot = {}
     for g in groups.values():
-        g.close()
-    if rank != 0:
-        return None
-    fp64_peak, fp32_peak = aderdg.probe_peaks()
-    mixed = prec == aderdg.FP32_MIXED
-    peak = fp32_peak if mixed else fp64_peak
-    pred_ms = phase_tot.get("predictor", 0.0)
-    kern_ms = {k: v for k, v in phase_tot.items() if k not in ("begin", "end")}
-    dominant = max(kern_ms, key=lambda k: kern_ms[k])
-    ach = pred_flops / (pred_ms * 1e-3) / 1e9 if pred_ms > 0 else None
-    roof = {"bound": "fp32" if mixed else "fp64", "kernel": "k_predictor (all (system, N) groups of the mix)",
-            "achieved": ach, "peak": peak, "unit": "GFLOP/s", "frac": (ach / peak) if ach else None,
-            "peak_source": "FMA throughput measured on this GPU by aderdg_probe_peaks (dependent-FMA "
-                           "microkernel); MEASURED_PEAKS.json carries no non-tensor FP32/FP64 figure",
-            "flops_per_launch": pred_flops, "flop_model": "bench.py predictor_flops_per_cell x cells",
-            "launch_ms": pred_ms, "dominant_phase": dominant,
-            "phase_share": {k: v / sum(kern_ms.values()) for k, v in kern_ms.items()},
-            "phase_ms_one_step": phase_tot, "traffic": None,
-            "limiter": ("FP32: shared-memory wavefronts of the flux contractions (79% of peak, FP32 pipe 46%, in the "
-                        "ncu capture of profiles/k_predictor_k_cells_euler_vortex_256_N4.md); FP64: the FP64 pipe"
-                        if mixed else "the FP64 pipe (90% busy in profiles/k_predictor_k_cells_euler_vortex_256_N4.md)")}
-    try:
-        with open(os.path.join(REPO, "profiles", "traffic.json")) as fh:
-            tr = json.load(fh)
-        per = tr.get("k_predictor_fp32mixed_bytes_per_dof" if mixed else "k_predictor_fp64_bytes_per_dof")
-        if per:
-            roof["traffic"] = per * total_dofs
-            roof["traffic_note"] = ("DRAM bytes per DOF of k_predictor from one ncu capture (profiles/traffic.json), "
-                                    "times the DOFs of the mix")
-    except (OSError, ValueError):
-        pass
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
-            "ms_per_step": batched_s / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32+f64" if prec == aderdg.FP32_MIXED else "f64",
-            "data": "synthetic: seeded request mix (request_mix seed 0), projected initial fields; no dataset",
-            "config": {"workload": "mix (served/batched request mix)", "requests": len(specs),
-                       "steps_per_request": K, "dofs_per_step": total_dofs,
-                       "dof_updates_timed": updates, "groups": len(groups),
-                       "precision": args.precision, "l2": "state (%.1f GB on device) far larger than L2" %
-                       (dev_bytes / 1e9), "parallelism": "replicas" if ws > 1 else "single",
-                       "arrival_rate_per_s": args.rate},
-            "roofline": roof, "clocks": clk.summary(),
-            "gpu_launches": sum(7 if k[0] != 0 else 5 for k in groups) * K}
-    return line
+        for k, v in g.profile().items():
+            tot[k] = tot.get(k, 0.0) + v
+    return tot
 
 
-def run_plain_fp64(aderdg, specs, steps):
-    """The plain single-instance FP64 path: one simulation at a time, CUDA
-    events per step, L2 flushed before every timed step."""
+def _launches_per_step(groups, prec, aderdg):
+    """Kernel launches of one step of every group: control, predictor, faces,
+    cells, [settle (FP32-mixed), mark, subcell,] control."""
+    n = 0
+    for key in groups:
+        if key[0] == aderdg.SYS_ADVDIFF:
+            n += 5
+        else:
+            n += 8 if prec == aderdg.FP32_MIXED else 7
+    return n
+
+
+def _err_stats(errs):
+    """Summary of the per-request errors against the FP64 path."""
+    l1 = np.array([e["rel_l1"] for e in errs])
+    li = np.array([e["rel_linf"] for e in errs])
+    lim64 = sum(e["limited_fp64"] for e in errs)
+    dcount = sum(abs(e["limited"] - e["limited_fp64"]) for e in errs)
+    return {"requests": len(errs), "max_l1": float(l1.max()), "p99_l1": float(np.percentile(l1, 99)),
+            "median_l1": float(np.median(l1)), "max_linf": float(li.max()),
+            "max_count_diff_pct": float(max(100.0 * abs(e["limited"] - e["limited_fp64"]) / max(e["limited_fp64"], 1)
+                                            for e in errs)),
+            "total_count_diff_pct": 100.0 * dcount / max(lim64, 1),
+            "limited_cells_fp64": lim64, "mask_disagreements": sum(e["mask_diff"] for e in errs),
+            "what": "per request, after the same steps from the same initial state: relative L1 (sum|u - u64| / "
+                    "sum|u64|) and L-infinity (max|u - u64| / max|u64|) of uh against the plain FP64 GPU path; "
+                    "limited cells (status != 0) against the FP64 path's"}
+
+
+def run_plain_fp64(aderdg, specs, W, K, compare):
+    """The plain single-instance FP64 path: one simulation at a time, W
+    untimed steps, then K steps timed with CUDA events, L2 flushed before each.
+    After them, each request's state is compared with its state in every
+    batch run of `compare` ({label: (groups, slots)}, the same W + K steps)."""
     dofs, ms = 0, 0.0
-    for spec in specs:
+    errs = {lab: [] for lab in compare}
+    for k, spec in enumerate(specs):
         cfg, ic = spec_config(aderdg, spec, aderdg.FP64)
-        uh, lh = aderdg.project_initial_condition(cfg, ic, spec["params"])
         s = aderdg.Solver(cfg)
-        s.upload(uh)
-        if cfg.limiter and cfg.system != aderdg.SYS_ADVDIFF:
-            s.init_limiter(lh)
-        t, _, _ = s.step(0.0, spec["tend"])
-        t, st = s.time_steps(t, spec["tend"], steps, flush_l2=True)
-        dofs += cfg.dofs * steps
+        s.initial_condition(ic, spec["params"])
+        t = 0.0
+        for _ in range(W):
+            t, _, _ = s.step(t, spec["tend"])
+        t, st = s.time_steps(t, spec["tend"], K, flush_l2=True)
+        dofs += cfg.dofs * K
         ms += float(st.sum())
+        u64, s64 = s.download()
         s.close()
-    return dofs / (ms * 1e-3), ms
+        n64 = int((s64 != 0).sum())
+        for lab, (groups, slots) in compare.items():
+            key, slot, _ = slots[k]
+            u = groups[key].download(slot)
+            stt = groups[key].download_status(slot)
+            den1, deni = float(np.abs(u64).sum()), float(np.abs(u64).max())
+            errs[lab].append({"rel_l1": float(np.abs(u - u64).sum()) / (den1 if den1 > 0 else 1.0),
+                              "rel_linf": float(np.abs(u - u64).max()) / (deni if deni > 0 else 1.0),
+                              "limited": int((stt != 0).sum()), "limited_fp64": n64,
+                              "mask_diff": int(((stt != 0) != (s64 != 0)).sum())})
+    return dofs / (ms * 1e-3), ms, errs
+
+
+
 
 
 def run_served(aderdg, args, specs, prec, rate):
-    """Continuous batching of the mix: Poisson arrivals at `rate` requests/s
+    """Continuous batching of `specs`: Poisson arrivals at `rate` requests/s
     (inf: all at once), initial fields evaluated on the device at admission
     (the request's parameters cross to the device), each result downloaded to
     the host when its request ends."""
@@ -432,7 +455,7 @@ def run_served(aderdg, args, specs, prec, rate):
     rep = srv.run(specs, rate=rate, seed=0, max_steps=args.steps)
     rep.pop("requests_done")
     srv.close()
-    return rep, rep["h2d_bytes"], rep["d2h_bytes"]
+    return rep
 
 
 def run_single(args, aderdg, dist, rank, ws, lr):
@@ -508,8 +531,140 @@ def run_to_tend(aderdg, cfg, ic, params, tend):
     return out
 
 
+def allsum(dist, x):
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def _traffic(aderdg, groups, mode_key):
+    """DRAM bytes of one k_predictor launch per group from the per-(system, N)
+    captures in profiles/traffic.json (bytes per DOF, times the group's DOFs),
+    and the limiter the captures name; (None, None) without a capture."""
+    try:
+        with open(os.path.join(REPO, "profiles", "traffic.json")) as fh:
+            tr = json.load(fh)
+    except (OSError, ValueError):
+        return None, None
+    per = tr.get("k_predictor_bytes_per_dof", {}).get(mode_key, {})
+    tot, miss = 0.0, 0
+    for key, dofs in groups.items():
+        b = per.get("%d_%d" % key)
+        if b is None:
+            miss += 1
+        else:
+            tot += b * dofs
+    return (tot if miss == 0 else None), tr.get("k_predictor_limiter", {}).get(mode_key)
+
+
+def run_mix(args, aderdg, dist, rank, ws, lr):
+    """The seeded request mix, resident: `value` (FP32-mixed), the FP32-wide
+    split beside it, the plain FP64 path on the same requests, and every
+    request's error against its FP64 run."""
+    W, K = args.warmup, args.steps
+    specs = mix_specs(args.requests, rank, ws)
+    if args.precision == "fp64":
+        modes = [("fp64", aderdg.FP64)]
+    else:
+        modes = [("fp32_mixed", aderdg.FP32_MIXED)] + ([] if args.no_wide else [("fp32_wide", aderdg.FP32_WIDE)])
+    runs, clk_samples = {}, []
+    for lab, prec in modes:
+        barrier(dist)
+        with ClockSampler(lr) as clk:
+            groups, slots, secs, updates, total_dofs = _resident(aderdg, specs, prec, W, K)
+        clk_samples += clk.samples
+        secs = allmax(dist, secs)
+        updates = allsum(dist, updates)
+        runs[lab] = dict(prec=prec, groups=groups, slots=slots, secs=secs, updates=updates, dofs=total_dofs)
+    barrier(dist)
+    compare = {lab: (r["groups"], r["slots"]) for lab, r in runs.items() if r["prec"] != aderdg.FP64}
+    plain = None
+    if not args.no_plain:
+        plain = run_plain_fp64(aderdg, specs, W, K, compare)
+    for r in runs.values():
+        r["phases"] = _profile_groups(r["groups"])
+        r["group_dofs"] = {}
+        for key, slot, cfg in r["slots"]:
+            r["group_dofs"][key] = r["group_dofs"].get(key, 0) + cfg.dofs
+        r["dev_bytes"] = sum(g.info()["device_bytes"] for g in r["groups"].values())
+        r["launches"] = _launches_per_step(r["groups"], r["prec"], aderdg)
+        for g in r["groups"].values():
+            g.close()
+        r["groups"] = None
+    plain_rate = allsum(dist, plain[0]) if plain else None
+    if rank != 0:
+        return None
+    head_lab = modes[0][0]
+    head = runs[head_lab]
+    clk = ClockSampler(lr)
+    clk.samples = clk_samples
+    fp64_peak, fp32_peak = aderdg.probe_peaks()
+    mixed = head["prec"] != aderdg.FP64
+    peak = fp32_peak if mixed else fp64_peak
+    pred_flops = sum(predictor_flops_per_cell(cfg.system, cfg.N, ad_fused=cfg.ad_flux_mode != 0) * cfg.cells
+                     for _, _, cfg in head["slots"])
+    ph = head["phases"]
+    kern_ms = {k: v for k, v in ph.items() if k not in ("begin", "end")}
+    pred_ms = ph.get("predictor", 0.0)
+    ach = pred_flops / (pred_ms * 1e-3) / 1e9 if pred_ms > 0 else None
+    traffic, limiter = _traffic(aderdg, head["group_dofs"], "fp32" if mixed else "fp64")
+    roof = {"bound": "fp32" if mixed else "fp64", "kernel": "k_predictor (all (system, N) groups of the mix)",
+            "achieved": ach, "peak": peak, "unit": "GFLOP/s", "frac": (ach / peak) if ach else None,
+            "peak_source": "FMA throughput measured on this GPU by aderdg_probe_peaks (dependent-FMA "
+                           "microkernel); MEASURED_PEAKS.json carries no non-tensor FP32/FP64 figure",
+            "flops_per_launch": pred_flops, "flop_model": "bench.py predictor_flops_per_cell x cells",
+            "launch_ms": pred_ms, "dominant_phase": max(kern_ms, key=lambda k: kern_ms[k]),
+            "phase_share": {k: v / sum(kern_ms.values()) for k, v in kern_ms.items()},
+            "phase_ms_one_step": ph, "traffic": traffic,
+            "traffic_source": "profiles/traffic.json: DRAM bytes per DOF of k_predictor per (system, N) group from "
+                              "one ncu capture of the batched mix, times each group's DOFs",
+            "limiter": limiter}
+    value = head["updates"] / head["secs"]
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
+            "ms_per_step": head["secs"] / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64" if mixed else "f64",
+            "data": "synthetic: seeded request mix (request_mix seed 0), initial fields evaluated on the device; "
+                    "no dataset",
+            "config": {"workload": "mix: the first %d of the 1024 seeded requests%s, all resident in HBM in their "
+                                   "(system, N) batches, K steps each" % (args.requests * ws,
+                                                                         " (sharded over the ranks)" if ws > 1 else ""),
+                       "requests": args.requests * ws, "steps_per_request": K, "dofs_per_step": head["dofs"],
+                       "dof_updates_timed": head["updates"], "groups": len(head["group_dofs"]),
+                       "precision": head_lab, "l2": "state (%.1f GB on device) far larger than L2" %
+                       (head["dev_bytes"] / 1e9), "parallelism": "request shards, no collective" if ws > 1 else
+                       "single", "serving": "config 5: %d requests, Poisson rates %s req/s (e2e.rates)" %
+                       (args.serve_requests, args.rates)},
+            "roofline": roof, "clocks": clk.summary(), "gpu_launches": head["launches"] * K}
+    for lab, r in runs.items():
+        if lab == head_lab:
+            continue
+        line[lab] = {"value": r["updates"] / r["secs"], "unit": UNIT, "ms_per_step": r["secs"] / K * 1e3,
+                     "phase_ms_one_step": r["phases"],
+                     "what": "the same resident mix with the Baer-Nunziato face flux and the subcell re-solve in "
+                             "FP32 and uncertified FP32 DMP comparisons (ADERDG_FP32_WIDE)"}
+    if plain:
+        rate, ms, errs = plain
+        line["plain_fp64"] = {"value": plain_rate, "unit": UNIT, "steps_per_request": K,
+                              "what": "single-instance FP64 path, one request at a time, same requests, L2 flushed"}
+        line["batched_over_plain_fp64"] = value / plain_rate
+        for lab, e in errs.items():
+            tgt = line if lab == head_lab else line[lab]
+            tgt["error_vs_fp64"] = _err_stats(e)
+            if lab != head_lab:
+                tgt["over_plain_fp64"] = tgt["value"] / plain_rate
+    return line
+
+
 def run_ours(args):
     dist, rank, ws, lr = dist_init()
+    if args.gpus != ws:
+        print("bench.py --gpus %d: launch it with torchrun --nproc-per-node %d (WORLD_SIZE is %d)"
+              % (args.gpus, args.gpus, ws), file=sys.stderr, flush=True)
+        sys.exit(2)
     import aderdg
     aderdg.build()
     if args.workload != "mix":
@@ -518,38 +673,53 @@ def run_ours(args):
             print(json.dumps(line), flush=True)
         return
     line = run_mix(args, aderdg, dist, rank, ws, lr)
+    prec = aderdg.FP64 if args.precision == "fp64" else aderdg.FP32_MIXED
+    serve = mix_specs(args.serve_requests // ws, rank, ws) if args.serve_requests >= ws else []
+    served = {}
+    if not args.no_serve and serve:
+        # e2e: the served requests all submitted at once through the serving
+        # API; then Poisson arrivals at each rate of the sweep (each rank takes
+        # its share of the arrival stream)
+        rates = [float(x) for x in args.rates.split(",") if x]
+        for rate in [float("inf")] + rates:
+            barrier(dist)
+            rep = run_served(aderdg, args, serve, prec, rate / ws)
+            makespan = allmax(dist, rep["makespan_s"])
+            served[rate] = dict(rep, makespan_s=makespan,
+                                dof_updates_per_s=allsum(dist, rep["dof_updates"]) / makespan)
     if rank != 0:
         return
-    prec = aderdg.FP32_MIXED if args.precision == "fp32" else aderdg.FP64
-    specs = mix_specs(args.requests)
-    if not args.no_serve:
-        # e2e: every request submitted at once through the serving API (the
-        # throughput of `value`, end to end); latency: Poisson arrivals at --rate
+    if served:
         api = ("aderdg_batch_admit_ic / launch / sync / download / release (continuous batching)"
                if not args.host_setup else
                "aderdg_batch_admit / launch / sync / download / release (continuous batching)")
-        rep, h2d, d2h = run_served(aderdg, args, specs, prec, float("inf"))
-        line["e2e"] = {"value": rep["dof_updates_per_s"], "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
-                       "d2h_bytes_per_step": d2h / args.steps, "api": api,
-                       "arrivals": "all requests at t = 0", "makespan_s": rep["makespan_s"],
-                       "tts_p50_s": rep["tts_p50_s"], "tts_p99_s": rep["tts_p99_s"], "requests": rep["requests"]}
-        rp, _, _ = run_served(aderdg, args, specs, prec, args.rate)
-        line["e2e"]["poisson"] = {"rate_per_s": args.rate, "value": rp["dof_updates_per_s"],
-                                  "makespan_s": rp["makespan_s"]}
-        line["latency_s"] = {"p50": rp["tts_p50_s"], "p99": rp["tts_p99_s"],
-                             "what": "time to solution, arrival to result on the host, Poisson arrivals at %.0f/s"
-                                     % args.rate}
-    if not args.no_plain:
-        plain_steps = min(args.steps, 10)
-        rate, ms = run_plain_fp64(aderdg, specs, plain_steps)
-        line["plain_fp64"] = {"value": rate, "unit": UNIT, "steps_per_request": plain_steps,
-                              "what": "single-instance FP64 path, one request at a time, same requests"}
-        line["batched_over_plain_fp64"] = line["value"] / rate
+        burst = served[float("inf")]
+        line["e2e"] = {"value": burst["dof_updates_per_s"], "unit": UNIT,
+                       "h2d_bytes_per_step": burst["h2d_bytes"] / args.steps,
+                       "d2h_bytes_per_step": burst["d2h_bytes"] / args.steps, "api": api,
+                       "arrivals": "all %d requests at t = 0" % args.serve_requests,
+                       "makespan_s": burst["makespan_s"], "tts_p50_s": burst["tts_p50_s"],
+                       "tts_p99_s": burst["tts_p99_s"], "requests": burst["requests"], "failed": burst["failed"],
+                       "steps_per_request": args.steps,
+                       "rates": [{"rate_per_s": r, "dof_updates_per_s": v["dof_updates_per_s"],
+                                  "tts_p50_s": v["tts_p50_s"], "tts_p99_s": v["tts_p99_s"],
+                                  "makespan_s": v["makespan_s"], "requests": v["requests"], "failed": v["failed"]}
+                                 for r, v in served.items() if np.isfinite(r)]}
+        mid = [v for r, v in served.items() if np.isfinite(r)]
+        line["latency_s"] = {"per_rate": {"%g" % r: {"p50": v["tts_p50_s"], "p99": v["tts_p99_s"]}
+                                          for r, v in served.items() if np.isfinite(r)},
+                             "what": "time to solution, arrival to result on the host, %d requests of %d steps, "
+                                     "Poisson arrivals" % (args.serve_requests, args.steps)}
+        if mid:
+            line["latency_s"].update(p50=float(np.median([v["tts_p50_s"] for v in mid])),
+                                     p99=float(max(v["tts_p99_s"] for v in mid)))
     if not args.no_cpu_baseline:
-        rate, used, el = oracle_rate(specs, budget_s=20.0, side_cap=48)
+        rate, wall, dofs = cpu_arm(mix_specs(CPU_SET), 1, CPU_SIDE_CAP, args.warmup, args.steps)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
-                                "sample": "one FP64 oracle step of each of the first %d requests of the mix with grid "
-                                          "sides capped at 48 (%.1f s), one thread" % (used, el)}
+                                "sample": "the reference arm's per-core sample on one host core: the first %d "
+                                          "requests of the mix, grid sides capped at %d, %d warm-up + %d timed steps "
+                                          "each (%.1f s); FP64" % (CPU_SET, CPU_SIDE_CAP, args.warmup, args.steps,
+                                                                   wall)}
     print(json.dumps(line), flush=True)
 
 

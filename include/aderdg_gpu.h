@@ -268,6 +268,9 @@ int aderdg_batch_sync(aderdg_batch* b, int* n_running);
  * after it). */
 int aderdg_batch_query(aderdg_batch* b, int slot, double* time, double* dt, long* steps, int* done);
 int aderdg_batch_download(aderdg_batch* b, int slot, double* uh);
+/* The simulation's limiter status(IMAX,JMAX) (as aderdg_download's status):
+ * 1 for the cells its last step limited; zeros without the limiter. */
+int aderdg_batch_download_status(aderdg_batch* b, int slot, int* status);
 int aderdg_batch_info(aderdg_batch* b, long* used_units, long* capacity_units, long* device_bytes, int* n_instances);
 /* One fused step of the batch, eager, with CUDA events between its launches:
  * device ms of each in phase_ms[7] (as aderdg_profile_step). */
