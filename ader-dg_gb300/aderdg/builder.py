@@ -2,7 +2,8 @@
 
 Each (system, N) pair is compiled from two translation units: predictor_tu.cu
 (fused multiply-adds) and exact_tu.cu (--fmad=false, reference operation
-order).  All units compile in parallel; a content hash of the sources and
+order), plus the tuner's candidates (predictor_var_tu.cu per variant,
+cells_var_tu.cu).  All units compile in parallel; a content hash of the sources and
 flags skips the build when nothing changed.
 """
 import concurrent.futures
@@ -23,6 +24,7 @@ DRIVER_PATH = os.path.join(BUILD_DIR, "aderdg_driver")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SYSTEMS = (0, 1, 2)
 DEGREES = (1, 2, 3, 4, 5)
+PRED_VARIANTS = 6  # predictor.cuh kPredVariants
 
 
 def _nvcc():
@@ -50,6 +52,13 @@ def _jobs():
                          "pred_%d_%d.o" % (s, n)))
             jobs.append(([nv] + _common_flags() + ["--fmad=false"] + d + ["-c", os.path.join(CSRC, "exact_tu.cu")],
                          "exact_%d_%d.o" % (s, n)))
+            # the tuner's candidates (aderdg/tuner.py): FP32 predictor shapes and K3 CTA sizes
+            jobs.append(([nv] + _common_flags() + ["--fmad=false"] + d + ["-c", os.path.join(CSRC, "cells_var_tu.cu")],
+                         "cellsvar_%d_%d.o" % (s, n)))
+            for var in range(1, PRED_VARIANTS):
+                jobs.append(([nv] + _common_flags() + d + ["-DADERDG_VAR=%d" % var, "-c",
+                                                          os.path.join(CSRC, "predictor_var_tu.cu")],
+                             "predvar_%d_%d_%d.o" % (s, n, var)))
     for src in ("registry.cu", "api.cu", "probe.cu", "batch.cu"):
         jobs.append(([nv] + _common_flags() + ["-c", os.path.join(CSRC, src)], src.replace(".cu", ".o")))
     jobs.append(([nv] + _common_flags() + ["--fmad=false", "-c", os.path.join(CSRC, "noalloc.cu")], "noalloc.o"))

@@ -7,6 +7,7 @@ There is no CPU fallback: every call goes to the CUDA library, and a missing
 library or a failing CUDA call raises.
 """
 import ctypes
+import json
 import dataclasses
 import os
 
@@ -53,7 +54,12 @@ class _Config(ctypes.Structure):
 class _Info(ctypes.Structure):
     _fields_ = [("cells", ctypes.c_long), ("dofs", ctypes.c_long), ("device_bytes", ctypes.c_long),
                 ("steps", ctypes.c_long), ("time", ctypes.c_double), ("dt", ctypes.c_double),
-                ("n_recompute", ctypes.c_int), ("n_limited", ctypes.c_int), ("n_settled", ctypes.c_int)]
+                ("n_recompute", ctypes.c_int), ("n_limited", ctypes.c_int), ("n_settled", ctypes.c_int),
+                ("n_listed", ctypes.c_int)]
+
+
+class _Tuning(ctypes.Structure):
+    _fields_ = [("predictor", ctypes.c_int), ("cells", ctypes.c_int), ("subcell_per_sm", ctypes.c_int)]
 
 
 @dataclasses.dataclass
@@ -160,6 +166,7 @@ def load(build_if_missing=False):
         "aderdg_batch_release": (i, [vp, i]), "aderdg_batch_launch": (i, [vp, i]), "aderdg_batch_sync": (i, [vp, ip]),
         "aderdg_batch_query": (i, [vp, i, dp, dp, ctypes.POINTER(ctypes.c_long), ip]),
         "aderdg_batch_download": (i, [vp, i, dp]), "aderdg_batch_download_status": (i, [vp, i, ip]),
+        "aderdg_batch_counters": (i, [vp, ip, ip, ip]),
         "aderdg_batch_info": (i, [vp, ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long),
                                   ctypes.POINTER(ctypes.c_long), ip]),
         "aderdg_batch_last_error": (ctypes.c_char_p, [vp]), "aderdg_batch_profile": (i, [vp, dp]),
@@ -168,13 +175,59 @@ def load(build_if_missing=False):
         "aderdg_batch_admit_ic": (i, [vp, cfgp, i, dp, d, ctypes.c_long, ip]),
         "aderdg_cell_averages": (i, [vp, i, dp]), "aderdg_batch_cell_averages": (i, [vp, i, i, dp]),
         "aderdg_error_norms": (i, [vp, i, dp, i, dp]),
+        "aderdg_set_tuning": (i, [i, i, i, ctypes.POINTER(_Tuning)]),
+        "aderdg_get_tuning": (i, [i, i, i, ctypes.POINTER(_Tuning)]),
+        "aderdg_tuning_variants": (i, [ip, ip]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
         f.restype = res
         f.argtypes = args
     _lib = L
+    tuning_file = os.environ.get("ADERDG_TUNING", TUNING_FILE)
+    if tuning_file and os.path.exists(tuning_file):
+        apply_tuning(load_tuning(tuning_file))
     return L
+
+
+# The tuner's table measured on the GB300 (aderdg/tuner.py), applied when the
+# library is loaded; ADERDG_TUNING names another file ("" for none).
+TUNING_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning_gb300.json")
+PRECISION_NAMES = {0: "fp64", 1: "fp32_mixed", 2: "fp32_wide"}
+
+
+def set_tuning(system, N, precision, predictor=0, cells=0, subcell_per_sm=0):
+    t = _Tuning(predictor, cells, subcell_per_sm)
+    r = load().aderdg_set_tuning(system, N, precision, ctypes.byref(t))
+    if r:
+        raise AderdgError(r, "bad tuning entry")
+
+
+def get_tuning(system, N, precision):
+    t = _Tuning()
+    r = load().aderdg_get_tuning(system, N, precision, ctypes.byref(t))
+    if r:
+        raise AderdgError(r, "bad tuning key")
+    return dict(predictor=t.predictor, cells=t.cells, subcell_per_sm=t.subcell_per_sm)
+
+
+def tuning_variants():
+    a, b = ctypes.c_int(0), ctypes.c_int(0)
+    load().aderdg_tuning_variants(ctypes.byref(a), ctypes.byref(b))
+    return a.value, b.value
+
+
+def load_tuning(path):
+    with open(path) as fh:
+        return json.load(fh)
+
+
+def apply_tuning(table):
+    """Sets every entry of a tuner table {"entries": {"<system>_<N>_<precision>": {...}}}."""
+    for key, e in table.get("entries", {}).items():
+        system, N, prec = (int(x) for x in key.split("_"))
+        t = _Tuning(int(e.get("predictor", 0)), int(e.get("cells", 0)), int(e.get("subcell_per_sm", 0)))
+        _lib.aderdg_set_tuning(system, N, prec, ctypes.byref(t))
 
 
 EXPORTED = ("aderdg_create", "aderdg_destroy", "aderdg_upload", "aderdg_init_limiter", "aderdg_upload_limiter",
@@ -186,10 +239,10 @@ EXPORTED = ("aderdg_create", "aderdg_destroy", "aderdg_upload", "aderdg_init_lim
             "aderdg_operator", "aderdg_step_host", "aderdg_time_steps", "aderdg_profile_step",
             "aderdg_batch_unit_bytes", "aderdg_batch_create", "aderdg_batch_destroy", "aderdg_batch_admit",
             "aderdg_batch_release", "aderdg_batch_launch", "aderdg_batch_sync", "aderdg_batch_query",
-            "aderdg_batch_download", "aderdg_batch_download_status", "aderdg_batch_info", "aderdg_batch_last_error", "aderdg_batch_profile",
+            "aderdg_batch_download", "aderdg_batch_download_status", "aderdg_batch_counters", "aderdg_batch_info", "aderdg_batch_last_error", "aderdg_batch_profile",
             "aderdg_batch_run_timed", "aderdg_initial_condition", "aderdg_batch_admit_ic",
             "aderdg_cell_averages", "aderdg_batch_cell_averages", "aderdg_error_norms", "aderdg_host_alloc",
-            "aderdg_host_free")
+            "aderdg_host_free", "aderdg_set_tuning", "aderdg_get_tuning", "aderdg_tuning_variants")
 
 
 def _dp(a):
@@ -543,6 +596,12 @@ class Batch:
             uh = out[: cfg.dofs]
         self._ck(self.L.aderdg_batch_download(self.h, slot, _dp(uh)))
         return uh
+
+    def counters(self):
+        """The last step's troubled, re-solved and FP64-settled cells, summed over the simulations."""
+        a, b, c = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        self._ck(self.L.aderdg_batch_counters(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return dict(n_recompute=a.value, n_listed=b.value, n_settled=c.value)
 
     def download_status(self, slot):
         """The simulation's limiter status per cell (1: limited by its last step)."""

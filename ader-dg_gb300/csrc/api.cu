@@ -128,7 +128,7 @@ int cur_par(aderdg_ctx* c) { return (int)(c->h_st->steps & 1); }
 
 int cells(aderdg_ctx* c, int mode) {
   c->args.mode = mode;
-  CK(c, c->kt->cells(c->args, c->ops64.data(), c->fp32 ? 1 : 0, c->stream));
+  CK(c, aderdg::launch_cells(c->kt, c->args, c->ops64.data(), c->prec, c->stream));
   // FP32-mixed: the DMP decisions the FP32 bounds left open
   if (c->args.settle && (mode == aderdg::kCellFused || mode == aderdg::kCellUpdate || mode == aderdg::kCellInitDmp))
     CK(c, c->kt->settle(c->args, c->ops64.data(), c->num_sms, c->stream));
@@ -158,13 +158,13 @@ int set_clock(aderdg_ctx* c, double time, double tend) {
 // one fused loop body of main.f90
 int launch_step(aderdg_ctx* c) {
   CK(c, control(c, aderdg::kCtlBegin));
-  CK(c, c->kt->predictor(c->args, pred_ops(c), c->fp32 ? 1 : 0, false, c->stream));
+  CK(c, aderdg::launch_predictor(c->kt, c->args, pred_ops(c), c->prec, c->stream));
   CK(c, aderdg::launch_faces(c->kt, c->args, c->fc, c->prec, c->stream));
   int r = cells(c, aderdg::kCellFused);
   if (r) return r;
   if (c->limiter) {
     CK(c, c->kt->mark(c->args, c->stream));
-    CK(c, aderdg::launch_subcell(c->kt, c->args, c->ops64.data(), c->fc, c->subcell_grid, c->prec, c->stream));
+    CK(c, aderdg::launch_subcell(c->kt, c->args, c->ops64.data(), c->fc, c->subcell_grid, c->num_sms, c->prec, c->stream));
   }
   CK(c, control(c, aderdg::kCtlEnd));
   return ADERDG_OK;
@@ -392,6 +392,8 @@ int aderdg_create(const aderdg_config* cfg, aderdg_ctx** out) {
     z.ncells = 0;
     z.nfx = z.nfy = 0;
     if (kt->predictor(z, pred_ops(c), c->fp32 ? 1 : 0, false, c->stream) != cudaSuccess ||
+        aderdg::launch_predictor(kt, z, pred_ops(c), c->prec, c->stream) != cudaSuccess ||
+        aderdg::launch_cells(kt, z, c->ops64.data(), c->prec, c->stream) != cudaSuccess ||
         kt->cells(z, c->ops64.data(), 0, c->stream) != cudaSuccess || kt->cells(z, c->ops64.data(), 1, c->stream) != cudaSuccess)
       return bail(fail(nullptr, ADERDG_ECUDA, "kernel attribute setup failed"));
     if (!c->fp32) kt->predictor(z, pred_ops(c), 0, true, c->stream);
@@ -652,7 +654,7 @@ int aderdg_limiter(aderdg_ctx* c) {
   if (!c->pending) return fail(c, ADERDG_ESTATE, "run aderdg_element_update first");
   CK(c, cudaMemsetAsync(c->args.list_count, 0, sizeof(int), c->stream));
   CK(c, c->kt->mark(c->args, c->stream));
-  CK(c, aderdg::launch_subcell(c->kt, c->args, c->ops64.data(), c->fc, c->subcell_grid, c->prec, c->stream));
+  CK(c, aderdg::launch_subcell(c->kt, c->args, c->ops64.data(), c->fc, c->subcell_grid, c->num_sms, c->prec, c->stream));
   CK(c, control(c, aderdg::kCtlEnd));
   c->pending = false;
   return pull_state(c);
@@ -776,7 +778,7 @@ int aderdg_profile_step(aderdg_ctx* c, double* time, double tend, double* phase_
   CK(c, cudaEventRecord(ev[0], c->stream));
   CK(c, control(c, aderdg::kCtlBegin));
   CK(c, cudaEventRecord(ev[1], c->stream));
-  CK(c, c->kt->predictor(c->args, pred_ops(c), c->fp32 ? 1 : 0, false, c->stream));
+  CK(c, aderdg::launch_predictor(c->kt, c->args, pred_ops(c), c->prec, c->stream));
   CK(c, cudaEventRecord(ev[2], c->stream));
   CK(c, aderdg::launch_faces(c->kt, c->args, c->fc, c->prec, c->stream));
   CK(c, cudaEventRecord(ev[3], c->stream));
@@ -786,7 +788,7 @@ int aderdg_profile_step(aderdg_ctx* c, double* time, double tend, double* phase_
   if (c->limiter) CK(c, c->kt->mark(c->args, c->stream));
   CK(c, cudaEventRecord(ev[5], c->stream));
   if (c->limiter)
-    CK(c, aderdg::launch_subcell(c->kt, c->args, c->ops64.data(), c->fc, c->subcell_grid, c->prec, c->stream));
+    CK(c, aderdg::launch_subcell(c->kt, c->args, c->ops64.data(), c->fc, c->subcell_grid, c->num_sms, c->prec, c->stream));
   CK(c, cudaEventRecord(ev[6], c->stream));
   CK(c, control(c, aderdg::kCtlEnd));
   CK(c, cudaEventRecord(ev[7], c->stream));
@@ -968,6 +970,7 @@ int aderdg_get_info(aderdg_ctx* c, aderdg_info* info) {
   info->dt = c->h_st->dt;
   info->n_recompute = c->h_st->n_recompute;
   info->n_settled = c->h_st->n_settled;
+  info->n_listed = c->h_st->n_list;
   info->n_limited = 0;
   if (c->limiter) {
     std::vector<int> st((size_t)c->ncells);

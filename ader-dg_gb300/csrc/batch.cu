@@ -65,6 +65,10 @@ struct aderdg_batch {
   size_t bytes = 0;
   cudaGraphExec_t gexec = nullptr;
   long long graph_hw = -1;
+  // set when an admission or release failed after editing the instance table:
+  // the host and device tables may then disagree, so the batch refuses
+  // further work (ADERDG_ESTATE) instead of stepping a table it cannot trust
+  bool broken = false;
   std::string err;
 };
 
@@ -76,6 +80,17 @@ int bfail(aderdg_batch* b, int code, const std::string& msg) {
   if (b) b->err = msg;
   aderdg::set_last_error(msg);
   return code;
+}
+// marks the batch unusable after a failure that left its table edited
+int bbreak(aderdg_batch* b, int code) {
+  b->broken = true;
+  b->err = "batch unusable after a failed admission or release: " + b->err;
+  aderdg::set_last_error(b->err);
+  return code;
+}
+int bcheck(aderdg_batch* b) {
+  if (b && b->broken) return bfail(b, ADERDG_ESTATE, b->err);
+  return ADERDG_OK;
 }
 int bcuda(aderdg_batch* b, const char* what, cudaError_t e) {
   return bfail(b, ADERDG_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
@@ -204,15 +219,14 @@ int blaunch_step(aderdg_batch* b) {
   a.nfx = b->hw;
   a.nfy = b->hw;
   a.mode = aderdg::kCellFused;
-  const int fp32 = b->precision ? 1 : 0;
   BK(b, bcontrol(b, aderdg::kCtlBegin, -1));
-  BK(b, b->kt->predictor(a, bpred_ops(b), fp32, false, b->stream));
+  BK(b, aderdg::launch_predictor(b->kt, a, bpred_ops(b), b->precision, b->stream));
   BK(b, aderdg::launch_faces(b->kt, a, b->fc, b->precision, b->stream));
-  BK(b, b->kt->cells(a, b->ops64.data(), fp32, b->stream));
+  BK(b, aderdg::launch_cells(b->kt, a, b->ops64.data(), b->precision, b->stream));
   if (a.settle) BK(b, b->kt->settle(a, b->ops64.data(), b->num_sms, b->stream));
   if (b->limiter) {
     BK(b, b->kt->mark(a, b->stream));
-    BK(b, aderdg::launch_subcell(b->kt, a, b->ops64.data(), b->fc, b->subcell_grid, b->precision, b->stream));
+    BK(b, aderdg::launch_subcell(b->kt, a, b->ops64.data(), b->fc, b->subcell_grid, b->num_sms, b->precision, b->stream));
   }
   BK(b, bcontrol(b, aderdg::kCtlEnd, -1));
   return ADERDG_OK;
@@ -249,7 +263,7 @@ int bcells_one(aderdg_batch* b, int pos, int mode, const double* lh_ic) {
   a.ncells = in.cell_base + (long long)in.imax * in.jmax;
   a.only_inst = pos;
   a.lh_ic = lh_ic;
-  BK(b, b->kt->cells(a, b->ops64.data(), b->precision ? 1 : 0, b->stream));
+  BK(b, aderdg::launch_cells(b->kt, a, b->ops64.data(), b->precision, b->stream));
   if (a.settle && mode == aderdg::kCellInitDmp) BK(b, b->kt->settle(a, b->ops64.data(), b->num_sms, b->stream));
   return ADERDG_OK;
 }
@@ -380,6 +394,8 @@ int aderdg_batch_create(int system, int N, int precision, int limiter, long capa
     z.ncells = z.nfx = z.nfy = 0;
     kt->predictor(z, bpred_ops(b), precision ? 1 : 0, false, b->stream);
     kt->cells(z, b->ops64.data(), precision ? 1 : 0, b->stream);
+    aderdg::launch_predictor(kt, z, bpred_ops(b), precision, b->stream);
+    aderdg::launch_cells(kt, z, b->ops64.data(), precision, b->stream);
   }
   r = push_table(b);
   if (r) return bail(r);
@@ -399,9 +415,13 @@ namespace {
 
 // Admission of one simulation: its initial state comes from host arrays
 // (uh, lh_ic) or, with ic >= 0, is evaluated on the device.
+int badmit_fill(aderdg_batch* b, const aderdg_config* cfg, const double* uh, const double* lh_ic, int ic,
+                const double* params, long long base, int pos);
+
 int badmit(aderdg_batch* b, const aderdg_config* cfg, const double* uh, const double* lh_ic, int ic,
            const double* params, double tend, long max_steps, int* slot) {
   if (!b || !cfg || !slot || (ic < 0 && !uh)) return bfail(b, ADERDG_EINVAL, "null argument");
+  if (int r = bcheck(b)) return r;
   if (ic >= 0) {
     double p[32] = {0};
     if (params) std::memcpy(p, params, sizeof(p));
@@ -453,7 +473,16 @@ int badmit(aderdg_batch* b, const aderdg_config* cfg, const double* uh, const do
   st.max_steps = max_steps;
   recompute_hw(b);
   r = btable_edit(b, n_before, pos, true, in, st);
-  if (r) return r;
+  if (!r) r = badmit_fill(b, cfg, uh, lh_ic, ic, params, base, pos);
+  if (r) return bbreak(b, r);
+  *slot = s;
+  return ADERDG_OK;
+}
+
+// the new simulation's state and its priming, after its table entry
+int badmit_fill(aderdg_batch* b, const aderdg_config* cfg, const double* uh, const double* lh_ic, int ic,
+                const double* params, long long base, int pos) {
+  int r = ADERDG_OK;
   // state of the new simulation (parity 0); host-given subcell candidates of
   // the initial limiter are staged in the next-parity Lh slab of this
   // simulation, device-evaluated ones are formed after the initial DMP for the
@@ -500,7 +529,6 @@ int badmit(aderdg_batch* b, const aderdg_config* cfg, const double* uh, const do
   // the next sync or query), except that host arrays are copied before the
   // call returns, so that the caller may reuse them
   if (ic < 0) BK(b, cudaStreamSynchronize(b->stream));
-  *slot = s;
   return ADERDG_OK;
 }
 
@@ -519,6 +547,7 @@ int aderdg_batch_admit_ic(aderdg_batch* b, const aderdg_config* cfg, int ic, con
 
 int aderdg_batch_release(aderdg_batch* b, int slot) {
   if (!b || slot < 0 || slot >= b->max_inst || b->pos_of[slot] < 0) return bfail(b, ADERDG_EINVAL, "bad slot");
+  if (int r = bcheck(b)) return r;
   const int pos = b->pos_of[slot];
   const int n_before = b->n_used;
   const InstDesc in = b->h_inst[pos];
@@ -536,7 +565,7 @@ int aderdg_batch_release(aderdg_batch* b, int slot) {
   InstState zero;
   std::memset(&zero, 0, sizeof(zero));
   int r = btable_edit(b, n_before, pos, false, d, zero);
-  if (r) return r;
+  if (r) return bbreak(b, r);
   b->slot_at[b->n_used] = -1;
   b->pos_of[slot] = -1;
   // return the range to the free list, merging neighbours
@@ -555,6 +584,7 @@ int aderdg_batch_release(aderdg_batch* b, int slot) {
 
 int aderdg_batch_launch(aderdg_batch* b, int steps) {
   if (!b) return bfail(b, ADERDG_EINVAL, "null batch");
+  if (int r = bcheck(b)) return r;
   if (steps <= 0 || b->n_used == 0) return ADERDG_OK;
   int r = bensure_graph(b);
   if (r) return r;
@@ -564,8 +594,10 @@ int aderdg_batch_launch(aderdg_batch* b, int steps) {
 
 int aderdg_batch_run_timed(aderdg_batch* const* batches, int n, int steps, double* ms) {
   if (!batches || n <= 0 || !ms) return bfail(nullptr, ADERDG_EINVAL, "null argument");
-  for (int k = 0; k < n; ++k)
+  for (int k = 0; k < n; ++k) {
     if (!batches[k]) return bfail(nullptr, ADERDG_EINVAL, "null batch");
+    if (int r = bcheck(batches[k])) return r;
+  }
   aderdg_batch* b0 = batches[0];
   for (int k = 0; k < n; ++k) {
     if (batches[k]->n_used == 0) continue;
@@ -628,6 +660,22 @@ int aderdg_batch_query(aderdg_batch* b, int slot, double* time, double* dt, long
   if (steps) *steps = (long)s.steps;
   if (done) *done = (!(s.time < s.tend) || s.nonfinite || (s.max_steps > 0 && s.steps >= s.max_steps)) ? 1 : 0;
   if (s.nonfinite) return bfail(b, ADERDG_ENONFINITE, "the time step became non-finite");
+  return ADERDG_OK;
+}
+
+int aderdg_batch_counters(aderdg_batch* b, int* n_recompute, int* n_listed, int* n_settled) {
+  if (!b) return bfail(b, ADERDG_EINVAL, "null batch");
+  int r = pull_states(b);
+  if (r) return r;
+  long long a = 0, l = 0, s = 0;
+  for (int p = 0; p < b->n_used; ++p) {
+    a += b->h_st[p].n_recompute;
+    l += b->h_st[p].n_list;
+    s += b->h_st[p].n_settled;
+  }
+  if (n_recompute) *n_recompute = (int)a;
+  if (n_listed) *n_listed = (int)l;
+  if (n_settled) *n_settled = (int)s;
   return ADERDG_OK;
 }
 
@@ -705,23 +753,22 @@ int aderdg_batch_profile(aderdg_batch* b, double* phase_ms) {
   BatchArgs a = b->args;
   a.ncells = a.nfx = a.nfy = b->hw;
   a.mode = aderdg::kCellFused;
-  const int fp32 = b->precision ? 1 : 0;
   cudaEvent_t ev[8];
   for (auto& e : ev) BK(b, cudaEventCreate(&e));
   BK(b, cudaEventRecord(ev[0], b->stream));
   BK(b, bcontrol(b, aderdg::kCtlBegin, -1));
   BK(b, cudaEventRecord(ev[1], b->stream));
-  BK(b, b->kt->predictor(a, bpred_ops(b), fp32, false, b->stream));
+  BK(b, aderdg::launch_predictor(b->kt, a, bpred_ops(b), b->precision, b->stream));
   BK(b, cudaEventRecord(ev[2], b->stream));
   BK(b, aderdg::launch_faces(b->kt, a, b->fc, b->precision, b->stream));
   BK(b, cudaEventRecord(ev[3], b->stream));
-  BK(b, b->kt->cells(a, b->ops64.data(), fp32, b->stream));
+  BK(b, aderdg::launch_cells(b->kt, a, b->ops64.data(), b->precision, b->stream));
   if (a.settle) BK(b, b->kt->settle(a, b->ops64.data(), b->num_sms, b->stream));
   BK(b, cudaEventRecord(ev[4], b->stream));
   if (b->limiter) BK(b, b->kt->mark(a, b->stream));
   BK(b, cudaEventRecord(ev[5], b->stream));
   if (b->limiter)
-    BK(b, aderdg::launch_subcell(b->kt, a, b->ops64.data(), b->fc, b->subcell_grid, b->precision, b->stream));
+    BK(b, aderdg::launch_subcell(b->kt, a, b->ops64.data(), b->fc, b->subcell_grid, b->num_sms, b->precision, b->stream));
   BK(b, cudaEventRecord(ev[6], b->stream));
   BK(b, bcontrol(b, aderdg::kCtlEnd, -1));
   BK(b, cudaEventRecord(ev[7], b->stream));

@@ -253,7 +253,10 @@ __device__ __forceinline__ unsigned long long seg_max(unsigned long long x) {
   return x;
 }
 
-template <class Sys, int N>
+// VAR: the CTA size the tuner (aderdg/tuner.py) picks for the FP32 modes: 0
+// the default below, 1 twice, 2 half of it
+constexpr int kCellVariants = 3;
+template <class Sys, int N, int VAR = 0>
 struct CellCfg {
   static constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1, V = Sys::V;
   // small CTAs (the kernel waits on latency and barriers: smaller CTAs, more
@@ -261,7 +264,8 @@ struct CellCfg {
   // 128 at N = 4 and 256 at N = 5, where the 25- and 36-thread cells fill
   // smaller CTAs badly (measured: BN cylinder 0.559 -> 0.508 -> 0.487 ms,
   // Riemann problem 0.344 -> 0.330 -> 0.324 ms for 256 -> 128 -> 64 threads)
-  static constexpr int CTA = N == 5 ? 256 : N == 4 ? 128 : 64;
+  static constexpr int CTA0 = N == 5 ? 256 : N == 4 ? 128 : 64;
+  static constexpr int CTA = VAR == 1 ? 2 * CTA0 : VAR == 2 ? (CTA0 / 2 < 32 ? 32 : CTA0 / 2) : CTA0;
   static constexpr int CPB = (CTA / P2) < 1 ? 1 : (CTA / P2);
   static constexpr int THREADS = ((CPB * P2 + 31) / 32) * 32;
   // per cell: U [V][P2], LY [V][S][P], LB [V][P][P], red [2][V][P2] (FP64);
@@ -276,14 +280,16 @@ struct CellCfg {
   // Euler's FP32-mixed cell kernel is latency-bound and gains from a fourth;
   // the other variants keep the allocation they reach unconstrained
   static constexpr int min_blocks(bool fast) {
-    return (Sys::ID == kSysEuler ? (fast ? 4 : 3) : (Sys::ID == kSysBN ? 2 : 4)) * (256 / CTA);
+    return (Sys::ID == kSysEuler ? (fast ? 4 : 3) : (Sys::ID == kSysBN ? 2 : 4)) * 256 / CTA < 1
+               ? 1
+               : (Sys::ID == kSysEuler ? (fast ? 4 : 3) : (Sys::ID == kSysBN ? 2 : 4)) * 256 / CTA;
   }
 };
 
-template <class Sys, int N, bool kFast>
-__global__ void __launch_bounds__(CellCfg<Sys, N>::THREADS, CellCfg<Sys, N>::min_blocks(kFast))
+template <class Sys, int N, bool kFast, int VAR = 0>
+__global__ void __launch_bounds__(CellCfg<Sys, N, VAR>::THREADS, CellCfg<Sys, N, VAR>::min_blocks(kFast))
     k_cells(BatchArgs a, DevOps<N, double> op) {
-  using C = CellCfg<Sys, N>;
+  using C = CellCfg<Sys, N, VAR>;
   constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1, V = Sys::V, CPB = C::CPB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* sm = reinterpret_cast<double*>(smem_raw);

@@ -61,7 +61,7 @@ struct InstState {
   int active;                        // 1 while time < tend
   int n_recompute;                   // troubled cells of the last step (nRecompute)
   int n_settled;                     // FP32-mixed: DMP decisions of the last step settled from FP64 values
-  int n_list;                        // cells with recompute > 0
+  int n_list;                        // cells the last step's limiter re-solved (recompute > 0)
   int nonfinite;                     // set when dt came out non-finite
   long long steps;
   long long max_steps;               // > 0: stop after this many steps

@@ -42,6 +42,7 @@ static __global__ void k_control(InstDesc* inst, InstState* st, int ninst, int* 
       s.denom_next = 0ull;
       s.n_recompute = 0;
       s.n_settled = 0;
+      s.n_list = 0;
       const double maxd = __longlong_as_double((long long)s.denom_bits);
       // a NaN denominator anywhere folds to the largest bit pattern
       if (isnan(maxd)) s.nonfinite = 1;

@@ -48,6 +48,7 @@ __global__ void __launch_bounds__(256) k_mark(BatchArgs a) {
     if (rec > 0) {
       const int pos = atomicAdd(a.list_count, 1);
       a.list[pos] = (int)c;
+      atomicAdd(&a.st[k].n_list, 1);
     } else {
       val = (unsigned long long)__double_as_longlong(a.denom[c]);
     }

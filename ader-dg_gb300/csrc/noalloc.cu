@@ -14,7 +14,9 @@
 //
 // Set-up: the first call on each device (with that device current) asks the
 // runtime for the array's device address with cudaGetSymbolAddress and caches
-// it; make that first call before any stream capture.  Every call shares the
+// it, keyed on the CUDA context current at that call; make that first call
+// before any stream capture.  A call in another context of that device (after
+// cudaDeviceReset, for instance) looks the address up again.  Every call shares the
 // array and leaves its contents behind, so each call clears the ticket before
 // its kernel runs, and calls whose kernels overlap on the GPU race on the
 // array: serialise them (one stream, or events).
@@ -22,6 +24,8 @@
 // The kernel computes the same quantity as calc_time_step.f90 (Euler :9-52,
 // BN :9-52, AD :9-57), in the same FP64 operation order as the time-step path
 // of the context API (this unit is compiled with --fmad=false as well).
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -34,6 +38,7 @@
 
 namespace aderdg {
 void set_last_error(const std::string& msg);
+int validate_config(const aderdg_config* c, std::string* why);
 InstDesc make_inst_desc(const aderdg_config* cfg);
 }
 
@@ -49,7 +54,13 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned long long g_scratch[kMaxBlocks + 1];
 
 std::mutex g_mu;
-unsigned long long* g_addr[kMaxDevices] = {nullptr};
+// per device: the context the address was looked up in, and the address
+struct Cached {
+  CUcontext ctx;
+  unsigned long long* addr;
+};
+Cached g_addr[kMaxDevices] = {};
+PFN_cuCtxGetCurrent_v4000 g_ctx_current = nullptr;  // the driver's cuCtxGetCurrent, from the runtime
 
 template <int SYS>
 __device__ double node_denom(const aderdg::InstDesc& in, int N, const double* Q) {
@@ -115,6 +126,25 @@ __global__ void __launch_bounds__(kThreads) k_cfl_noalloc(const double* __restri
   }
 }
 
+// the current context (null when none is current yet); called under g_mu
+int current_context(CUcontext* ctx) {
+  if (!g_ctx_current) {
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    const cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", reinterpret_cast<void**>(&g_ctx_current),
+                                                           4000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !g_ctx_current) {
+      g_ctx_current = nullptr;
+      aderdg::set_last_error("cudaGetDriverEntryPointByVersion(cuCtxGetCurrent) failed");
+      return ADERDG_ECUDA;
+    }
+  }
+  if (g_ctx_current(ctx) != CUDA_SUCCESS) {
+    aderdg::set_last_error("cuCtxGetCurrent failed");
+    return ADERDG_ECUDA;
+  }
+  return ADERDG_OK;
+}
+
 int scratch_address(unsigned long long** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -127,16 +157,23 @@ int scratch_address(unsigned long long** out) {
     return ADERDG_EUNSUPPORTED;
   }
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[dev]) {
+  CUcontext ctx = nullptr;
+  int r = current_context(&ctx);
+  if (r) return r;
+  if (!ctx || g_addr[dev].ctx != ctx || !g_addr[dev].addr) {
+    // set-up in this context (the lookup makes the device's primary context
+    // current when none was)
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_scratch);
     if (e != cudaSuccess || !p) {
       aderdg::set_last_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
       return ADERDG_ECUDA;
     }
-    g_addr[dev] = static_cast<unsigned long long*>(p);
+    r = current_context(&ctx);
+    if (r) return r;
+    g_addr[dev] = Cached{ctx, static_cast<unsigned long long*>(p)};
   }
-  *out = g_addr[dev];
+  *out = g_addr[dev].addr;
   return ADERDG_OK;
 }
 
@@ -148,10 +185,11 @@ extern "C" int aderdg_calc_time_step_noalloc(const aderdg_config* cfg, const dou
     aderdg::set_last_error("null argument");
     return ADERDG_EINVAL;
   }
-  if (cfg->system < 0 || cfg->system > 2 || cfg->N < 1 || cfg->N > 9 || cfg->imax < 1 || cfg->jmax < 1 ||
-      !(cfg->xr[0] > cfg->xl[0]) || !(cfg->xr[1] > cfg->xl[1]) || !(cfg->cfl > 0.0)) {
-    aderdg::set_last_error("bad configuration");
-    return ADERDG_EINVAL;
+  std::string why;
+  const int v = aderdg::validate_config(cfg, &why);  // the checks of aderdg_create
+  if (v) {
+    aderdg::set_last_error("aderdg_calc_time_step_noalloc: " + why);
+    return v;
   }
   const long long ncells = (long long)cfg->imax * cfg->jmax;
   if (ncells > kMaxCells) {

@@ -30,7 +30,30 @@
 
 namespace aderdg {
 
-template <class Sys, int N, class R>
+// Shape of the FP32 predictor that the tuner (aderdg/tuner.py) picks per
+// (system, N, precision): kCta scales the cells per CTA (+1: twice the
+// threads, -1: half), kBlocks adds to the CTAs per SM the register
+// allocation aims at, kUnroll unrolls the middle Picard iterations, and
+// kNoRowCol contracts per node instead of by rows and columns.  PredTune<>
+// is the hand-measured default.
+template <int kCta = 0, int kBlocks = 0, bool kUnroll = false, bool kNoRowCol = false>
+struct PredTune {
+  static constexpr int CTA = kCta, BLOCKS = kBlocks;
+  static constexpr bool UNROLL = kUnroll, NO_ROWCOL = kNoRowCol;
+};
+// the tuner's candidates, variant 0 the default
+template <int K>
+using PredVariant = typename std::conditional<
+    K == 1, PredTune<1>,
+    typename std::conditional<
+        K == 2, PredTune<-1>,
+        typename std::conditional<K == 3, PredTune<0, 1>,
+                                  typename std::conditional<K == 4, PredTune<0, 0, true>,
+                                                            typename std::conditional<K == 5, PredTune<0, 0, false, true>,
+                                                                                      PredTune<>>::type>::type>::type>::type>::type;
+constexpr int kPredVariants = 6;
+
+template <class Sys, int N, class R, class Tune = PredTune<>>
 struct PredCfg {
   static constexpr int P = N + 1, P2 = P * P, V = Sys::V;
   // variables of one node padded to whole 16-byte vectors (AD: scalar)
@@ -62,7 +85,7 @@ struct PredCfg {
   // The x levels then the y levels, each level padded to XL / YL nodes; at
   // P >= 5 the y pass takes level j and column i (the lanes of a quarter-warp
   // then meet no bank group twice at these paddings).
-  static constexpr bool ROWCOL = PLANAR && P >= 4;
+  static constexpr bool ROWCOL = PLANAR && P >= 4 && !Tune::NO_ROWCOL;
   static constexpr int XL = ROWCOL ? P2 + ((P == 5) ? 0 : 1) : 2 * P2;  // nodes from x level to x level
   static constexpr int YL = ROWCOL ? P2 + ((P == 5) ? 4 : 2) : 2 * P2;
   static constexpr int Y0 = ROWCOL ? P * XL : P2;  // node offset of the y fluxes of level 0
@@ -84,7 +107,8 @@ struct PredCfg {
   // FP32 up to N = 4: CTAs of at most 128 threads, twice as many per SM (each
   // Picard iteration's barriers then wait on fewer warps); N = 5 keeps 256,
   // whose 36-thread cells fill 128 badly; FP64 is pipe-bound either way
-  static constexpr int MAX_THREADS = (sizeof(R) == 4 && N <= 4) ? 128 : 256;
+  static constexpr int MAX_THREADS0 = (sizeof(R) == 4 && N <= 4) ? 128 : 256;
+  static constexpr int MAX_THREADS = Tune::CTA > 0 ? 2 * MAX_THREADS0 : Tune::CTA < 0 ? MAX_THREADS0 / 2 : MAX_THREADS0;
   static constexpr int SMEM_BUDGET = 100 * 1024;
   static constexpr int CPB_T = MAX_THREADS / P2;
   static constexpr int CPB_S = SMEM_BUDGET / (CELL_ELEMS * (int)sizeof(R));
@@ -94,10 +118,13 @@ struct PredCfg {
   // and degree (more resident warps hide the shared-memory latency of the
   // contractions; Baer-Nunziato's time column does not fit in fewer
   // registers without spilling at N >= 3); FP64 is pipe-bound either way
+  static constexpr int BLOCK_UNITS =
+      (Sys::ID == kSysAD ? 4 : Sys::ID == kSysEuler ? (N <= 3 ? 4 : 3) : (N <= 2 ? 3 : 2)) + Tune::BLOCKS;
   static constexpr int MIN_BLOCKS =
-      (sizeof(R) == 4 && THREADS > 64)
-          ? (Sys::ID == kSysAD ? 4 : Sys::ID == kSysEuler ? (N <= 3 ? 4 : 3) : (N <= 2 ? 3 : 2)) * (256 / MAX_THREADS)
-          : 1;
+      (sizeof(R) == 4 && THREADS > 64) ? (BLOCK_UNITS * 256 / MAX_THREADS < 1 ? 1 : BLOCK_UNITS * 256 / MAX_THREADS)
+                                       : 1;
+  // the middle Picard iterations: a loop (default) or unrolled
+  static constexpr int UNROLL = (Tune::UNROLL && P > 3) ? P - 2 : 1;
   // threads past CPB*P2 (the tail of the last warp) take part in the barriers
   // and get a scratch slot of their own so they never touch a real cell's data
   static constexpr int SLOTS = CPB + (THREADS > CPB * P2 ? 1 : 0);
@@ -288,10 +315,10 @@ __device__ __forceinline__ void predictor_outputs(const BatchArgs& a, const DevO
   }
 }
 
-template <class Sys, int N, class R, bool kPhase>
-__global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R>::MIN_BLOCKS)
+template <class Sys, int N, class R, bool kPhase, class Tune = PredTune<>>
+__global__ void __launch_bounds__(PredCfg<Sys, N, R, Tune>::THREADS, PredCfg<Sys, N, R, Tune>::MIN_BLOCKS)
     k_predictor(BatchArgs a, DevOps<N, R> op) {
-  using C = PredCfg<Sys, N, R>;
+  using C = PredCfg<Sys, N, R, Tune>;
   constexpr int P = N + 1, P2 = P * P, V = Sys::V, CPB = C::CPB, VP = C::VP;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R* sm = reinterpret_cast<R*>(smem_raw);
@@ -456,7 +483,7 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
       }
       __syncthreads();
     };
-#pragma unroll 1
+#pragma unroll C::UNROLL
     for (int it = 2; it < P; ++it) picard(std::false_type{});
     picard(std::true_type{});
   } else {
@@ -623,7 +650,7 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R>::THREADS, PredCfg<Sys, N, R
       }
       __syncthreads();
     };
-#pragma unroll 1
+#pragma unroll C::UNROLL
     for (int it = 2; it < P; ++it) picard(std::false_type{});
     picard(std::true_type{});
   }

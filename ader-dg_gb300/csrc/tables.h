@@ -16,6 +16,10 @@
 
 namespace aderdg {
 
+// candidates of the tuner (predictor.cuh PredVariant, cells.cuh CellCfg VAR)
+constexpr int kPredVariantsMax = 6;
+constexpr int kCellVariantsMax = 3;
+
 struct KernelTable {
   int sys = -1, N = 0;
   // predictor translation unit
@@ -25,6 +29,12 @@ struct KernelTable {
   cudaError_t (*predictor)(const BatchArgs&, const void* ops, int fp32, bool phase, cudaStream_t) = nullptr;
   int pred_cells_per_cta[2] = {0, 0};
   int pred_threads[2] = {0, 0};
+  // FP32 predictor candidates 1.. (predictor_var_tu.cu); [0] unused (the default)
+  cudaError_t (*predictor_var[kPredVariantsMax])(const BatchArgs&, const void* ops, cudaStream_t) = {};
+  int pred_var_cpb[kPredVariantsMax] = {}, pred_var_threads[kPredVariantsMax] = {};
+  // FP32-mode cell-kernel candidates 1.. (cells_var_tu.cu); [0] unused (the default)
+  cudaError_t (*cells_var[kCellVariantsMax])(const BatchArgs&, const void* ops64, cudaStream_t) = {};
+  int cells_var_threads[kCellVariantsMax] = {};
   // FP32-mixed faces where they differ from the FP32 faces (Baer-Nunziato:
   // FP64 arithmetic on FP32 storage); null: use faces(..., fp32 = 1, ...)
   cudaError_t (*faces_mixed)(const BatchArgs&, const FaceConst&, cudaStream_t) = nullptr;
@@ -66,6 +76,36 @@ cudaError_t launch_error_norms(const aderdg_config& cfg, const double* uh, int i
 // Returns the table for (sys, N) or nullptr when that pair was not built.
 const KernelTable* kernel_table(int sys, int N);
 
+// The tuner's choice for (system, N, precision) (registry.cu; zeros: the defaults).
+aderdg_tuning tuning_of(int sys, int N, int precision);
+
+// The FP32 modes' predictor and cell kernel in the tuned variant; FP64 keeps
+// the reference-order kernels of its own.
+inline cudaError_t launch_predictor(const KernelTable* kt, const BatchArgs& a, const void* ops, int precision,
+                                    cudaStream_t s) {
+  const int fp32 = precision != ADERDG_FP64 ? 1 : 0;
+  if (fp32) {
+    const int v = tuning_of(kt->sys, kt->N, precision).predictor;
+    if (v > 0 && v < kPredVariantsMax && kt->predictor_var[v]) return kt->predictor_var[v](a, ops, s);
+  }
+  return kt->predictor(a, ops, fp32, false, s);
+}
+inline cudaError_t launch_cells(const KernelTable* kt, const BatchArgs& a, const void* ops64, int precision,
+                                cudaStream_t s) {
+  const int fast = precision != ADERDG_FP64 ? 1 : 0;
+  if (fast) {
+    const int v = tuning_of(kt->sys, kt->N, precision).cells;
+    if (v > 0 && v < kCellVariantsMax && kt->cells_var[v]) return kt->cells_var[v](a, ops64, s);
+  }
+  return kt->cells(a, ops64, fast, s);
+}
+// the subcell kernel's persistent grid: the tuned CTAs per SM, at most max_grid
+inline int subcell_launch_grid(const KernelTable* kt, int max_grid, int num_sms, int precision) {
+  const int per = tuning_of(kt->sys, kt->N, precision).subcell_per_sm;
+  if (per > 0 && per * num_sms < max_grid) return per * num_sms;
+  return max_grid;
+}
+
 // The face kernel of a precision mode (aderdg_precision).
 inline cudaError_t launch_faces(const KernelTable* kt, const BatchArgs& a, const FaceConst& fc, int precision,
                                 cudaStream_t s) {
@@ -76,8 +116,11 @@ inline cudaError_t launch_faces(const KernelTable* kt, const BatchArgs& a, const
 // with the reciprocal-sharing physics in the FP32-mixed mode, FP64 in the
 // reference's order otherwise.
 inline int subcell_fp32(int precision) { return precision == ADERDG_FP32_WIDE ? 1 : 0; }
+// max_grid: the most CTAs that fit (subcell_grid_of); the tuned CTAs per SM
+// apply within it
 inline cudaError_t launch_subcell(const KernelTable* kt, const BatchArgs& a, const void* ops64, const FaceConst& fc,
-                                  int grid, int precision, cudaStream_t s) {
+                                  int max_grid, int num_sms, int precision, cudaStream_t s) {
+  const int grid = subcell_launch_grid(kt, max_grid, num_sms, precision);
   if (precision == ADERDG_FP32_MIXED && kt->subcell_mixed) return kt->subcell_mixed(a, ops64, fc, grid, s);
   return kt->subcell(a, ops64, fc, grid, subcell_fp32(precision), s);
 }

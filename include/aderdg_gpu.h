@@ -226,6 +226,7 @@ typedef struct aderdg_info {
   int n_limited;        /* cells with status != 0 after the last step */
   int n_settled;        /* FP32-mixed: DMP decisions of the last step that the FP32
                            error bounds left open and FP64 values settled */
+  int n_listed;         /* cells the last step's limiter re-solved (recompute > 0) */
 } aderdg_info;
 int aderdg_get_info(aderdg_ctx* ctx, aderdg_info* info);
 
@@ -268,6 +269,10 @@ int aderdg_batch_sync(aderdg_batch* b, int* n_running);
  * after it). */
 int aderdg_batch_query(aderdg_batch* b, int slot, double* time, double* dt, long* steps, int* done);
 int aderdg_batch_download(aderdg_batch* b, int slot, double* uh);
+/* Sums over the batch's simulations of the last step's counters: troubled
+ * cells (nRecompute), cells the limiter re-solved (recompute > 0) and, in the
+ * FP32-mixed mode, DMP decisions settled from FP64 values. */
+int aderdg_batch_counters(aderdg_batch* b, int* n_recompute, int* n_listed, int* n_settled);
 /* The simulation's limiter status(IMAX,JMAX) (as aderdg_download's status):
  * 1 for the cells its last step limited; zeros without the limiter. */
 int aderdg_batch_download_status(aderdg_batch* b, int slot, int* status);
@@ -343,6 +348,30 @@ int aderdg_operator(int N, int which, double* out);
  * the GPU race, so serialise them. */
 int aderdg_calc_time_step_noalloc(const aderdg_config* cfg, const double* uh, double time, double tend, double* dt,
                                   void* stream);
+
+/* ---- tuning ----
+ * Kernel shapes of the FP32 modes, per (system, N, precision), as picked by
+ * the tuner (ader-dg_gb300/aderdg/tuner.py times every candidate on the GPU
+ * and stores its table in a JSON file that the Python package applies when it
+ * loads this library).  No counterpart in the reference, whose shapes are its
+ * compile-time parameters (Euler/ader_dg.f90:17-20).  All zero selects the
+ * hand-measured defaults.  The cell-kernel and subcell shapes change no
+ * result; the predictor shapes change results by FP32 rounding (each is
+ * compiled with fused multiply-adds, which the compiler may group
+ * differently).  Contexts and batches read
+ * the table when they launch; a CUDA graph captured earlier keeps the shapes
+ * it was captured with, so set the table before the first step. */
+typedef struct aderdg_tuning {
+  int predictor;      /* FP32 predictor: 0 default, 1 twice the cells per CTA, 2 half,
+                         3 one more CTA per SM for the register allocation,
+                         4 middle Picard iterations unrolled, 5 per-node contractions */
+  int cells;          /* FP32-mode cell kernel: 0 default CTA, 1 twice its size, 2 half */
+  int subcell_per_sm; /* subcell re-solve CTAs per SM; 0: as many as fit */
+} aderdg_tuning;
+int aderdg_set_tuning(int system, int N, int precision, const aderdg_tuning* t);
+int aderdg_get_tuning(int system, int N, int precision, aderdg_tuning* t);
+/* Numbers of predictor and cell-kernel candidates. */
+int aderdg_tuning_variants(int* n_predictor, int* n_cells);
 
 /* Measured device peaks for roofline reporting: FP64 and FP32 FMA throughput
  * (GFLOP/s) from dependent-FMA microkernels on the current device. */

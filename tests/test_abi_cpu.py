@@ -3,6 +3,7 @@ declared in include/aderdg_gpu.h, builds operators and initial fields that are
 bit-identical to the oracle's, and rejects bad configurations before touching
 the GPU.  No kernel runs here."""
 import ctypes
+import dataclasses
 import os
 import re
 
@@ -99,3 +100,36 @@ def test_workload_definitions():
     cfg, ic, p, tend = aderdg.workloads.make("euler_vortex")
     assert (cfg.N, cfg.imax, cfg.jmax, tend) == (4, 256, 256, 10.0)
     assert cfg.dofs == 4 * 25 * 65536
+
+
+def test_noalloc_entry_validates_like_create(gpu_lib):
+    """The allocation-free time step refuses what aderdg_create refuses (N
+    outside 1..5, a bad precision), before it touches the device."""
+    f = gpu_lib.aderdg_calc_time_step_noalloc
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.POINTER(aderdg.core._Config), ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
+                  ctypes.c_void_p, ctypes.c_void_p]
+    dummy = ctypes.c_double(0)
+    for over, code in ((dict(N=6), -7), (dict(N=0), -7), (dict(precision=7), -1)):
+        cfg = dataclasses.replace(aderdg.Config(system=aderdg.SYS_EULER, N=3, imax=8, jmax=8), **over)
+        c = cfg.to_c()
+        assert f(ctypes.byref(c), ctypes.addressof(dummy), 0.0, 1.0, ctypes.addressof(dummy), None) == code
+        c2 = cfg.to_c()
+        h = ctypes.c_void_p()
+        assert gpu_lib.aderdg_create(ctypes.byref(c2), ctypes.byref(h)) == code
+
+
+def test_tuning_table_round_trip(gpu_lib):
+    """The tuner's table: set, read back, and refused outside the candidates."""
+    n_pred, n_cells = aderdg.tuning_variants()
+    assert n_pred >= 2 and n_cells >= 2
+    old = aderdg.get_tuning(aderdg.SYS_BN, 4, aderdg.FP32_WIDE)
+    aderdg.set_tuning(aderdg.SYS_BN, 4, aderdg.FP32_WIDE, predictor=n_pred - 1, cells=1, subcell_per_sm=2)
+    assert aderdg.get_tuning(aderdg.SYS_BN, 4, aderdg.FP32_WIDE) == dict(predictor=n_pred - 1, cells=1,
+                                                                        subcell_per_sm=2)
+    for bad in (dict(predictor=n_pred), dict(cells=n_cells), dict(predictor=-1), dict(subcell_per_sm=-1)):
+        with pytest.raises(aderdg.AderdgError):
+            aderdg.set_tuning(aderdg.SYS_BN, 4, aderdg.FP32_WIDE, **bad)
+    with pytest.raises(aderdg.AderdgError):
+        aderdg.set_tuning(aderdg.SYS_BN, 6, aderdg.FP32_WIDE)
+    aderdg.set_tuning(aderdg.SYS_BN, 4, aderdg.FP32_WIDE, **old)
