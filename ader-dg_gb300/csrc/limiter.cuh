@@ -113,19 +113,22 @@ __device__ __forceinline__ void rusanov_s(const PhysC<T>& pc, const T* QL, const
   constexpr int V = Sys::V;
   T FLf[2 * V], FRf[2 * V], smax;
   if constexpr (kRcp) {
+    // the flux along d only (the other direction's would be multiplied by 0)
     T eL, eR;
-    Sys::flux_eig_r(pc, QL, d, FLf, eL);
-    Sys::flux_eig_r(pc, QR, d, FRf, eR);
+    Sys::flux_dir_eig_r(pc, QL, d, FLf, eL);
+    Sys::flux_dir_eig_r(pc, QR, d, FRf, eR);
     smax = tmax(eL, eR);
+#pragma unroll
+    for (int v = 0; v < V; ++v) F[v] = T(0.5) * (FLf[v] + FRf[v]) - T(0.5) * smax * (QR[v] - QL[v]);
   } else {
     smax = tmax(Sys::max_eig(pc, QL, d), Sys::max_eig(pc, QR, d));
     Sys::flux(pc, QL, FLf);
     Sys::flux(pc, QR, FRf);
-  }
-  const T nv0 = d == 0 ? T(1) : T(0), nv1 = d == 0 ? T(0) : T(1);
+    const T nv0 = d == 0 ? T(1) : T(0), nv1 = d == 0 ? T(0) : T(1);
 #pragma unroll
-  for (int v = 0; v < V; ++v)
-    F[v] = T(0.5) * ((FLf[v] + FRf[v]) * nv0 + (FLf[V + v] + FRf[V + v]) * nv1) - T(0.5) * smax * (QR[v] - QL[v]);
+    for (int v = 0; v < V; ++v)
+      F[v] = T(0.5) * ((FLf[v] + FRf[v]) * nv0 + (FLf[V + v] + FRf[V + v]) * nv1) - T(0.5) * smax * (QR[v] - QL[v]);
+  }
   if constexpr (Sys::ID == kSysBN) {
     if constexpr (kRcp) BNSys::roe_times_jump_r(pc, QL, QR, d, D);
     else BNSys::roe_times_jump(pc, QL, QR, d, D);
@@ -227,7 +230,17 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
     const T ix0 = T(1) / ldx0, ix1 = T(1) / ldx1;  // kRcp only
     auto divx = [&](T q) -> T { if constexpr (kRcp) return q * ix0; else return q / ldx0; };
     auto divy = [&](T q) -> T { if constexpr (kRcp) return q * ix1; else return q / ldx1; };
-    auto flux = [&](const T* Q, T* F) { if constexpr (kRcp) Sys::flux_r(pc, Q, F); else Sys::flux(pc, Q, F); };
+    // the flux of Q into F[d * V + v]; kRcp: along d only (the MUSCL half step
+    // uses the x flux of the x-reconstructed states and the y flux of the
+    // y-reconstructed ones), otherwise both directions as the reference
+    auto flux = [&](const T* Q, int d, T* F) {
+      if constexpr (kRcp) {
+        T e;
+        Sys::flux_dir_eig_r(pc, Q, d, F + d * V, e);
+      } else {
+        Sys::flux(pc, Q, F);
+      }
+    };
     auto ncp = [&](const T* Q, T ax, T ay, T* Sr) {
       if constexpr (Sys::ID == kSysBN) {
         if constexpr (kRcp) BNSys::src_ncp_r(pc, Q, ax, ay, Sr);
@@ -265,6 +278,10 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
       if (nbs[n] != 0) continue;
       const int r = p - n * (V * P * S);
       const int v = r / (P * S), kk = (r / S) % P, sb = r % S;
+      // the neighbours below / above contribute their two rows nearest to
+      // the cell only (subcell rows S-2, S-1 / 0, 1)
+      const int bj = n / 3 - 1;
+      if ((bj < 0 && sb < S - 2) || (bj > 0 && sb > 1)) continue;
       const T* u = NB + (n * V + v) * P2;
       T ly = T(0);
 #pragma unroll
@@ -345,8 +362,8 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
         wl[v] = q0[v] - T(0.5) * slx[hx(v, ii, jj)];
         wr[v] = q0[v] + T(0.5) * slx[hx(v, ii, jj)];
       }
-      flux(wl, FLx);
-      flux(wr, FRx);
+      flux(wl, 0, FLx);
+      flux(wr, 0, FRx);
 #pragma unroll
       for (int v = 0; v < V; ++v) {
         if constexpr (BN) Qt[v] = src[v] - divx(FRx[v] - FLx[v]);
@@ -359,8 +376,8 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
         wl[v] = q0[v] - T(0.5) * sly[hx(v, ii, jj)];
         wr[v] = q0[v] + T(0.5) * sly[hx(v, ii, jj)];
       }
-      flux(wl, FLy);
-      flux(wr, FRy);
+      flux(wl, 1, FLy);
+      flux(wr, 1, FRy);
 #pragma unroll
       for (int v = 0; v < V; ++v) {
         Qt[v] = Qt[v] - divy(FRy[V + v] - FLy[V + v]);

@@ -114,6 +114,21 @@ struct EulerSys {
     flux_eig_r<T>(pc, Q, d, nullptr, e);
     return e;
   }
+  // The flux along axis d only, F[v] (Fx = F[0..3], Fy = F[4..7] of
+  // flux_eig_r; Q1 v = Q2 u), and maxval(abs(Lambda)) along d
+  template <class T>
+  __device__ static void flux_dir_eig_r(const PhysC<T>& pc, const T* Q, int d, T* F, T& eig) {
+    const T irho = T(1) / Q[0];
+    const T u = Q[1] * irho, v = Q[2] * irho;
+    const T p = pc.gm1 * (Q[3] - T(0.5) * (Q[1] * u + Q[2] * v));
+    const T un = d == 0 ? u : v;
+    F[0] = d == 0 ? Q[1] : Q[2];
+    F[1] = Q[1] * un + (d == 0 ? p : T(0));
+    F[2] = Q[2] * un + (d == 1 ? p : T(0));
+    F[3] = un * (Q[3] + p);
+    const T c = tsqrt(pc.gamma * p * irho);
+    eig = tmax(tabs(un - c), tabs(un + c));
+  }
   // Constants of the FP32-mixed cell kernel (CFL eigenvalues, admissibility pre-test).
   struct FConst {
     float gm1, gamma;
@@ -411,6 +426,30 @@ struct BNSys {
     T e;
     flux_eig_r<T>(pc, Q, d, nullptr, e);
     return e;
+  }
+  // The flux along axis d only, F[v] (the d-th half of flux_eig_r's F; Q1 v_s
+  // = Q2 u_s), and maxval(abs(Lambda)) along d
+  template <class T>
+  __device__ static void flux_dir_eig_r(const PhysC<T>& pc, const T* Q, int d, T* F, T& eig) {
+    const T r = T(1) / (Q[0] * Q[4]);
+    const T i0 = Q[4] * r, i4 = Q[0] * r;
+    const T u_s = Q[1] * i0, v_s = Q[2] * i0, u_g = Q[5] * i4, v_g = Q[6] * i4;
+    const T phi_s = Q[8], phi_g = T(1) - Q[8];
+    const T pps = pc.gs1 * (Q[3] - T(0.5) * (Q[1] * u_s + Q[2] * v_s)) - pc.gsps * phi_s;  // phi p_s
+    const T ppg = pc.gg1 * (Q[7] - T(0.5) * (Q[5] * u_g + Q[6] * v_g)) - pc.ggpg * phi_g;  // phi_g p_g
+    const T us = d == 0 ? u_s : v_s, ug = d == 0 ? u_g : v_g;
+    F[0] = d == 0 ? Q[1] : Q[2];
+    F[1] = Q[1] * us + (d == 0 ? pps : T(0));
+    F[2] = Q[2] * us + (d == 1 ? pps : T(0));
+    F[3] = us * (Q[3] + pps);
+    F[4] = d == 0 ? Q[5] : Q[6];
+    F[5] = Q[5] * ug + (d == 0 ? ppg : T(0));
+    F[6] = Q[6] * ug + (d == 1 ? ppg : T(0));
+    F[7] = ug * (Q[7] + ppg);
+    F[8] = T(0);
+    const T a_s = tsqrt(pc.gs * (pps + pc.ps * phi_s) * i0);
+    const T a_g = tsqrt(pc.gg * (ppg + pc.pg * phi_g) * i4);
+    eig = tmax(tmax(tabs(ug - a_g), tabs(ug + a_g)), tmax(tabs(us - a_s), tabs(us + a_s)));
   }
   // p_g = (gamma_g - 1) (Q7 Q4 - (Q5^2 + Q6^2) / 2) / (Q4 phi_g) - gamma_g pi_g
   // and u_n = qn / Q0 (qn = n . (Q1, Q2)) from one reciprocal of Q0 Q4 phi_g

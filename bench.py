@@ -136,6 +136,37 @@ def predictor_flops_per_cell(system, N, ad_fused=True):
     return P2 * (setup + it1 + mids * mid + last + vol) + faces
 
 
+def subcell_flops_per_cell(system, N):
+    """Floating-point operations of the subcell re-solve (k_subcell, FP64 in the
+    FP32-mixed mode) per re-solved cell, from its loop structure: the 3x3
+    neighbourhood's subcell data (y pass of the rows the reconstruction reads,
+    x pass of the gathered strip; every neighbour counted unlimited), the
+    MUSCL-Hancock reconstruction (slopes, the four half-step fluxes along their
+    directions, the half-step update), the Rusanov fluxes of the subgrid
+    edges with their eigenvalues (Baer-Nunziato: plus the 3-point path
+    integral), the finite-volume update, put_subcell_data, the DMP
+    projections of the new polynomial and the CFL eigenvalues of its nodes.
+    A fused multiply-add counts 2, a division or square root 1, as in
+    predictor_flops_per_cell."""
+    P, S, V = N + 1, 2 * N + 1, NVAR[system]
+    R, H, NE = S + 4, S + 2, (S + 1) * S
+    dot = lambda n: 2 * n - 1  # noqa: E731
+    bn = system == 2
+    flux = 36 if bn else 15          # flux along one axis (reciprocal, velocities, pressure, components)
+    eig = 16 if bn else 7            # sound speeds and maxval(abs(Lambda))
+    ncp = 20 if bn else 0            # p_g, u_n and the NCP source
+    roe = 3 * (2 * 9 + 13 + 6) + 9 if bn else 0
+    gather = (3 * S + 12) * V * P * dot(P) + R * R * V * dot(P)
+    slope_states = H * H if bn else S * S
+    muscl = slope_states * 2 * V * 4 + H * H * (8 * V + 4 * flux + 4 * V + 8 * V + ncp + (V if bn else 0))
+    edges = 2 * NE * (2 * (flux + eig) + 5 * V + roe)
+    fv = S * S * (V * (16 if bn else 8) + ncp)
+    put = V * (P * S + P * P) * dot(S)
+    dmp = V * ((P * S + P * P) * dot(P) + (S * S + P * P) * dot(P))
+    cfl = P * P * (45 if bn else 21)
+    return gather + muscl + edges + fv + put + dmp + cfl
+
+
 # ---------------------------------------------------------------- clocks
 class ClockSampler:
     FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
@@ -373,12 +404,14 @@ def _resident(aderdg, specs, prec, W, K):
 
 
 def _profile_groups(groups):
-    """Per-launch device ms of one more (eager) step of every group, summed."""
-    tot = {}
-    for g in groups.values():
+    """Per-launch device ms of one more (eager) step of every group, summed,
+    and each group's re-solved cells in that step."""
+    tot, listed = {}, {}
+    for key, g in groups.items():
         for k, v in g.profile().items():
             tot[k] = tot.get(k, 0.0) + v
-    return tot
+        listed[key] = g.counters()["n_listed"]
+    return tot, listed
 
 
 def _launches_per_step(groups, prec, aderdg):
@@ -541,24 +574,38 @@ def allsum(dist, x):
     return float(t.item())
 
 
-def _traffic(aderdg, groups, mode_key):
-    """DRAM bytes of one k_predictor launch per group from the per-(system, N)
-    captures in profiles/traffic.json (bytes per DOF, times the group's DOFs),
-    and the limiter the captures name; (None, None) without a capture."""
+def _traffic(units, kernel_key, mode_key):
+    """DRAM bytes of one launch of a kernel over the groups, from the
+    per-(system, N) captures in profiles/traffic.json (bytes per unit --
+    DOF for k_predictor, re-solved cell for k_subcell -- times each group's
+    units), and the limiter the captures name; None where a group has no
+    capture."""
     try:
         with open(os.path.join(REPO, "profiles", "traffic.json")) as fh:
             tr = json.load(fh)
     except (OSError, ValueError):
         return None, None
-    per = tr.get("k_predictor_bytes_per_dof", {}).get(mode_key, {})
+    per = tr.get(kernel_key, {}).get(mode_key, {})
     tot, miss = 0.0, 0
-    for key, dofs in groups.items():
+    for key, n in units.items():
         b = per.get("%d_%d" % key)
         if b is None:
             miss += 1
         else:
-            tot += b * dofs
-    return (tot if miss == 0 else None), tr.get("k_predictor_limiter", {}).get(mode_key)
+            tot += b * n
+    return (tot if miss == 0 else None), tr.get("limiter", {}).get(kernel_key, {}).get(mode_key)
+
+
+def _tuning_desc(aderdg):
+    """The tuner's table the run used (applied when the library loaded)."""
+    import hashlib
+    path = os.environ.get("ADERDG_TUNING", aderdg.core.TUNING_FILE)
+    if not path or not os.path.exists(path):
+        return {"table": None, "what": "default kernel shapes"}
+    with open(path, "rb") as fh:
+        digest = hashlib.sha256(fh.read()).hexdigest()[:16]
+    return {"table": os.path.relpath(path, REPO), "sha256_16": digest,
+            "what": "kernel shapes of the FP32 modes picked per (system, N, precision) by aderdg/tuner.py"}
 
 
 def run_mix(args, aderdg, dist, rank, ws, lr):
@@ -586,7 +633,7 @@ def run_mix(args, aderdg, dist, rank, ws, lr):
     if not args.no_plain:
         plain = run_plain_fp64(aderdg, specs, W, K, compare)
     for r in runs.values():
-        r["phases"] = _profile_groups(r["groups"])
+        r["phases"], r["listed"] = _profile_groups(r["groups"])
         r["group_dofs"] = {}
         for key, slot, cfg in r["slots"]:
             r["group_dofs"][key] = r["group_dofs"].get(key, 0) + cfg.dofs
@@ -611,15 +658,36 @@ def run_mix(args, aderdg, dist, rank, ws, lr):
     kern_ms = {k: v for k, v in ph.items() if k not in ("begin", "end")}
     pred_ms = ph.get("predictor", 0.0)
     ach = pred_flops / (pred_ms * 1e-3) / 1e9 if pred_ms > 0 else None
-    traffic, limiter = _traffic(aderdg, head["group_dofs"], "fp32" if mixed else "fp64")
+    mode_key = "fp32" if mixed else "fp64"
+    traffic, limiter = _traffic(head["group_dofs"], "k_predictor_bytes_per_dof", mode_key)
+    listed = {k: n for k, n in head["listed"].items() if k[0] != aderdg.SYS_ADVDIFF}
+    sub_traffic, sub_limiter = _traffic(listed, "k_subcell_bytes_per_listed_cell", mode_key)
+    dominant = max(kern_ms, key=lambda k: kern_ms[k])
+    sub_ms = ph.get("subcell", 0.0)
+    sub_flops = sum(subcell_flops_per_cell(key[0], key[1]) * n for key, n in head["listed"].items())
+    sub_ach = sub_flops / (sub_ms * 1e-3) / 1e9 if sub_ms > 0 else None
+    roof_sub = {"bound": "fp64", "kernel": "k_subcell (the subcell re-solve, FP64, all groups with the limiter)",
+                "achieved": sub_ach, "peak": fp64_peak, "unit": "GFLOP/s",
+                "frac": (sub_ach / fp64_peak) if sub_ach else None,
+                "peak_source": "FP64 FMA throughput measured on this GPU by aderdg_probe_peaks",
+                "flops_per_launch": sub_flops, "listed_cells": int(sum(head["listed"].values())),
+                "flop_model": "bench.py subcell_flops_per_cell x re-solved cells of the profiled step",
+                "launch_ms": sub_ms, "dominant_phase": dominant,
+                "phase_share": {k: v / sum(kern_ms.values()) for k, v in kern_ms.items()},
+                "phase_ms_one_step": ph, "traffic": sub_traffic,
+                "traffic_source": "profiles/traffic.json: DRAM bytes per re-solved cell of k_subcell per (system, N) "
+                                  "group from one ncu capture of the batched mix, times each group's re-solved cells",
+                "limiter": sub_limiter}
     roof = {"bound": "fp32" if mixed else "fp64", "kernel": "k_predictor (all (system, N) groups of the mix)",
             "achieved": ach, "peak": peak, "unit": "GFLOP/s", "frac": (ach / peak) if ach else None,
             "peak_source": "FMA throughput measured on this GPU by aderdg_probe_peaks (dependent-FMA "
                            "microkernel); MEASURED_PEAKS.json carries no non-tensor FP32/FP64 figure",
             "flops_per_launch": pred_flops, "flop_model": "bench.py predictor_flops_per_cell x cells",
-            "launch_ms": pred_ms, "dominant_phase": max(kern_ms, key=lambda k: kern_ms[k]),
+            "launch_ms": pred_ms, "dominant_phase": dominant,
             "phase_share": {k: v / sum(kern_ms.values()) for k, v in kern_ms.items()},
             "phase_ms_one_step": ph, "traffic": traffic,
+            "groups": {"%d_%d" % k: {"dofs": head["group_dofs"][k], "listed_cells": head["listed"].get(k, 0)}
+                       for k in head["group_dofs"]},
             "traffic_source": "profiles/traffic.json: DRAM bytes per DOF of k_predictor per (system, N) group from "
                               "one ncu capture of the batched mix, times each group's DOFs",
             "limiter": limiter}
@@ -638,7 +706,11 @@ def run_mix(args, aderdg, dist, rank, ws, lr):
                        (head["dev_bytes"] / 1e9), "parallelism": "request shards, no collective" if ws > 1 else
                        "single", "serving": "config 5: %d requests, Poisson rates %s req/s (e2e.rates)" %
                        (args.serve_requests, args.rates)},
-            "roofline": roof, "clocks": clk.summary(), "gpu_launches": head["launches"] * K}
+            "roofline": roof_sub if (dominant == "subcell" and sub_ach) else roof,
+            "roofline_predictor" if (dominant == "subcell" and sub_ach) else "roofline_subcell":
+                roof if (dominant == "subcell" and sub_ach) else roof_sub,
+            "clocks": clk.summary(), "gpu_launches": head["launches"] * K,
+            "tuning": _tuning_desc(aderdg)}
     for lab, r in runs.items():
         if lab == head_lab:
             continue
