@@ -24,7 +24,7 @@ DRIVER_PATH = os.path.join(BUILD_DIR, "aderdg_driver")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SYSTEMS = (0, 1, 2)
 DEGREES = (1, 2, 3, 4, 5)
-PRED_VARIANTS = 6  # predictor.cuh kPredVariants
+PRED_VARIANTS = 7  # predictor.cuh kPredVariants
 
 
 def _nvcc():

@@ -4,8 +4,9 @@ For each (system, N, precision) it times the candidates of three knobs on the
 GPU and keeps the fastest:
   predictor       the FP32 space-time predictor's shape: cells per CTA
                   (default, twice, half), one more CTA per SM for the register
-                  allocation, the middle Picard iterations unrolled, or
-                  per-node contractions instead of the row/column tiling
+                  allocation, the middle Picard iterations unrolled,
+                  per-node contractions instead of the row/column tiling, or
+                  the row/column pass on the tensor cores (mma.sync, 3xTF32)
                   (predictor.cuh PredVariant);
   cells           the cell kernel's CTA size (default, twice, half);
   subcell_per_sm  the subcell re-solve's persistent CTAs per SM (0: as many
@@ -19,9 +20,12 @@ counterpart: its shapes are compile-time parameters (Euler/ader_dg.f90:17-20).
 
     python -m aderdg.tuner [--out FILE] [--precisions fp32_mixed,fp32_wide]
                            [--systems 0,1,2] [--degrees 1,2,3,4,5] [--reps 5]
+                           [--workload NAME --side S]
 
 writes the table (default: the package's tuning_gb300.json, which aderdg.load
-applies; ADERDG_TUNING names another file).
+applies; ADERDG_TUNING names another file).  --workload / --side time the
+candidates on another workload of the system (e.g. euler_vortex at 256^2)
+instead of its base case.
 """
 import argparse
 import json
@@ -40,11 +44,14 @@ SIDE = {1: 320, 2: 256, 3: 192, 4: 160, 5: 128}  # 40k-100k cells, as the larger
 PHASE = {"predictor": "predictor", "cells": "cells", "subcell_per_sm": "subcell"}
 
 
-def tune_one(system, N, precision, reps=5, side=None, warm_steps=10):
+def tune_one(system, N, precision, reps=5, side=None, warm_steps=10, workload=None):
     """Tunes (system, N, precision) and sets the result in the library's
     table; returns {"predictor", "cells", "subcell_per_sm", "ms": {knob: {candidate: ms}}}."""
     n_pred, n_cells = tuning_variants()
-    cfg, ic, params, tend = workloads.make(BASE[system], side=side or SIDE[N], N=N, precision=precision)
+    name = workload or BASE[system]
+    if workloads.WORKLOADS[name]["system"] != system:
+        raise ValueError("workload %s is not of system %d" % (name, system))
+    cfg, ic, params, tend = workloads.make(name, side=side or SIDE[N], N=N, precision=precision)
     limiter = cfg.limiter and system != SYS_ADVDIFF
     s = Solver(cfg)
     s.initial_condition(ic, params)
@@ -66,23 +73,24 @@ def tune_one(system, N, precision, reps=5, side=None, warm_steps=10):
         times[knob] = med
     s.close()
     set_tuning(system, N, precision, **cur)
-    return dict(cur, ms=times, workload=dict(name=BASE[system], side=cfg.imax, N=N))
+    return dict(cur, ms=times, workload=dict(name=name, side=cfg.imax, N=N))
 
 
 def tune(systems=(SYS_ADVDIFF, SYS_EULER, SYS_BN), degrees=(1, 2, 3, 4, 5), precisions=(FP32_MIXED, FP32_WIDE),
-         reps=5, log=None):
+         reps=5, log=None, workload=None, side=None):
     """Tunes every combination; returns the table {"entries": {...}, ...}."""
     entries = {}
     for prec in precisions:
         for system in systems:
             for N in degrees:
                 t0 = time.perf_counter()
-                r = tune_one(system, N, prec, reps=reps)
+                r = tune_one(system, N, prec, reps=reps, workload=workload, side=side)
                 entries["%d_%d_%d" % (system, N, prec)] = r
                 if log:
-                    log("system %d N %d precision %d: predictor %d cells %d subcell/SM %d (%.1f s)"
+                    log("system %d N %d precision %d: predictor %d cells %d subcell/SM %d (%.1f s); predictor ms %s"
                         % (system, N, prec, r["predictor"], r["cells"], r["subcell_per_sm"],
-                           time.perf_counter() - t0))
+                           time.perf_counter() - t0,
+                           " ".join("%d:%.4f" % (k, v) for k, v in sorted(r["ms"]["predictor"].items()))))
     return {"version": 1, "entries": entries,
             "what": "kernel shapes of the FP32 modes per '<system>_<N>_<precision>', picked by aderdg/tuner.py "
                     "from per-kernel device times (ms: median per candidate)"}
@@ -95,13 +103,15 @@ def main(argv=None):
     ap.add_argument("--systems", default="0,1,2")
     ap.add_argument("--degrees", default="1,2,3,4,5")
     ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--workload", default=None, help="time on this workload instead of the base case")
+    ap.add_argument("--side", type=int, default=None)
     args = ap.parse_args(argv)
     os.environ["ADERDG_TUNING"] = ""  # start from the defaults, not from an earlier table
     load()
     names = {"fp32_mixed": FP32_MIXED, "fp32_wide": FP32_WIDE}
     table = tune(systems=[int(x) for x in args.systems.split(",")], degrees=[int(x) for x in args.degrees.split(",")],
                  precisions=[names[x] for x in args.precisions.split(",")], reps=args.reps,
-                 log=lambda m: print(m, flush=True))
+                 log=lambda m: print(m, flush=True), workload=args.workload, side=args.side)
     with open(args.out, "w") as fh:
         json.dump(table, fh, indent=1, sort_keys=True)
     print("wrote", args.out)

@@ -4,14 +4,15 @@
 //   cells of all instances are numbered globally; instance k owns the cell
 //   range [cell_base, cell_base + imax*jmax), cell = i + imax*j inside it.
 //   uh      [cell][P*P nodes][V]   FP64, exactly the Fortran uh(v,i,j,I,J)
-//   duh     [cell][P*P][V]         FP64 (FP32 in the FP32-mixed mode)
+//   duh     [cell][P*P][V]         FP64 (FP32 in the FP32 modes)
 //   qbnd    [cell][4][P][V]        face-major: a face's P points contiguous
 //   fbnd    [cell][4][P][V]        (AD: gradQbnd [cell][4][P][2][V]); the API's
 //                                  get/set give the reference's qbnd(v,face,l,I,J)
 //   fu/gu   x faces [fx_base + i + (imax+1)*j][P][V], y faces [fy_base + i + imax*j][P][V]
-//           (FP32 in the FP32-mixed mode)
+//           (FP32 in the FP32 modes)
 //   lh      [cell][S*S][V]         subcell state of limited cells
 //   mm      [cell][2][V]           per-cell min/max for the DMP neighbourhood
+//   mme     [cell][V]              FP32-mixed: a bound on the error of mm (0: exact FP64 value)
 #pragma once
 
 #include <cstdint>
@@ -119,10 +120,10 @@ struct BatchArgs {
   long long ncells;
   long long nfx, nfy;                // total x / y faces
   double* uh[2];                     // uh [cell][P*P][V]
-  double* duh;                       // FP32 storage in the FP32-mixed mode
+  double* duh;                       // FP32 storage in the FP32 modes
   void* qbnd;                        // R precision (predictor output)
   void* fbnd;                        // R precision; AD: gradQbnd
-  double* fu;                        // BN: Fm; fu..gp FP32 storage in the FP32-mixed mode
+  double* fu;                        // BN: Fm; fu..gp FP32 storage in the FP32 modes
   double* gu;                        // BN: Gm
   double* fp;                        // BN only: Fp
   double* gp;                        // BN only: Gp

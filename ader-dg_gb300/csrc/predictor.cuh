@@ -34,12 +34,13 @@ namespace aderdg {
 // (system, N, precision): kCta scales the cells per CTA (+1: twice the
 // threads, -1: half), kBlocks adds to the CTAs per SM the register
 // allocation aims at, kUnroll unrolls the middle Picard iterations, and
-// kNoRowCol contracts per node instead of by rows and columns.  PredTune<>
-// is the hand-measured default.
-template <int kCta = 0, int kBlocks = 0, bool kUnroll = false, bool kNoRowCol = false>
+// kNoRowCol contracts per node instead of by rows and columns, and kMma runs
+// the row/column pass on the tensor cores (mma_pass).  PredTune<> is the
+// hand-measured default.
+template <int kCta = 0, int kBlocks = 0, bool kUnroll = false, bool kNoRowCol = false, bool kMma = false>
 struct PredTune {
   static constexpr int CTA = kCta, BLOCKS = kBlocks;
-  static constexpr bool UNROLL = kUnroll, NO_ROWCOL = kNoRowCol;
+  static constexpr bool UNROLL = kUnroll, NO_ROWCOL = kNoRowCol, MMA = kMma;
 };
 // the tuner's candidates, variant 0 the default
 template <int K>
@@ -50,8 +51,9 @@ using PredVariant = typename std::conditional<
         typename std::conditional<K == 3, PredTune<0, 1>,
                                   typename std::conditional<K == 4, PredTune<0, 0, true>,
                                                             typename std::conditional<K == 5, PredTune<0, 0, false, true>,
-                                                                                      PredTune<>>::type>::type>::type>::type>::type;
-constexpr int kPredVariants = 6;
+                                                                                      typename std::conditional<K == 6, PredTune<0, 0, false, false, true>,
+                                                                                                                PredTune<>>::type>::type>::type>::type>::type>::type;
+constexpr int kPredVariants = 7;
 
 template <class Sys, int N, class R, class Tune = PredTune<>>
 struct PredCfg {
@@ -86,6 +88,7 @@ struct PredCfg {
   // P >= 5 the y pass takes level j and column i (the lanes of a quarter-warp
   // then meet no bank group twice at these paddings).
   static constexpr bool ROWCOL = PLANAR && P >= 4 && !Tune::NO_ROWCOL;
+  static constexpr bool MMA = ROWCOL && Tune::MMA;  // the row/column pass on the tensor cores
   static constexpr int XL = ROWCOL ? P2 + ((P == 5) ? 0 : 1) : 2 * P2;  // nodes from x level to x level
   static constexpr int YL = ROWCOL ? P2 + ((P == 5) ? 4 : 2) : 2 * P2;
   static constexpr int Y0 = ROWCOL ? P * XL : P2;  // node offset of the y fluxes of level 0
@@ -240,6 +243,87 @@ __device__ __forceinline__ void rowcol_pass(float* __restrict__ cs, int i, int j
     line(cs + c * C::CS + ((size_t)i * C::XL + P * j) * 4, 4);
     const int m = P >= 5 ? j : i, col = P >= 5 ? i : j;
     line(cs + c * C::CS + ((size_t)C::Y0 + (size_t)m * C::YL + col) * 4, 4 * P);
+  }
+}
+
+// TF32 part of an FP32 value (round to nearest, ties away) as the .b32 operand of mma.sync
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+// D += A B, one warp: A 16x8 TF32 (row-major fragment a0..a3), B 8x8 TF32
+// (column fragment b0, b1), D 16x8 FP32
+__device__ __forceinline__ void mma_tf32(float* d, const uint32_t* a, uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Tensor-core form of the row/column pass (PredTune kMma): every x row and y
+// column of every time level of the CTA's cells (the lines rowcol_pass
+// contracts), 16 lines to one mma.sync m16n8k8 tile, X(o) <- sum_k Kxi(k, o)
+// X(k) with k padded from P to 8 and the P outputs to 8.  Each FP32 value is
+// split into a TF32 high part and a TF32 low part, and three products are
+// accumulated in FP32 (lo*hi + hi*lo + hi*hi; the dropped lo*lo term is
+// below FP32 rounding), so the results carry FP32 accuracy.  Line L (v
+// fastest) = (cell, chunk, direction, level, row or column, component v);
+// the lines are read and written in place, and the node's thread applies
+// dt/(dx w_i), dt/(dy w_j) when it reads them back, as after rowcol_pass.
+template <class C, class Ops>
+__device__ __forceinline__ void mma_pass(float* __restrict__ sm, int t, const Ops& op) {
+  constexpr int P = C::P;
+  static_assert(P <= 8, "one k8 step");
+  constexpr int LPC = C::NCH * 2 * P * P * 4;  // lines per cell
+  constexpr int LINES = C::CPB * LPC, TILES = (LINES + 15) / 16, NW = C::THREADS / 32;
+  const int lane = t & 31, w = t >> 5, g = lane >> 2, q = lane & 3;
+  // B(k, o) = Kxi(k, o) = op.Kxi[k + P o]: b0 (k = q, o = g), b1 (k = q + 4, o = g)
+  const float b0 = (g < P) ? op.Kxi[q + P * g] : 0.0f;
+  const float b1 = (g < P && q + 4 < P) ? op.Kxi[q + 4 + P * g] : 0.0f;
+  const uint32_t bh0 = to_tf32(b0), bh1 = to_tf32(b1);
+  const uint32_t bl0 = to_tf32(b0 - __uint_as_float(bh0)), bl1 = to_tf32(b1 - __uint_as_float(bh1));
+  auto line = [&](int L, int& base, int& stride) {
+    const int v = L & 3, r1 = L >> 2;
+    const int r = r1 % P, r2 = r1 / P;
+    const int l = r2 % P, r3 = r2 / P;
+    const int d = r3 & 1, r4 = r3 >> 1;
+    const int ch = r4 % C::NCH, c = r4 / C::NCH;
+    const int cb = c * C::CELL_ELEMS + ch * C::CS + v;
+    if (d == 0) { base = cb + (l * C::XL + P * r) * 4; stride = 4; }
+    else { base = cb + (C::Y0 + l * C::YL + r) * 4; stride = 4 * P; }
+  };
+  for (int tile = w; tile < TILES; tile += NW) {
+    const int L0 = tile * 16 + g, L1 = L0 + 8;
+    const bool ok0 = L0 < LINES, ok1 = L1 < LINES;
+    int s0 = 0, d0 = 0, s1 = 0, d1 = 0;
+    if (ok0) line(L0, s0, d0);
+    if (ok1) line(L1, s1, d1);
+    // A fragment: a0 (row g, k = q), a1 (row g + 8, k = q), a2 (row g, k = q + 4), a3 (row g + 8, k = q + 4)
+    float af[4];
+    af[0] = ok0 ? sm[s0 + q * d0] : 0.0f;
+    af[1] = ok1 ? sm[s1 + q * d1] : 0.0f;
+    af[2] = (ok0 && q + 4 < P) ? sm[s0 + (q + 4) * d0] : 0.0f;
+    af[3] = (ok1 && q + 4 < P) ? sm[s1 + (q + 4) * d1] : 0.0f;
+    uint32_t ah[4], al[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      ah[e] = to_tf32(af[e]);
+      al[e] = to_tf32(af[e] - __uint_as_float(ah[e]));
+    }
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    mma_tf32(acc, al, bh0, bh1);
+    mma_tf32(acc, ah, bl0, bl1);
+    mma_tf32(acc, ah, bh0, bh1);
+    __syncwarp();  // every lane's loads of these lines precede the stores
+    // D fragment: d0, d1 (row g, o = 2q, 2q + 1), d2, d3 (row g + 8, o = 2q, 2q + 1)
+    const int o = 2 * q;
+    if (ok0 && o < P) sm[s0 + o * d0] = acc[0];
+    if (ok0 && o + 1 < P) sm[s0 + (o + 1) * d0] = acc[1];
+    if (ok1 && o < P) sm[s1 + o * d1] = acc[2];
+    if (ok1 && o + 1 < P) sm[s1 + (o + 1) * d1] = acc[3];
   }
 }
 
@@ -591,7 +675,10 @@ __global__ void __launch_bounds__(PredCfg<Sys, N, R, Tune>::THREADS, PredCfg<Sys
       }
       __syncthreads();
       if constexpr (!last) {
-        if constexpr (C::ROWCOL) {
+        if constexpr (C::MMA) {
+          mma_pass<C>(sm, t, op);
+          __syncthreads();
+        } else if constexpr (C::ROWCOL) {
           rowcol_pass<C>(cs, i, j, op);
           __syncthreads();
         }

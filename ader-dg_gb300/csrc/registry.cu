@@ -12,7 +12,8 @@ namespace aderdg {
   void register_predvar_##S##_##NN##_2(KernelTable& t); \
   void register_predvar_##S##_##NN##_3(KernelTable& t); \
   void register_predvar_##S##_##NN##_4(KernelTable& t); \
-  void register_predvar_##S##_##NN##_5(KernelTable& t);
+  void register_predvar_##S##_##NN##_5(KernelTable& t); \
+  void register_predvar_##S##_##NN##_6(KernelTable& t);
 #define ADERDG_DECL_N(S) ADERDG_DECL(S, 1) ADERDG_DECL(S, 2) ADERDG_DECL(S, 3) ADERDG_DECL(S, 4) ADERDG_DECL(S, 5)
 ADERDG_DECL_N(0)
 ADERDG_DECL_N(1)
@@ -30,7 +31,8 @@ struct Registry {
   register_predvar_##S##_##NN##_2(t[S][NN]); \
   register_predvar_##S##_##NN##_3(t[S][NN]); \
   register_predvar_##S##_##NN##_4(t[S][NN]); \
-  register_predvar_##S##_##NN##_5(t[S][NN]);
+  register_predvar_##S##_##NN##_5(t[S][NN]); \
+  register_predvar_##S##_##NN##_6(t[S][NN]);
 #define ADERDG_REG_N(S) ADERDG_REG(S, 1) ADERDG_REG(S, 2) ADERDG_REG(S, 3) ADERDG_REG(S, 4) ADERDG_REG(S, 5)
     ADERDG_REG_N(0)
     ADERDG_REG_N(1)

@@ -17,7 +17,7 @@
 namespace aderdg {
 
 // candidates of the tuner (predictor.cuh PredVariant, cells.cuh CellCfg VAR)
-constexpr int kPredVariantsMax = 6;
+constexpr int kPredVariantsMax = 7;
 constexpr int kCellVariantsMax = 3;
 
 struct KernelTable {

@@ -4,16 +4,16 @@
 ! A maintainer adds this module to the reference's Makefile, `use`s it in
 ! main.f90 and replaces the per-cell phase loops of the time loop
 ! (Euler/main.f90:24-100) by the grid-level calls below; module arrays are
-! passed unchanged (Fortran layout uh(nVar,N+1,N+1,IMAX,JMAX)).  See
-! INTEGRATION.md for the edited loop.  No Fortran compiler exists on the
-! build machines of this project, so this file is shipped uncompiled.
+! passed unchanged (Fortran layout uh(nVar,N+1,N+1,IMAX,JMAX)).  No Fortran
+! compiler exists on the build machines of this project, so this file is
+! shipped uncompiled.
 module aderdg_gpu
     use iso_c_binding
     implicit none
 
     integer(c_int), parameter :: ADERDG_OK = 0
     integer(c_int), parameter :: ADERDG_SYS_ADVDIFF = 0, ADERDG_SYS_EULER = 1, ADERDG_SYS_BN = 2
-    integer(c_int), parameter :: ADERDG_FP64 = 0, ADERDG_FP32_MIXED = 1
+    integer(c_int), parameter :: ADERDG_FP64 = 0, ADERDG_FP32_MIXED = 1, ADERDG_FP32_WIDE = 2
 
     type, bind(C) :: aderdg_config
         integer(c_int) :: system, N, imax, jmax

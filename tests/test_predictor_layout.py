@@ -150,3 +150,58 @@ def test_flux_buffer_fits_the_cell_slot(system, N):
     assert 4 * (top + 1) <= c["flux"] <= c["cell"]
     assert c["cell"] >= 3 * c["V"] * c["P2"]                   # epilogue Q, FX, FY [V][P2]
     assert c["cell"] % 4 == 0 and c["cpb"] * c["cell"] * 4 <= 100 * 1024 or c["cpb"] == 1
+
+
+def mma_lines(c):
+    """(base, stride) in floats of every line of mma_pass (predictor.cuh): line
+    L (component v fastest) = (cell, chunk, direction, level, row or column, v)."""
+    P, out = c["P"], []
+    for L in range(c["cpb"] * c["NCH"] * 2 * P * P * 4):
+        v, r1 = L & 3, L >> 2
+        r, r2 = r1 % P, r1 // P
+        lv, r3 = r2 % P, r2 // P
+        d, r4 = r3 & 1, r3 >> 1
+        ch, cell = r4 % c["NCH"], r4 // c["NCH"]
+        cb = cell * c["cell"] + ch * 4 * c["PLANE"] + v
+        if d == 0:
+            out.append((cb + (lv * c["XL"] + P * r) * 4, 4))
+        else:
+            out.append((cb + (c["Y0"] + lv * c["YL"] + r) * 4, 4 * P))
+    return out
+
+
+@pytest.mark.parametrize("system,N", [(s, N) for s, N in CASES if N >= 3])
+def test_mma_pass_lines_are_the_row_column_lines(system, N):
+    """The tensor-core pass contracts the lines of the row/column pass: the
+    same elements, each in exactly one line (so that the warps' in-place
+    writes never meet), inside the CTA's cell slots."""
+    c = pred_cfg(system, N)
+    P = c["P"]
+    a = layout(c)
+    expect = set()
+    for cell in range(c["cpb"]):
+        for ch in range(c["NCH"]):
+            for d in (0, 1):
+                for lv in range(P):
+                    for x in range(P):
+                        for y in range(P):
+                            for v in range(4):
+                                expect.add(cell * c["cell"] + 4 * a(ch, d, lv, x, y) + v)
+    seen = []
+    for base, stride in mma_lines(c):
+        seen += [base + k * stride for k in range(P)]
+    assert len(seen) == len(set(seen)) == len(expect)
+    assert set(seen) == expect
+    assert max(seen) < c["cpb"] * c["cell"]
+    # the A-fragment loads of one tile (row g = lane / 4 reads element lane % 4):
+    # shared-memory wavefronts per 32-bit warp access, for the record
+    lines = mma_lines(c)
+    worst = 0
+    for t0 in range(0, len(lines) - 15, 16):
+        for half in (0, 8):
+            words = [lines[t0 + half + (ln >> 2)][0] + (ln & 3) * lines[t0 + half + (ln >> 2)][1] for ln in range(32)]
+            banks = {}
+            for w in set(words):
+                banks.setdefault(w % 32, set()).add(w)
+            worst = max(worst, max(len(b) for b in banks.values()))
+    print("system %d N %d: mma_pass A loads, worst %d wavefronts per access" % (system, N, worst))
