@@ -532,7 +532,9 @@ def run_single(args, aderdg, dist, rank, ws, lr):
             "config": {"workload": args.workload, "N": cfg.N, "grid": [cfg.imax, cfg.jmax],
                        "precision": args.precision, "l2": "flushed before every timed step"},
             "latency_ms": {"p50": float(np.percentile(ms, 50)), "p99": float(np.percentile(ms, 99))},
-            "phase_ms": phases, "gpu_launches": (7 if cfg.limiter else 5) * args.steps,
+            "phase_ms": phases,
+            "gpu_launches": ((8 if prec == aderdg.FP32_MIXED else 7)
+                             if cfg.limiter and cfg.system != aderdg.SYS_ADVDIFF else 5) * args.steps,
             "roofline": {"bound": "fp32" if prec == aderdg.FP32_MIXED else "fp64", "kernel": "k_predictor",
                          "achieved": ach, "peak": fpeak, "unit": "GFLOP/s", "frac": ach / fpeak, "traffic": None,
                          "peak_source": "aderdg_probe_peaks on this GPU"},
