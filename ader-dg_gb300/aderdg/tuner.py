@@ -15,7 +15,10 @@ The knobs are tuned one after the other, each with the others at their best
 so far.  A candidate's time is its kernel's device time in eager steps with
 CUDA events between the launches (aderdg_profile_step), the median over
 `reps` rounds that interleave the candidates, on the system's base case at a
-grid whose cell count is typical of the request mix.  The reference has no
+grid whose cell count is typical of the request mix.  A candidate replaces
+the default only when it is at least MARGIN (2%) faster, so that timing noise
+does not pick shapes (a candidate that does not apply to a system and degree,
+e.g. the tensor-core pass below N = 3, runs the default and times alike).  The reference has no
 counterpart: its shapes are compile-time parameters (Euler/ader_dg.f90:17-20).
 
     python -m aderdg.tuner [--out FILE] [--precisions fp32_mixed,fp32_wide]
@@ -42,6 +45,7 @@ from .core import (FP32_MIXED, FP32_WIDE, SYS_ADVDIFF, SYS_BN, SYS_EULER, TUNING
 BASE = {SYS_ADVDIFF: "ad_sine", SYS_EULER: "euler_rp2d", SYS_BN: "bn_cylinder"}
 SIDE = {1: 320, 2: 256, 3: 192, 4: 160, 5: 128}  # 40k-100k cells, as the larger requests of the mix
 PHASE = {"predictor": "predictor", "cells": "cells", "subcell_per_sm": "subcell"}
+MARGIN = 0.02
 
 
 def tune_one(system, N, precision, reps=5, side=None, warm_steps=10, workload=None):
@@ -69,7 +73,8 @@ def tune_one(system, N, precision, reps=5, side=None, warm_steps=10, workload=No
                 t, ph = s.profile_step(t, tend)
                 samples[c].append(ph[PHASE[knob]])
         med = {c: float(np.median(v)) for c, v in samples.items()}
-        cur[knob] = min(med, key=lambda c: med[c])
+        best = min(med, key=lambda c: med[c])
+        cur[knob] = best if med[best] < (1.0 - MARGIN) * med[cands[0]] else cands[0]
         times[knob] = med
     s.close()
     set_tuning(system, N, precision, **cur)

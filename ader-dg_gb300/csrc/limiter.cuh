@@ -74,21 +74,32 @@ struct SubCfg {
   static constexpr int R = S + 4;  // gathered region: subcells -1 .. S+2 (1-based)
   static constexpr int H = S + 2;  // reconstructed region: 0 .. S+1
   static constexpr int THREADS = 128;
-  // CTAs per SM the register allocation aims at (FP32: one more than the
-  // unconstrained allocation allows where that does not spill)
-  static constexpr int MIN_BLOCKS = sizeof(T) == 4 ? (Sys::ID == kSysBN ? (N == 3 ? 4 : N == 2 ? 5 : 1) : 6) : 1;
+  // CTAs per SM the register allocation aims at.  FP32: one more than the
+  // unconstrained allocation allows where that does not spill.  FP64 (the
+  // FP64 pipe bounds it): as many as shared memory admits, up to 4 (Euler:
+  // 128 registers; Baer-Nunziato N <= 3: 3, 168 registers, 16 bytes spilled
+  // at N = 2, 3; N = 4: 2; N = 5: 1), so that the CTAs' phases without FP64
+  // work (gather loads, barriers) overlap other CTAs' arithmetic.
+  static constexpr int MIN_BLOCKS = sizeof(T) == 4 ? (Sys::ID == kSysBN ? (N == 3 ? 4 : N == 2 ? 5 : 1) : 6)
+                                                   : (Sys::ID == kSysBN ? (N <= 3 ? 3 : N == 4 ? 2 : 1) : 4);
   static constexpr int NE = (S + 1) * S;               // x edges (and y edges) of the subgrid
   static constexpr int NEF = (Sys::ID == kSysBN ? 4 : 2) * V * NE;  // edge fluxes (+ BN fluctuations)
-  // compute-type (T) elements: sub0 [V][R*R], slopes x/y/t and wLx wRx wLy wRy
-  // [7][V][H*H], edge fluxes, subuh1 [V][S*S], luhy [V][P][S], and the
-  // operators uh2lim [S*P], lim2uh [P*S] in T.  The gather stages the 3x3
+  // compute-type (T) elements: sub0 [V][R*R]; the reconstructed states wLx
+  // wRx wLy wRy [4][V][H*H] (Baer-Nunziato: then the half-step increment
+  // [V][H*H] and the volume-fraction slopes [2][H*H], which its finite-volume
+  // update reads; the other slopes live in registers); the edge fluxes; the
+  // operators uh2lim [S*P], lim2uh [P*S], uh2lob [P*P] in T.  Arrays whose
+  // lifetimes do not meet share room: the gather stages the 3x3
   // neighbourhood's uh [9][V][P2] and its y pass [9][V][P][S] in the room of
-  // the slopes, which are formed after it.
-  static constexpr int TSLOPE = 7 * V * H * H;
-  static_assert(9 * V * P2 + 9 * V * P * S <= TSLOPE, "gather staging room");
-  static constexpr int TEL = V * R * R + TSLOPE + NEF + V * S * S + V * S * P + 2 * S * P + P * P;
-  // FP32-mixed DMP of the new polynomial, in the room of the slopes: UN, LY, LB
-  static_assert(V * P2 + V * S * P + V * P * P <= TSLOPE, "FP32 DMP room");
+  // the states and edge fluxes, formed after it; subuh1 [V][S*S] takes wLx's
+  // room, luhy [V][P][S] wRx's and the FP32 DMP of the new polynomial (UN, LY,
+  // LB) wLy's, all after the edge fluxes.
+  static constexpr int TW = V * H * H;
+  static constexpr int TSTATE = 4 * TW + (Sys::ID == kSysBN ? TW + 2 * H * H : 0);
+  static_assert(9 * V * P2 + 9 * V * P * S <= TSTATE + NEF, "gather staging room");
+  static_assert(V * S * S <= TW && V * S * P <= TW, "subuh1 / luhy room");
+  static_assert(V * P2 + V * S * P + V * P * P <= 2 * TW, "FP32 DMP room");
+  static constexpr int TEL = V * R * R + TSTATE + NEF + 2 * S * P + P * P;
   static constexpr int TBYTES = ((TEL * (int)sizeof(T) + 15) / 16) * 16;
   // FP64 elements: new polynomial UN [V][P2], DMP y pass LY [V][S][P], LB
   // [V][P][P], reduction [2][V][warps], operators uh2lim, uh2lob (FP64)
@@ -104,6 +115,17 @@ template <class T>
 __device__ __forceinline__ T minmod(T a, T b) {
   if (a * b <= T(0)) return T(0);
   return (tabs(a) < tabs(b)) ? a : b;
+}
+// The same decisions on the FP64 bit patterns (integer pipe, not the FP64
+// pipe): 0 when the signs differ or either is 0, else the smaller magnitude
+// (magnitude bits order like the magnitudes).  It differs from minmod only
+// where a * b underflows to 0 for same-signed |a b| < 2^-1074 (the smaller
+// slope instead of 0).
+__device__ __forceinline__ double minmod_bits(double a, double b) {
+  const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+  const long long ma = ia & 0x7fffffffffffffffLL, mb = ib & 0x7fffffffffffffffLL;
+  if ((ia ^ ib) < 0 || ma == 0 || mb == 0) return 0.0;
+  return ma < mb ? a : b;
 }
 
 // Subgrid Rusanov flux (Euler/limiter.f90:361-378; BN :359-383 adds D = B~ dQ);
@@ -171,20 +193,19 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
   constexpr bool BN = Sys::ID == kSysBN;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sub0 = reinterpret_cast<T*>(smem_raw);
-  T* slx = sub0 + V * R * R;
-  T* sly = slx + V * H * H;
-  T* slt = sly + V * H * H;
-  T* wLx = slt + V * H * H;
-  T* wRx = wLx + V * H * H;
-  T* wLy = wRx + V * H * H;
-  T* wRy = wLy + V * H * H;
-  T* EF = slx + C::TSLOPE;           // x edges: F [V][NE] (BN: then D [V][NE]); then the y edges
-  T* sub1 = EF + C::NEF;
-  T* LUY = sub1 + V * S * S;         // [V][P][S]: luhy(v, iii, s) at (v*P + s)*S + iii
-  T* limT = LUY + V * S * P;         // uh2lim (s,k) at [s + S*k]
+  T* wLx = sub0 + V * R * R;
+  T* wRx = wLx + C::TW;
+  T* wLy = wRx + C::TW;
+  T* wRy = wLy + C::TW;
+  T* slt = wRy + C::TW;              // BN: half-step increment [V][H*H]
+  T* sa8 = slt + C::TW;              // BN: volume-fraction slopes x [H*H], y [H*H]
+  T* EF = wLx + C::TSTATE;           // x edges: F [V][NE] (BN: then D [V][NE]); then the y edges
+  T* limT = EF + C::NEF;             // uh2lim (s,k) at [s + S*k]
   T* l2uT = limT + S * P;            // lim2uh (k,s) at [k + P*s]
   T* lobT = l2uT + S * P;            // uh2lob (q,k) at [q + P*k]
-  T* NB = slx;                       // gather staging: [9][V][P2]
+  T* sub1 = wLx;                     // [V][S*S], after the edge fluxes
+  T* LUY = wRx;                      // [V][P][S]: luhy(v, iii, s) at (v*P + s)*S + iii
+  T* NB = wLx;                       // gather staging: [9][V][P2]
   T* LYN = NB + 9 * V * P2;          // [9][V][P][S]: sum_m uh(k, m) uh2lim(s, m) at ((n*V + v)*P + k)*S + s
   double* UN = reinterpret_cast<double*>(smem_raw + C::TBYTES);  // [V][P2]
   double* LY = UN + V * P2;          // DMP y pass [V][S][P]
@@ -197,7 +218,7 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
   long long* nbc = reinterpret_cast<long long*>(misc + 16);  // 3x3 neighbour cells, n = (bi+1) + 3 (bj+1)
   int* nbs = reinterpret_cast<int*>(misc + 16 + 9 * 8);     // their status (0: project olduh)
   unsigned* amax = reinterpret_cast<unsigned*>(nbs + 9);     // FP32-mixed: max |UN| per variable
-  float* UNf = reinterpret_cast<float*>(slx);                // FP32-mixed DMP (after the re-solve)
+  float* UNf = reinterpret_cast<float*>(wLy);                // FP32 DMP (after the re-solve)
   float* LYf = UNf + V * P2;
   float* LBf = LYf + V * S * P;
   float* redf = reinterpret_cast<float*>(red);              // [2][V][NW]
@@ -332,56 +353,65 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
     }
     __syncthreads();
 
-    // ---- MUSCL-Hancock reconstruction on subcells 0..S+1
+    // ---- MUSCL-Hancock reconstruction on subcells 0..S+1; the slopes of
+    // one direction at a time in registers
     for (int p = t; p < H * H; p += NT) {
       const int ii = p % H, jj = p / H;
-      T Qt[V], FLx[2 * V], FRx[2 * V], FLy[2 * V], FRy[2 * V];
+      T Qt[V], FL[2 * V], FR[2 * V];
       const bool interior = ii >= 1 && ii <= S && jj >= 1 && jj <= S;
       // Euler computes slopes for interior subcells only (halo slopes stay 0,
       // Euler/limiter.f90:529-536); BN also on the halo (BN :486-492)
-#pragma unroll
-      for (int v = 0; v < V; ++v) {
-        T sx = T(0), sy = T(0);
-        if (BN || interior) {
-          sx = minmod(SU(v, ii + 1, jj) - SU(v, ii, jj), SU(v, ii, jj) - SU(v, ii - 1, jj));
-          sy = minmod(SU(v, ii, jj + 1) - SU(v, ii, jj), SU(v, ii, jj) - SU(v, ii, jj - 1));
-        }
-        slx[hx(v, ii, jj)] = sx;
-        sly[hx(v, ii, jj)] = sy;
-      }
-      T q0[V], wl[V], wr[V];
+      // FP32-mixed (FP64 re-solve): minmod on the bit patterns
+      auto mm = [](T a, T b) -> T {
+        if constexpr (kRcp && sizeof(T) == 8) return minmod_bits(a, b);
+        else return minmod(a, b);
+      };
+      auto slope_x = [&](int v) -> T {
+        return (BN || interior) ? mm(SU(v, ii + 1, jj) - SU(v, ii, jj), SU(v, ii, jj) - SU(v, ii - 1, jj)) : T(0);
+      };
+      auto slope_y = [&](int v) -> T {
+        return (BN || interior) ? mm(SU(v, ii, jj + 1) - SU(v, ii, jj), SU(v, ii, jj) - SU(v, ii, jj - 1)) : T(0);
+      };
+      T q0[V], wl[V], wr[V], sl[V];
 #pragma unroll
       for (int v = 0; v < V; ++v) q0[v] = SU(v, ii, jj);
       T src[V];
       if constexpr (BN) {
         // Baer-Nunziato/limiter.f90:494-497
-        ncp(q0, divx(slx[hx(8, ii, jj)]), divy(sly[hx(8, ii, jj)]), src);
+        const T ax = slope_x(8), ay = slope_y(8);
+        sa8[p] = ax;
+        sa8[H * H + p] = ay;
+        ncp(q0, divx(ax), divy(ay), src);
       }
 #pragma unroll
-      for (int v = 0; v < V; ++v) {
-        wl[v] = q0[v] - T(0.5) * slx[hx(v, ii, jj)];
-        wr[v] = q0[v] + T(0.5) * slx[hx(v, ii, jj)];
-      }
-      flux(wl, 0, FLx);
-      flux(wr, 0, FRx);
+      for (int v = 0; v < V; ++v) sl[v] = slope_x(v);
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        if constexpr (BN) Qt[v] = src[v] - divx(FRx[v] - FLx[v]);
-        else Qt[v] = -divx(FRx[v] - FLx[v]);
+        wl[v] = q0[v] - T(0.5) * sl[v];
+        wr[v] = q0[v] + T(0.5) * sl[v];
+      }
+      flux(wl, 0, FL);
+      flux(wr, 0, FR);
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        if constexpr (BN) Qt[v] = src[v] - divx(FR[v] - FL[v]);
+        else Qt[v] = -divx(FR[v] - FL[v]);
         wLx[hx(v, ii, jj)] = wl[v];
         wRx[hx(v, ii, jj)] = wr[v];
       }
 #pragma unroll
-      for (int v = 0; v < V; ++v) {
-        wl[v] = q0[v] - T(0.5) * sly[hx(v, ii, jj)];
-        wr[v] = q0[v] + T(0.5) * sly[hx(v, ii, jj)];
-      }
-      flux(wl, 1, FLy);
-      flux(wr, 1, FRy);
+      for (int v = 0; v < V; ++v) sl[v] = slope_y(v);
 #pragma unroll
       for (int v = 0; v < V; ++v) {
-        Qt[v] = Qt[v] - divy(FRy[V + v] - FLy[V + v]);
-        slt[hx(v, ii, jj)] = Qt[v];
+        wl[v] = q0[v] - T(0.5) * sl[v];
+        wr[v] = q0[v] + T(0.5) * sl[v];
+      }
+      flux(wl, 1, FL);
+      flux(wr, 1, FR);
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        Qt[v] = Qt[v] - divy(FR[V + v] - FL[V + v]);
+        if constexpr (BN) slt[hx(v, ii, jj)] = Qt[v];
         wLx[hx(v, ii, jj)] = wLx[hx(v, ii, jj)] + T(0.5) * dt * Qt[v];
         wRx[hx(v, ii, jj)] = wRx[hx(v, ii, jj)] + T(0.5) * dt * Qt[v];
         wLy[hx(v, ii, jj)] = wl[v] + T(0.5) * dt * Qt[v];
@@ -432,7 +462,7 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
           T qh[V], src[V];
 #pragma unroll
           for (int v = 0; v < V; ++v) qh[v] = SU(v, ii, jj) + T(0.5) * dt * slt[hx(v, ii, jj)];
-          ncp(qh, divx(slx[hx(8, ii, jj)]), divy(sly[hx(8, ii, jj)]), src);
+          ncp(qh, divx(sa8[ii + H * jj]), divy(sa8[H * H + ii + H * jj]), src);
 #pragma unroll
           for (int v = 0; v < V; ++v)
             sub1[v * S * S + p] = SU(v, ii, jj) - divx(dt) * (EX[v * NE + xp] - EX[v * NE + xm]) -

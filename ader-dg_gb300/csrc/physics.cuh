@@ -101,7 +101,7 @@ struct EulerSys {
     }
     const T un = d == 0 ? u : v;
     const T c = tsqrt(pc.gamma * p * irho);
-    eig = tmax(tabs(un - c), tabs(un + c));
+    eig = tabs(un) + c;  // = max(|un - c|, |un + c|) exactly, c >= 0
   }
   template <class T>
   __device__ static void flux_r(const PhysC<T>& pc, const T* Q, T* F) {
@@ -127,7 +127,7 @@ struct EulerSys {
     F[2] = Q[2] * un + (d == 1 ? p : T(0));
     F[3] = un * (Q[3] + p);
     const T c = tsqrt(pc.gamma * p * irho);
-    eig = tmax(tabs(un - c), tabs(un + c));
+    eig = tabs(un) + c;  // = max(|un - c|, |un + c|) exactly, c >= 0
   }
   // Constants of the FP32-mixed cell kernel (CFL eigenvalues, admissibility pre-test).
   struct FConst {
@@ -414,7 +414,8 @@ struct BNSys {
     const T a_s = tsqrt(pc.gs * (pps + pc.ps * phi_s) * i0);
     const T a_g = tsqrt(pc.gg * (ppg + pc.pg * phi_g) * i4);
     const T us = d == 0 ? u_s : v_s, ug = d == 0 ? u_g : v_g;
-    eig = tmax(tmax(tabs(ug - a_g), tabs(ug + a_g)), tmax(tabs(us - a_s), tabs(us + a_s)));
+    // max(|u - a|, |u + a|) = |u| + a exactly for a >= 0 (a NaN propagates alike)
+    eig = tmax(tabs(ug) + a_g, tabs(us) + a_s);
   }
   template <class T>
   __device__ static void flux_r(const PhysC<T>& pc, const T* Q, T* F) {
@@ -449,7 +450,8 @@ struct BNSys {
     F[8] = T(0);
     const T a_s = tsqrt(pc.gs * (pps + pc.ps * phi_s) * i0);
     const T a_g = tsqrt(pc.gg * (ppg + pc.pg * phi_g) * i4);
-    eig = tmax(tmax(tabs(ug - a_g), tabs(ug + a_g)), tmax(tabs(us - a_s), tabs(us + a_s)));
+    // max(|u - a|, |u + a|) = |u| + a exactly for a >= 0 (a NaN propagates alike)
+    eig = tmax(tabs(ug) + a_g, tabs(us) + a_s);
   }
   // p_g = (gamma_g - 1) (Q7 Q4 - (Q5^2 + Q6^2) / 2) / (Q4 phi_g) - gamma_g pi_g
   // and u_n = qn / Q0 (qn = n . (Q1, Q2)) from one reciprocal of Q0 Q4 phi_g
