@@ -155,7 +155,8 @@ def load(build_if_missing=False):
         "aderdg_get_array": (i, [vp, i, vp]), "aderdg_get_info": (i, [vp, ctypes.POINTER(_Info)]),
         "aderdg_last_error": (ctypes.c_char_p, [vp]),
         "aderdg_project_initial_condition": (i, [cfgp, i, dp, dp, dp]),
-        "aderdg_probe_peaks": (i, [dp, dp]), "aderdg_set_array": (i, [vp, i, vp]),
+        "aderdg_probe_peaks": (i, [dp, dp]), "aderdg_probe_math": (i, [i, dp, dp]),
+        "aderdg_set_array": (i, [vp, i, vp]),
         "aderdg_host_alloc": (i, [ctypes.c_size_t, ctypes.POINTER(vp)]), "aderdg_host_free": (i, [vp]),
         "aderdg_operator": (i, [i, i, dp]), "aderdg_step_host": (i, [vp, dp, dp, d, dp, ip]),
         "aderdg_time_steps": (i, [vp, dp, d, i, i, dp]), "aderdg_profile_step": (i, [vp, dp, d, dp]),
@@ -242,7 +243,8 @@ EXPORTED = ("aderdg_create", "aderdg_destroy", "aderdg_upload", "aderdg_init_lim
             "aderdg_batch_download", "aderdg_batch_download_status", "aderdg_batch_counters", "aderdg_batch_info", "aderdg_batch_last_error", "aderdg_batch_profile",
             "aderdg_batch_run_timed", "aderdg_initial_condition", "aderdg_batch_admit_ic",
             "aderdg_cell_averages", "aderdg_batch_cell_averages", "aderdg_error_norms", "aderdg_host_alloc",
-            "aderdg_host_free", "aderdg_set_tuning", "aderdg_get_tuning", "aderdg_tuning_variants")
+            "aderdg_host_free", "aderdg_set_tuning", "aderdg_get_tuning", "aderdg_tuning_variants",
+            "aderdg_probe_math")
 
 
 def _dp(a):
@@ -310,6 +312,18 @@ def probe_peaks():
     if r:
         raise AderdgError(r, "probe failed")
     return a.value, b.value
+
+
+def probe_math(x):
+    """The FP32-mixed mode's FP64 reciprocal and square root on the device
+    beside the correctly rounded ones: array [n, 4] = (rcp, 1/x, sqrt, sqrt(x))."""
+    L = load()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty((x.size, 4), dtype=np.float64)
+    r = L.aderdg_probe_math(int(x.size), _dp(x), _dp(out))
+    if r:
+        raise AderdgError(r, "probe failed")
+    return out
 
 
 class Solver:

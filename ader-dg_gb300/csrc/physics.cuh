@@ -41,6 +41,45 @@ template <class T> __device__ __forceinline__ T tmin(T a, T b) {
 template <class T> __device__ __forceinline__ T tsqrt(T x) {
   if constexpr (sizeof(T) == 4) return sqrtf(x); else return sqrt(x);
 }
+// Reciprocal and square root of the FP32-mixed mode's FP64 arithmetic (the
+// reciprocal-sharing physics *_r; the FP64 mode keeps the correctly rounded
+// operations and the reference's divisions).  The hardware's approximations
+// (rcp.approx.ftz.f64, rsqrt.approx.ftz.f64) are refined by one third-order
+// Newton step, derived from the series of the exact quotients:
+//   1/x:     e = 1 - x r0,        1/x     = r0 / (1 - e)    ~ r0 (1 + e + e^2)
+//   sqrt(a): s0 = a y0, h = 1 - s0 y0, sqrt(a) = s0 (1 - h)^(-1/2) ~ s0 (1 + h/2 + 3 h^2 / 8)
+// (the neglected terms are e^3 and 5 h^3 / 16 relative).  Within 2 ulp of the
+// correctly rounded results for normal finite inputs (checked against them on
+// the device by aderdg_probe_math); zeros, denormals, infinities and NaNs (the
+// exponent field all zeros or all ones, an integer test) take the correctly
+// rounded operation.  FP32: the correctly rounded operations.
+__device__ __forceinline__ bool m_special(double x) {
+  const unsigned long long ex = (unsigned long long)__double_as_longlong(x) & 0x7ff0000000000000ull;
+  return ex == 0ull || ex == 0x7ff0000000000000ull;
+}
+template <class T> __device__ __forceinline__ T mrcp(T x) {
+  if constexpr (sizeof(T) == 4) {
+    return T(1) / x;
+  } else {
+    if (m_special(x)) return 1.0 / x;
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    const double e = fma(-x, r, 1.0);
+    return fma(fma(e, e, e), r, r);
+  }
+}
+template <class T> __device__ __forceinline__ T msqrt(T a) {
+  if constexpr (sizeof(T) == 4) {
+    return sqrtf(a);
+  } else {
+    if (m_special(a) || __double_as_longlong(a) < 0) return sqrt(a);
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(a));
+    const double s = a * y;
+    const double h = fma(-s, y, 1.0);
+    return fma(s * h, fma(h, 0.375, 0.5), s);
+  }
+}
 
 // ---------------------------------------------------------------------------
 struct EulerSys {
@@ -86,7 +125,7 @@ struct EulerSys {
   // multiply-adds; its values agree with the reference order to rounding).
   template <class T>
   __device__ static void flux_eig_r(const PhysC<T>& pc, const T* Q, int d, T* F, T& eig) {
-    const T irho = T(1) / Q[0];
+    const T irho = mrcp<T>(Q[0]);
     const T u = Q[1] * irho, v = Q[2] * irho;
     const T p = pc.gm1 * (Q[3] - T(0.5) * (Q[1] * u + Q[2] * v));
     if (F) {
@@ -100,7 +139,7 @@ struct EulerSys {
       F[7] = v * (Q[3] + p);
     }
     const T un = d == 0 ? u : v;
-    const T c = tsqrt(pc.gamma * p * irho);
+    const T c = msqrt<T>(pc.gamma * p * irho);
     eig = tabs(un) + c;  // = max(|un - c|, |un + c|) exactly, c >= 0
   }
   template <class T>
@@ -118,7 +157,7 @@ struct EulerSys {
   // flux_eig_r; Q1 v = Q2 u), and maxval(abs(Lambda)) along d
   template <class T>
   __device__ static void flux_dir_eig_r(const PhysC<T>& pc, const T* Q, int d, T* F, T& eig) {
-    const T irho = T(1) / Q[0];
+    const T irho = mrcp<T>(Q[0]);
     const T u = Q[1] * irho, v = Q[2] * irho;
     const T p = pc.gm1 * (Q[3] - T(0.5) * (Q[1] * u + Q[2] * v));
     const T un = d == 0 ? u : v;
@@ -126,7 +165,7 @@ struct EulerSys {
     F[1] = Q[1] * un + (d == 0 ? p : T(0));
     F[2] = Q[2] * un + (d == 1 ? p : T(0));
     F[3] = un * (Q[3] + p);
-    const T c = tsqrt(pc.gamma * p * irho);
+    const T c = msqrt<T>(pc.gamma * p * irho);
     eig = tabs(un) + c;  // = max(|un - c|, |un + c|) exactly, c >= 0
   }
   // Constants of the FP32-mixed cell kernel (CFL eigenvalues, admissibility pre-test).
@@ -399,7 +438,7 @@ struct BNSys {
   // Flux F[d*V + v] (pde.f90:74-119) and maxval(abs(Lambda)) along axis d (:125-144).
   template <class T>
   __device__ static void flux_eig_r(const PhysC<T>& pc, const T* Q, int d, T* F, T& eig) {
-    const T r = T(1) / (Q[0] * Q[4]);
+    const T r = mrcp<T>(Q[0] * Q[4]);
     const T i0 = Q[4] * r, i4 = Q[0] * r;
     const T u_s = Q[1] * i0, v_s = Q[2] * i0, u_g = Q[5] * i4, v_g = Q[6] * i4;
     const T phi_s = Q[8], phi_g = T(1) - Q[8];
@@ -411,8 +450,8 @@ struct BNSys {
       F[9] = Q[2]; F[10] = Q[2] * u_s; F[11] = Q[2] * v_s + pps; F[12] = v_s * (Q[3] + pps);
       F[13] = Q[6]; F[14] = Q[6] * u_g; F[15] = Q[6] * v_g + ppg; F[16] = v_g * (Q[7] + ppg); F[17] = T(0);
     }
-    const T a_s = tsqrt(pc.gs * (pps + pc.ps * phi_s) * i0);
-    const T a_g = tsqrt(pc.gg * (ppg + pc.pg * phi_g) * i4);
+    const T a_s = msqrt<T>(pc.gs * (pps + pc.ps * phi_s) * i0);
+    const T a_g = msqrt<T>(pc.gg * (ppg + pc.pg * phi_g) * i4);
     const T us = d == 0 ? u_s : v_s, ug = d == 0 ? u_g : v_g;
     // max(|u - a|, |u + a|) = |u| + a exactly for a >= 0 (a NaN propagates alike)
     eig = tmax(tabs(ug) + a_g, tabs(us) + a_s);
@@ -432,7 +471,7 @@ struct BNSys {
   // = Q2 u_s), and maxval(abs(Lambda)) along d
   template <class T>
   __device__ static void flux_dir_eig_r(const PhysC<T>& pc, const T* Q, int d, T* F, T& eig) {
-    const T r = T(1) / (Q[0] * Q[4]);
+    const T r = mrcp<T>(Q[0] * Q[4]);
     const T i0 = Q[4] * r, i4 = Q[0] * r;
     const T u_s = Q[1] * i0, v_s = Q[2] * i0, u_g = Q[5] * i4, v_g = Q[6] * i4;
     const T phi_s = Q[8], phi_g = T(1) - Q[8];
@@ -448,8 +487,8 @@ struct BNSys {
     F[6] = Q[6] * ug + (d == 1 ? ppg : T(0));
     F[7] = ug * (Q[7] + ppg);
     F[8] = T(0);
-    const T a_s = tsqrt(pc.gs * (pps + pc.ps * phi_s) * i0);
-    const T a_g = tsqrt(pc.gg * (ppg + pc.pg * phi_g) * i4);
+    const T a_s = msqrt<T>(pc.gs * (pps + pc.ps * phi_s) * i0);
+    const T a_g = msqrt<T>(pc.gg * (ppg + pc.pg * phi_g) * i4);
     // max(|u - a|, |u + a|) = |u| + a exactly for a >= 0 (a NaN propagates alike)
     eig = tmax(tabs(ug) + a_g, tabs(us) + a_s);
   }
@@ -458,7 +497,7 @@ struct BNSys {
   template <class T>
   __device__ static void p_gas_un_r(const PhysC<T>& pc, const T* Q, T qn, T& p_g, T& un) {
     const T b = Q[4] * (T(1) - Q[8]);
-    const T r = T(1) / (b * Q[0]);
+    const T r = mrcp<T>(b * Q[0]);
     p_g = pc.gg1 * (Q[7] * Q[4] - T(0.5) * (Q[5] * Q[5] + Q[6] * Q[6])) * (Q[0] * r) - pc.ggpg;
     un = qn * (b * r);
   }

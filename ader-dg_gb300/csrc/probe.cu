@@ -6,8 +6,21 @@
 #include <cuda_runtime.h>
 
 #include "../../include/aderdg_gpu.h"
+#include "physics.cuh"
 
 namespace {
+
+// the FP32-mixed mode's refined reciprocal and square root beside the
+// correctly rounded operations, for the accuracy check (aderdg_probe_math)
+__global__ void k_math(int n, const double* x, double* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = x[i];
+  out[4 * (size_t)i + 0] = aderdg::mrcp<double>(v);
+  out[4 * (size_t)i + 1] = 1.0 / v;
+  out[4 * (size_t)i + 2] = aderdg::msqrt<double>(v);
+  out[4 * (size_t)i + 3] = sqrt(v);
+}
 
 template <class R>
 __global__ void __launch_bounds__(256) k_fma_chain(R* out, int iters, R seed) {
@@ -77,4 +90,26 @@ extern "C" int aderdg_host_alloc(size_t bytes, void** ptr) {
 extern "C" int aderdg_host_free(void* ptr) {
   if (!ptr) return ADERDG_OK;
   return cudaFreeHost(ptr) == cudaSuccess ? ADERDG_OK : ADERDG_ECUDA;
+}
+
+extern "C" int aderdg_probe_math(int n, const double* x, double* out) {
+  if (n < 0 || (n > 0 && (!x || !out))) return ADERDG_EINVAL;
+  if (n == 0) return ADERDG_OK;
+  double *dx = nullptr, *dout = nullptr;
+  if (cudaMalloc(&dx, sizeof(double) * n) != cudaSuccess) return ADERDG_ENOMEM;
+  if (cudaMalloc(&dout, sizeof(double) * 4 * (size_t)n) != cudaSuccess) {
+    cudaFree(dx);
+    return ADERDG_ENOMEM;
+  }
+  int r = ADERDG_OK;
+  if (cudaMemcpy(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice) != cudaSuccess) r = ADERDG_ECUDA;
+  if (!r) {
+    k_math<<<(n + 255) / 256, 256>>>(n, dx, dout);
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpy(out, dout, sizeof(double) * 4 * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess)
+      r = ADERDG_ECUDA;
+  }
+  cudaFree(dx);
+  cudaFree(dout);
+  return r;
 }

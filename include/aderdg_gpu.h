@@ -376,6 +376,12 @@ int aderdg_tuning_variants(int* n_predictor, int* n_cells);
 /* Measured device peaks for roofline reporting: FP64 and FP32 FMA throughput
  * (GFLOP/s) from dependent-FMA microkernels on the current device. */
 int aderdg_probe_peaks(double* fp64_gflops, double* fp32_gflops);
+/* Accuracy check of the FP32-mixed mode's FP64 reciprocal and square root
+ * (Newton-refined hardware approximations): for each of the n inputs x[i],
+ * out[4i..4i+3] = refined 1/x, correctly rounded 1/x, refined sqrt(x),
+ * correctly rounded sqrt(x), evaluated on the current device.  No reference
+ * counterpart. */
+int aderdg_probe_math(int n, const double* x, double* out);
 
 /* Page-locked host memory for the host side of uploads and downloads
  * (aderdg_upload / aderdg_download / aderdg_batch_download and friends copy

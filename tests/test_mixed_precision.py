@@ -154,3 +154,35 @@ def test_initial_limiter_near_thresholds(gpu_lib):
     assert res[aderdg.FP32_MIXED] == (n_o, 0), res
     print("initial limiter near thresholds: oracle %d cells, FP32-wide mode %d cells (%d differ)"
           % (n_o, res[aderdg.FP32_WIDE][0], res[aderdg.FP32_WIDE][1]))
+
+
+def test_refined_reciprocal_and_sqrt_within_2ulp(gpu_lib):
+    """The FP32-mixed mode's FP64 reciprocal and square root (hardware
+    approximations refined by a third-order Newton step, physics.cuh mrcp /
+    msqrt) against the correctly rounded operations on the same device:
+    within 2 ulp on normal inputs over the whole exponent range, and the
+    correctly rounded result on zeros, denormals, infinities and NaNs."""
+    rng = np.random.default_rng(7)
+    e = rng.uniform(-1000, 1000, 200000)
+    x = np.concatenate([np.ldexp(rng.uniform(1.0, 2.0, e.size), e.astype(int)),
+                        rng.uniform(1e-3, 1e3, 100000),
+                        -rng.uniform(1e-3, 1e3, 1000)])
+    x = x[np.isfinite(x) & (np.abs(x) >= np.finfo(np.float64).tiny)]
+    out = aderdg.core.probe_math(x)
+
+    def ulps(a, b):
+        ia, ib = a.view(np.int64), b.view(np.int64)
+        return np.abs(ia - ib)
+
+    d_rcp = ulps(out[:, 0], out[:, 1])
+    pos = x > 0
+    d_sqrt = ulps(out[pos, 2], out[pos, 3])
+    print("refined rcp: max %d ulp (%.1f%% exact); sqrt: max %d ulp (%.1f%% exact)"
+          % (d_rcp.max(), 100 * np.mean(d_rcp == 0), d_sqrt.max(), 100 * np.mean(d_sqrt == 0)))
+    assert d_rcp.max() <= 2 and d_sqrt.max() <= 2
+    assert np.all(np.isnan(out[~pos, 2]))
+    special = np.array([0.0, -0.0, 5e-324, 1e-310, -1e-310, np.inf, -np.inf, np.nan])
+    o = aderdg.core.probe_math(special)
+    for k in (0, 2):
+        a, b = o[:, k], o[:, k + 1]
+        assert np.array_equal(np.isnan(a), np.isnan(b)) and np.array_equal(a[~np.isnan(a)], b[~np.isnan(b)]), (k, o)
