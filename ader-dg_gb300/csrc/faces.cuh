@@ -48,8 +48,8 @@ __device__ __forceinline__ void load_face_state(const R* qb, const R* fb, long l
   const size_t o = (((size_t)cell * 4 + f) * P + l) * V;  // [cell][face][point][v]
 #pragma unroll
   for (int v = 0; v < V; ++v) {
-    Q[v] = (T)qb[o + v];
-    if (F) F[v] = (T)fb[o + v];
+    Q[v] = widen<T>(qb[o + v]);
+    if (F) F[v] = widen<T>(fb[o + v]);
   }
 }
 

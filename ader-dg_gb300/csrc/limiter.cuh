@@ -294,20 +294,32 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
       if (nbs[n] == 0) NB[(n * V + v) * P2 + node] = (T)a.uh[par][(size_t)nbc[n] * P2 * V + r];
     }
     __syncthreads();
-    for (int p = t; p < 9 * V * P * S; p += NT) {
-      const int n = p / (V * P * S);
+    // the items actually read, enumerated densely (no idle lanes): all S
+    // rows of the neighbours beside the cell (n = 3, 4, 5), and the two rows
+    // nearest to the cell of those below (n = 0, 1, 2: subcell rows S-2, S-1)
+    // and above (n = 6, 7, 8: rows 0, 1); LYN keeps the full [9][V][P][S] index
+    constexpr int NMID = 3 * V * P * S, NROW = 2 * V * P;
+    for (int q = t; q < NMID + 6 * NROW; q += NT) {
+      int n, v, kk, sb;
+      if (q < NMID) {
+        n = 3 + q / (V * P * S);
+        const int r = q % (V * P * S);
+        v = r / (P * S);
+        kk = (r / S) % P;
+        sb = r % S;
+      } else {
+        const int q2 = q - NMID, n6 = q2 / NROW, r2 = q2 % NROW;
+        n = n6 < 3 ? n6 : n6 + 3;
+        v = r2 / (2 * P);
+        kk = (r2 >> 1) % P;
+        sb = (n < 3 ? S - 2 : 0) + (r2 & 1);
+      }
       if (nbs[n] != 0) continue;
-      const int r = p - n * (V * P * S);
-      const int v = r / (P * S), kk = (r / S) % P, sb = r % S;
-      // the neighbours below / above contribute their two rows nearest to
-      // the cell only (subcell rows S-2, S-1 / 0, 1)
-      const int bj = n / 3 - 1;
-      if ((bj < 0 && sb < S - 2) || (bj > 0 && sb > 1)) continue;
       const T* u = NB + (n * V + v) * P2;
       T ly = T(0);
 #pragma unroll
       for (int m = 0; m < P; ++m) ly = ly + u[kk + P * m] * limT[sb + S * m];
-      LYN[p] = ly;
+      LYN[((n * V + v) * P + kk) * S + sb] = ly;
     }
     __syncthreads();
     for (int p = t; p < R * R; p += NT) {

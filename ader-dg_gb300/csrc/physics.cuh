@@ -53,6 +53,23 @@ template <class T> __device__ __forceinline__ T tsqrt(T x) {
 // the device by aderdg_probe_math); zeros, denormals, infinities and NaNs (the
 // exponent field all zeros or all ones, an integer test) take the correctly
 // rounded operation.  FP32: the correctly rounded operations.
+// FP32 -> FP64, exact, on the integer pipe (sign, exponent rebias, mantissa
+// shift) for zeros and normal values; infinities, NaNs and denormals take the
+// hardware conversion.  The FP64-bound kernels of the FP32-mixed mode read
+// FP32 inputs (the Baer-Nunziato face states): their conversions then leave
+// the FP64 pipe.
+__device__ __forceinline__ double widen_bits(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  if (e == 0xffu || (e == 0u && m != 0u)) return (double)f;
+  unsigned long long d = (unsigned long long)(u & 0x80000000u) << 32;
+  if (e) d |= ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29);
+  return __longlong_as_double((long long)d);
+}
+template <class T, class R> __device__ __forceinline__ T widen(R x) {
+  if constexpr (sizeof(T) == 8 && sizeof(R) == 4) return widen_bits(x);
+  else return (T)x;
+}
 __device__ __forceinline__ bool m_special(double x) {
   const unsigned long long ex = (unsigned long long)__double_as_longlong(x) & 0x7ff0000000000000ull;
   return ex == 0ull || ex == 0x7ff0000000000000ull;
