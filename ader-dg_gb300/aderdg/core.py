@@ -315,12 +315,11 @@ def probe_peaks():
 
 
 def probe_math(x):
-    """The FP32-mixed mode's FP64 reciprocal, square root and FP64 -> FP32
-    rounding on the device beside the hardware's: array [n, 6] = (rcp, 1/x,
-    sqrt, sqrt(x), narrowed x, (float)x)."""
+    """The FP32-mixed mode's FP64 reciprocal and square root on the device
+    beside the correctly rounded ones: array [n, 4] = (rcp, 1/x, sqrt, sqrt(x))."""
     L = load()
     x = np.ascontiguousarray(x, dtype=np.float64)
-    out = np.empty((x.size, 6), dtype=np.float64)
+    out = np.empty((x.size, 4), dtype=np.float64)
     r = L.aderdg_probe_math(int(x.size), _dp(x), _dp(out))
     if r:
         raise AderdgError(r, "probe failed")

@@ -226,7 +226,7 @@ __device__ __forceinline__ double cfl_denom_f32(const InstDesc& in, const typena
     return cfl_denom<Sys, N>(in, nullptr);
   } else {
     float ex, ey;
-    if (Sys::max_eig2_f32(fc, q, ex, ey)) return widen_bits(ex * in.idxf + ey * in.idyf);
+    if (Sys::max_eig2_f32(fc, q, ex, ey)) return (double)(ex * in.idxf + ey * in.idyf);
     return cfl_denom<Sys, N>(in, Qd);
   }
 }
@@ -431,7 +431,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N, VAR>::THREADS, CellCfg<Sys, N,
           const float iw = op.iwwf[i + P * j];
 #pragma unroll
           for (int v = 0; v < V; ++v) {
-            u[v] = fma(dt, widen_bits(d[v] * iw), uo[v]);  // the exact FP32 -> FP64 conversion on the integer pipe
+            u[v] = fma(dt, (double)(d[v] * iw), uo[v]);
             un[v] = u[v];
           }
         }

@@ -318,8 +318,8 @@ __global__ void __launch_bounds__(256) k_faces(BatchArgs a, FaceConst fc) {
 #pragma unroll
       for (int v = 0; v < V; ++v) {
         const CT base = CT(0.5) * (FL[v] + FR[v]) - CT(0.5) * smax * (QR[v] - QL[v]);
-        dm[out + v] = narrow<R>(base - CT(0.5) * D[v]);
-        dp[out + v] = narrow<R>(base + CT(0.5) * D[v]);
+        dm[out + v] = (R)(base - CT(0.5) * D[v]);
+        dp[out + v] = (R)(base + CT(0.5) * D[v]);
       }
     } else {
       R* dst = reinterpret_cast<R*>(xdir ? a.fu : a.gu);

@@ -366,11 +366,38 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
     __syncthreads();
 
     // ---- MUSCL-Hancock reconstruction on subcells 0..S+1; the slopes of
-    // one direction at a time in registers
+    // one direction at a time in registers.  The S*S interior subcells come
+    // first, then the ring of halo subcells, so that the interior ones fill
+    // whole warps: Euler's halo subcells have zero slopes (Euler/limiter.f90:
+    // 529-536), so their two face states per direction are the subcell value,
+    // the half-step flux differences vanish exactly and their evolved face
+    // states are the subcell value itself; they are copied, and only the
+    // warps holding interior subcells evaluate fluxes.
     for (int p = t; p < H * H; p += NT) {
-      const int ii = p % H, jj = p / H;
+      int ii, jj;
+      if (p < S * S) {
+        ii = 1 + p % S;
+        jj = 1 + p / S;
+      } else {
+        const int r = p - S * S;  // the ring: bottom row, top row, left column, right column
+        if (r < H) { ii = r; jj = 0; }
+        else if (r < 2 * H) { ii = r - H; jj = H - 1; }
+        else if (r < 2 * H + S) { ii = 0; jj = 1 + (r - 2 * H); }
+        else { ii = H - 1; jj = 1 + (r - 2 * H - S); }
+      }
+      const bool interior = p < S * S;
+      if (!BN && !interior) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+          const T q = SU(v, ii, jj);
+          wLx[hx(v, ii, jj)] = q;
+          wRx[hx(v, ii, jj)] = q;
+          wLy[hx(v, ii, jj)] = q;
+          wRy[hx(v, ii, jj)] = q;
+        }
+        continue;
+      }
       T Qt[V], FL[2 * V], FR[2 * V];
-      const bool interior = ii >= 1 && ii <= S && jj >= 1 && jj <= S;
       // Euler computes slopes for interior subcells only (halo slopes stay 0,
       // Euler/limiter.f90:529-536); BN also on the halo (BN :486-492)
       // FP32-mixed (FP64 re-solve): minmod on the bit patterns

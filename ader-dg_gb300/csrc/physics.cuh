@@ -70,27 +70,6 @@ template <class T, class R> __device__ __forceinline__ T widen(R x) {
   if constexpr (sizeof(T) == 8 && sizeof(R) == 4) return widen_bits(x);
   else return (T)x;
 }
-// FP64 -> FP32 rounded to nearest even, on the integer pipe, for zeros and
-// values whose FP32 result is normal or overflows to infinity by rounding
-// (the 23 leading mantissa bits, rounded on the 29 others; a carry moves into
-// the exponent as the rounding prescribes); everything else (FP32 denormal
-// results, larger exponents, infinities, NaNs) takes the hardware conversion.
-// Bit-identical to the hardware conversion (checked by aderdg_probe_math).
-__device__ __forceinline__ float narrow_bits(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned hw = (unsigned)(b >> 32);
-  const unsigned sign = hw & 0x80000000u, e = (hw >> 20) & 0x7ffu;
-  if (e == 0u && (b << 1) == 0ull) return __uint_as_float(sign);
-  if (e < 897u || e > 1150u) return (float)x;
-  const unsigned hi = (unsigned)((b >> 29) & 0x7fffffull), lo = (unsigned)(b & 0x1fffffffull);
-  unsigned f = sign | ((e - 896u) << 23) | hi;
-  if (lo > 0x10000000u || (lo == 0x10000000u && (hi & 1u))) f += 1u;
-  return __uint_as_float(f);
-}
-template <class R, class T> __device__ __forceinline__ R narrow(T x) {
-  if constexpr (sizeof(T) == 8 && sizeof(R) == 4) return narrow_bits(x);
-  else return (R)x;
-}
 __device__ __forceinline__ bool m_special(double x) {
   const unsigned long long ex = (unsigned long long)__double_as_longlong(x) & 0x7ff0000000000000ull;
   return ex == 0ull || ex == 0x7ff0000000000000ull;

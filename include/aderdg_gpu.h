@@ -377,11 +377,10 @@ int aderdg_tuning_variants(int* n_predictor, int* n_cells);
  * (GFLOP/s) from dependent-FMA microkernels on the current device. */
 int aderdg_probe_peaks(double* fp64_gflops, double* fp32_gflops);
 /* Accuracy check of the FP32-mixed mode's FP64 reciprocal and square root
- * (Newton-refined hardware approximations) and of its integer-pipe FP64 ->
- * FP32 rounding: for each of the n inputs x[i], out[6i..6i+5] = refined 1/x,
- * correctly rounded 1/x, refined sqrt(x), correctly rounded sqrt(x), the
- * integer rounding of x to FP32 and the hardware's (both widened back to
- * FP64), evaluated on the current device.  No reference counterpart. */
+ * (Newton-refined hardware approximations): for each of the n inputs x[i],
+ * out[4i..4i+3] = refined 1/x, correctly rounded 1/x, refined sqrt(x),
+ * correctly rounded sqrt(x), evaluated on the current device.  No reference
+ * counterpart. */
 int aderdg_probe_math(int n, const double* x, double* out);
 
 /* Page-locked host memory for the host side of uploads and downloads

@@ -161,9 +161,7 @@ def test_refined_reciprocal_and_sqrt_within_2ulp(gpu_lib):
     approximations refined by a third-order Newton step, physics.cuh mrcp /
     msqrt) against the correctly rounded operations on the same device:
     within 2 ulp on normal inputs over the whole exponent range, and the
-    correctly rounded result on zeros, denormals, infinities and NaNs.  The
-    integer-pipe FP64 -> FP32 rounding (narrow_bits) equals the hardware
-    conversion bit for bit, halfway cases and overflow included."""
+    correctly rounded result on zeros, denormals, infinities and NaNs."""
     rng = np.random.default_rng(7)
     e = rng.uniform(-1000, 1000, 200000)
     x = np.concatenate([np.ldexp(rng.uniform(1.0, 2.0, e.size), e.astype(int)),
@@ -183,16 +181,8 @@ def test_refined_reciprocal_and_sqrt_within_2ulp(gpu_lib):
           % (d_rcp.max(), 100 * np.mean(d_rcp == 0), d_sqrt.max(), 100 * np.mean(d_sqrt == 0)))
     assert d_rcp.max() <= 2 and d_sqrt.max() <= 2
     assert np.all(np.isnan(out[~pos, 2]))
-    special = np.array([0.0, -0.0, 5e-324, 1e-310, -1e-310, np.inf, -np.inf, np.nan, 3.4028235677973366e38,
-                        3.4028236e38, 1.1754943508222875e-38, 1.1754942e-38, 2.0 ** -140, 1e300, -1e-300])
+    special = np.array([0.0, -0.0, 5e-324, 1e-310, -1e-310, np.inf, -np.inf, np.nan])
     o = aderdg.core.probe_math(special)
-    for k in (0, 2, 4):
+    for k in (0, 2):
         a, b = o[:, k], o[:, k + 1]
         assert np.array_equal(np.isnan(a), np.isnan(b)) and np.array_equal(a[~np.isnan(a)], b[~np.isnan(b)]), (k, o)
-    # FP64 -> FP32: random magnitudes over the FP32 range and beyond, and exact halfway cases
-    m = rng.integers(0, 2 ** 23, 50000)
-    ex = rng.integers(-140, 140, 50000)
-    half = (1.0 + (2 * m + 1) / 2.0 ** 24) * np.ldexp(1.0, ex)
-    y = np.concatenate([rng.standard_normal(200000) * 10.0 ** rng.uniform(-46, 40, 200000), half, -half])
-    o = aderdg.core.probe_math(y)
-    assert np.array_equal(o[:, 4].view(np.int64), o[:, 5].view(np.int64))
