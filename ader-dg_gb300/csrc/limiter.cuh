@@ -418,8 +418,8 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
       if constexpr (BN) {
         // Baer-Nunziato/limiter.f90:494-497
         const T ax = slope_x(8), ay = slope_y(8);
-        sa8[p] = ax;
-        sa8[H * H + p] = ay;
+        sa8[ii + H * jj] = ax;
+        sa8[H * H + ii + H * jj] = ay;
         ncp(q0, divx(ax), divy(ay), src);
       }
 #pragma unroll
