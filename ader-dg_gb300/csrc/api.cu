@@ -238,6 +238,16 @@ InstDesc make_inst_desc(const aderdg_config* cfg) {
   in.ph.cy = cfg->cy;
   in.ph.a = cfg->a;
   in.ph.ad_fused = cfg->ad_flux_mode;
+  for (int k = 0; k < 8; ++k) in.ph.f32c[k] = 0.0f;
+  if (cfg->system == ADERDG_SYS_EULER) {
+    in.ph.f32c[0] = (float)(cfg->gamma - 1.0);
+    in.ph.f32c[1] = (float)cfg->gamma;
+  } else if (cfg->system == ADERDG_SYS_BN) {
+    const double gs = cfg->gamma_s, gg = cfg->gamma_g, ps = cfg->pi_s, pg = cfg->pi_g;
+    const float c[8] = {(float)gs, (float)gg, (float)(gs - 1.0), (float)(gg - 1.0), (float)(gs * ps), (float)(gg * pg),
+                        (float)ps, (float)pg};
+    for (int k = 0; k < 8; ++k) in.ph.f32c[k] = c[k];
+  }
   if (cfg->system == ADERDG_SYS_ADVDIFF) {
     // the expressions of the face kernel and of calc_time_step, evaluated once
     const double pi = 4.0 * std::atan(1.0);

@@ -31,6 +31,10 @@ struct Phys {
   double gs, gg, ps, pg;       // Baer-Nunziato
   double cx, cy, a;            // advection-diffusion
   int ad_fused;                // 1: convective + viscous flux in the AD predictor
+  // the FP32-mixed mode's FP32 constants (Sys::FConst), rounded once on the
+  // host: Euler (gamma - 1, gamma); Baer-Nunziato (gs, gg, gs - 1, gg - 1,
+  // gs ps, gg pg, ps, pg)
+  float f32c[8];
 };
 
 // Read-only description of one instance.

@@ -188,7 +188,7 @@ struct EulerSys {
   // Constants of the FP32-mixed cell kernel (CFL eigenvalues, admissibility pre-test).
   struct FConst {
     float gm1, gamma;
-    __device__ explicit FConst(const Phys& ph) : gm1((float)(ph.gamma - 1.0)), gamma((float)ph.gamma) {}
+    __device__ explicit FConst(const Phys& ph) : gm1(ph.f32c[0]), gamma(ph.f32c[1]) {}
   };
   // FP32 eigenvalues for the mixed-precision CFL
   // False when the FP32 pressure is not settled (within 1e-4 of the energy
@@ -358,8 +358,8 @@ struct BNSys {
   struct FConst {
     float gs, gg, gs1, gg1, gsps, ggpg, ps, pg;
     __device__ explicit FConst(const Phys& ph)
-        : gs((float)ph.gs), gg((float)ph.gg), gs1((float)(ph.gs - 1.0)), gg1((float)(ph.gg - 1.0)),
-          gsps((float)(ph.gs * ph.ps)), ggpg((float)(ph.gg * ph.pg)), ps((float)ph.ps), pg((float)ph.pg) {}
+        : gs(ph.f32c[0]), gg(ph.f32c[1]), gs1(ph.f32c[2]), gg1(ph.f32c[3]), gsps(ph.f32c[4]), ggpg(ph.f32c[5]),
+          ps(ph.f32c[6]), pg(ph.f32c[7]) {}
   };
   // False when an FP32 pressure p + pi is not settled (within 1e-4 of the
   // terms it cancels, or not positive) or a fraction is out of (0.01, 0.99):
