@@ -636,6 +636,7 @@ __global__ void __launch_bounds__(CellCfg<Sys, N, VAR>::THREADS, CellCfg<Sys, N,
     if (act && node < V) {
       const int v = node;
       double cmn, cmx;
+      const double ubar = kFast ? (double)ubs[v] : 0.0;  // the cell's FP32 reference state (FP32-mixed)
       // FP32 projections: the cell's deviation min/max from its FP32 reference
       // state ubar, and a bound on |ubar + fmn - FP64 value| (and fmx): the
       // projections' bound as formed above (rounded up), plus the FP64
@@ -646,7 +647,6 @@ __global__ void __launch_bounds__(CellCfg<Sys, N, VAR>::THREADS, CellCfg<Sys, N,
         fmx = REDf[(V + v) * P2];
 #pragma unroll
         for (int k = 1; k < P2; ++k) { fmn = fminf(fmn, REDf[v * P2 + k]); fmx = fmaxf(fmx, REDf[(V + v) * P2 + k]); }
-        const double ubar = (double)ubs[v];
         cmn = ubar + (double)fmn;
         cmx = ubar + (double)fmx;
         const float am = __uint_as_float(amax[v]);
@@ -701,9 +701,9 @@ __global__ void __launch_bounds__(CellCfg<Sys, N, VAR>::THREADS, CellCfg<Sys, N,
           // from their FP64 values by less than 1e-11 and 1e-8 of themselves.
           // A comparison decides here only when it holds by that margin;
           // otherwise k_settle decides the cell from FP64 values (bit 4).
-          const double ub = (double)ubs[v];
+          const double ub = ubar;
           const float Lmin = (float)(lmin - ub), Lmax = (float)(lmax - ub);
-          const float ld = fmaxf(fmaxf(1.0e-4f, 1.0e-3f * (Lmax - Lmin)), (float)argmax);
+          const float ld = fmaxf(fmaxf(1.0e-4f, 1.0e-3f * (Lmax - Lmin)), mode == kCellInitDmp ? 0.1f : 0.0f);
           const float dl = Lmin - ld, dh = Lmax + ld;
           const float xl = f32red ? fmn : (float)(cmn - ub), xh = f32red ? fmx : (float)(cmx - ub);
           const float e = ecell + 1.002f * en + 2.5e-7f * (fabsf(Lmin) + fabsf(Lmax) + ld) + 1.0e-11f +

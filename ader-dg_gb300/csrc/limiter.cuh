@@ -77,8 +77,9 @@ struct SubCfg {
   // CTAs per SM the register allocation aims at.  FP32: one more than the
   // unconstrained allocation allows where that does not spill.  FP64 (the
   // FP64 pipe bounds it): as many as shared memory admits, up to 4 (Euler:
-  // 128 registers; Baer-Nunziato N <= 3: 3, 168 registers, 16 bytes spilled
-  // at N = 2, 3; N = 4: 2; N = 5: 1), so that the CTAs' phases without FP64
+  // 128 registers; Baer-Nunziato N <= 3: 3 at 168 registers, where the FP64
+  // mode's reference-order variant spills about 140 bytes and the FP32-mixed
+  // one none; N = 4: 2; N = 5: 1), so that the CTAs' phases without FP64
   // work (gather loads, barriers) overlap other CTAs' arithmetic.
   static constexpr int MIN_BLOCKS = sizeof(T) == 4 ? (Sys::ID == kSysBN ? (N == 3 ? 4 : N == 2 ? 5 : 1) : 6)
                                                    : (Sys::ID == kSysBN ? (N <= 3 ? 3 : N == 4 ? 2 : 1) : 4);
