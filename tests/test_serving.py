@@ -37,9 +37,10 @@ def _alone(r, device_setup, steps):
     return ref, t
 
 
-@pytest.mark.parametrize("device_setup,precision", [(True, aderdg.FP64), (False, aderdg.FP64),
-                                                    (True, aderdg.FP32_MIXED)])
-def test_served_results_equal_alone(gpu_lib, device_setup, precision):
+@pytest.mark.parametrize("device_setup,precision,share", [(True, aderdg.FP64, "equal"), (False, aderdg.FP64, "equal"),
+                                                          (True, aderdg.FP32_MIXED, "equal"),
+                                                          (True, aderdg.FP32_MIXED, "demand")])
+def test_served_results_equal_alone(gpu_lib, device_setup, precision, share):
     mix = _small_mix(16, seed=3)
     # a budget below every group's largest request: each group's batch then
     # holds exactly its largest request, so no two requests of a group run at
@@ -47,7 +48,7 @@ def test_served_results_equal_alone(gpu_lib, device_setup, precision):
     # most 12 (system, N) groups, so some wait for room while the groups run
     # side by side
     srv = aderdg.serving.Server(hbm_budget_bytes=1 << 20, precision=precision, sync_every=2, keep_results=True,
-                                device_setup=device_setup)
+                                device_setup=device_setup, share=share)
     rep = srv.run(mix, rate=float("inf"), seed=3, max_steps=5)
     srv.close()
     done = rep["requests_done"]
