@@ -90,14 +90,24 @@ class Server:
         self.groups = {}
         self.pool = concurrent.futures.ThreadPoolExecutor(max_workers=workers)
 
-    def _group(self, req, fraction, need_units):
+    @staticmethod
+    def split_budget(budget, demand, need, unit_bytes, share="equal"):
+        """Units of each group's batch: its share of `budget` bytes ("equal":
+        budget / groups; "demand": in proportion to demand[g], the bytes its
+        requests need in total), in units of unit_bytes[g], and never fewer
+        than need[g], its largest request."""
+        total = sum(demand.values())
+        out = {}
+        for g in need:
+            frac = 1.0 / len(need) if (share == "equal" or total <= 0) else demand[g] / total
+            out[g] = max(int(budget * frac / unit_bytes[g]), need[g])
+        return out
+
+    def _group(self, req, units):
         g = self.groups.get(req.group)
         if g is None:
             system, N = req.group
             lim = 0 if system == SYS_ADVDIFF else 1
-            ub = Batch.unit_bytes(system, N, self.precision, lim)
-            # the group's share of the budget, and never less than its largest request
-            units = max(int(self.budget * fraction / ub), need_units)
             g = Batch(system, N, self.precision, lim, capacity_units=units, max_instances=self.max_instances)
             self.groups[req.group] = g
         return g
@@ -116,18 +126,16 @@ class Server:
         reqs = [Request(k, s, float(a), self.precision, max_steps) for k, (s, a) in enumerate(zip(specs, arrivals))]
         need = collections.defaultdict(int)
         demand = collections.defaultdict(float)
+        ubytes = {}
         for r in reqs:
             u = Batch.units(r.cfg)
             need[r.group] = max(need[r.group], u)
             lim = 0 if r.cfg.system == SYS_ADVDIFF else 1
-            demand[r.group] += u * Batch.unit_bytes(r.cfg.system, r.N, self.precision, lim)
-        total = sum(demand.values())
+            ubytes[r.group] = Batch.unit_bytes(r.cfg.system, r.N, self.precision, lim)
+            demand[r.group] += u * ubytes[r.group]
+        units = self.split_budget(self.budget, demand, need, ubytes, self.share)
         for r in reqs:  # all batches exist before the clock starts
-            if self.share == "equal" or total <= 0:
-                frac = 1.0 / len(need)
-            else:
-                frac = demand[r.group] / total
-            self._group(r, frac, need[r.group])
+            self._group(r, units[r.group])
         # results that are not kept land in one page-locked buffer (full-rate
         # device-to-host copies, no first-touch page faults)
         stage = PinnedArray(max(r.dofs for r in reqs)) if (self.download_results and not self.keep_results

@@ -133,3 +133,22 @@ def test_tuning_table_round_trip(gpu_lib):
     with pytest.raises(aderdg.AderdgError):
         aderdg.set_tuning(aderdg.SYS_BN, 6, aderdg.FP32_WIDE)
     aderdg.set_tuning(aderdg.SYS_BN, 4, aderdg.FP32_WIDE, **old)
+
+
+def test_shipped_tuning_table_is_complete_and_valid(gpu_lib):
+    """The table aderdg.load applies (aderdg/tuning_gb300.json): one entry per
+    (system, N, FP32 mode), every choice among the library's candidates, and
+    the library holds exactly those choices after loading."""
+    import json
+    n_pred, n_cells = aderdg.tuning_variants()
+    with open(aderdg.core.TUNING_FILE) as fh:
+        table = json.load(fh)
+    entries = table["entries"]
+    keys = {"%d_%d_%d" % (s, n, p) for s in (0, 1, 2) for n in (1, 2, 3, 4, 5)
+            for p in (aderdg.FP32_MIXED, aderdg.FP32_WIDE)}
+    assert set(entries) == keys
+    for k, e in entries.items():
+        assert 0 <= e["predictor"] < n_pred and 0 <= e["cells"] < n_cells and 0 <= e["subcell_per_sm"] <= 3, k
+        s, n, p = (int(x) for x in k.split("_"))
+        if os.environ.get("ADERDG_TUNING") is None:
+            assert aderdg.get_tuning(s, n, p) == {q: e[q] for q in ("predictor", "cells", "subcell_per_sm")}, k
