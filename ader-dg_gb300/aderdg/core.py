@@ -165,6 +165,7 @@ def load(build_if_missing=False):
         "aderdg_batch_destroy": (i, [vp]),
         "aderdg_batch_admit": (i, [vp, cfgp, dp, dp, d, ctypes.c_long, ip]),
         "aderdg_batch_release": (i, [vp, i]), "aderdg_batch_launch": (i, [vp, i]), "aderdg_batch_sync": (i, [vp, ip]),
+        "aderdg_batch_ready": (i, [vp, ip]),
         "aderdg_batch_query": (i, [vp, i, dp, dp, ctypes.POINTER(ctypes.c_long), ip]),
         "aderdg_batch_download": (i, [vp, i, dp]), "aderdg_batch_download_status": (i, [vp, i, ip]),
         "aderdg_batch_counters": (i, [vp, ip, ip, ip]),
@@ -239,7 +240,7 @@ EXPORTED = ("aderdg_create", "aderdg_destroy", "aderdg_upload", "aderdg_init_lim
             "aderdg_last_error", "aderdg_project_initial_condition", "aderdg_probe_peaks", "aderdg_set_array",
             "aderdg_operator", "aderdg_step_host", "aderdg_time_steps", "aderdg_profile_step",
             "aderdg_batch_unit_bytes", "aderdg_batch_create", "aderdg_batch_destroy", "aderdg_batch_admit",
-            "aderdg_batch_release", "aderdg_batch_launch", "aderdg_batch_sync", "aderdg_batch_query",
+            "aderdg_batch_release", "aderdg_batch_launch", "aderdg_batch_sync", "aderdg_batch_ready", "aderdg_batch_query",
             "aderdg_batch_download", "aderdg_batch_download_status", "aderdg_batch_counters", "aderdg_batch_info", "aderdg_batch_last_error", "aderdg_batch_profile",
             "aderdg_batch_run_timed", "aderdg_initial_condition", "aderdg_batch_admit_ic",
             "aderdg_cell_averages", "aderdg_batch_cell_averages", "aderdg_error_norms", "aderdg_host_alloc",
@@ -592,6 +593,12 @@ class Batch:
         n = ctypes.c_int(0)
         self._ck(self.L.aderdg_batch_sync(self.h, ctypes.byref(n)))
         return n.value
+
+    def ready(self):
+        """True when the batch's queued work has completed (sync would not wait)."""
+        r = ctypes.c_int(0)
+        self._ck(self.L.aderdg_batch_ready(self.h, ctypes.byref(r)))
+        return bool(r.value)
 
     def query(self, slot):
         t, dt, st, done = ctypes.c_double(0), ctypes.c_double(0), ctypes.c_long(0), ctypes.c_int(0)

@@ -191,7 +191,15 @@ class Server:
                 else:
                     time.sleep(0.0005)
                 continue
-            for g in active:
+            # the groups whose round has completed, in completion order: a
+            # group's next round is queued as soon as its own round ends,
+            # without waiting behind another group's longer round
+            ready = [g for g in active if self.groups[g].ready()]
+            if not ready:
+                if not (pending and pending[0].arrival <= clock()):
+                    time.sleep(0.0002)
+                continue
+            for g in ready:
                 b = self.groups[g]
                 b.sync()
                 inflight[g] = False

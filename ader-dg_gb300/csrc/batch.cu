@@ -634,6 +634,19 @@ int aderdg_batch_run_timed(aderdg_batch* const* batches, int n, int steps, doubl
   return ADERDG_OK;
 }
 
+int aderdg_batch_ready(aderdg_batch* b, int* ready) {
+  if (!b || !ready) return bfail(b, ADERDG_EINVAL, "null argument");
+  if (int r = bcheck(b)) return r;
+  const cudaError_t e = cudaStreamQuery(b->stream);
+  if (e == cudaErrorNotReady) {
+    *ready = 0;
+    return ADERDG_OK;
+  }
+  if (e != cudaSuccess) return bbreak(b, bcuda(b, "cudaStreamQuery", e));
+  *ready = 1;
+  return ADERDG_OK;
+}
+
 int aderdg_batch_sync(aderdg_batch* b, int* n_running) {
   if (!b) return bfail(b, ADERDG_EINVAL, "null batch");
   int r = pull_states(b);

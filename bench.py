@@ -75,6 +75,7 @@ def parse():
     ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32"])
     ap.add_argument("--side", type=int, default=0)
     ap.add_argument("--hbm-budget-gb", type=float, default=160.0)
+    ap.add_argument("--sync-every", type=int, default=4, help="served runs: steps per host round of a group")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
@@ -483,7 +484,7 @@ def run_served(aderdg, args, specs, prec, rate):
     (inf: all at once), initial fields evaluated on the device at admission
     (the request's parameters cross to the device), each result downloaded to
     the host when its request ends."""
-    srv = aderdg.serving.Server(hbm_budget_bytes=args.hbm_budget_gb * 1e9, precision=prec, sync_every=4,
+    srv = aderdg.serving.Server(hbm_budget_bytes=args.hbm_budget_gb * 1e9, precision=prec, sync_every=args.sync_every,
                                 device_setup=not args.host_setup, download_results=True)
     rep = srv.run(specs, rate=rate, seed=0, max_steps=args.steps)
     rep.pop("requests_done")

@@ -264,6 +264,11 @@ int aderdg_batch_release(aderdg_batch* b, int slot);
  * back and gives the number still running. */
 int aderdg_batch_launch(aderdg_batch* b, int steps);
 int aderdg_batch_sync(aderdg_batch* b, int* n_running);
+/* Without waiting: *ready = 1 when everything queued on the batch's stream
+ * (steps, admissions, releases) has completed, so that aderdg_batch_sync
+ * returns at once; 0 otherwise.  Lets a host serve many batches in the order
+ * their work completes. */
+int aderdg_batch_ready(aderdg_batch* b, int* ready);
 /* One simulation's state as read back by the last aderdg_batch_sync (read
  * back now, waiting for the batch's stream, when an admission or release came
  * after it). */
