@@ -77,12 +77,13 @@ struct SubCfg {
   // CTAs per SM the register allocation aims at.  FP32: one more than the
   // unconstrained allocation allows where that does not spill.  FP64 (the
   // FP64 pipe bounds it): as many as shared memory admits, up to 4 (Euler:
-  // 128 registers; Baer-Nunziato N <= 3: 3 at 168 registers, where the FP64
-  // mode's reference-order variant spills about 140 bytes and the FP32-mixed
-  // one none; N = 4: 2; N = 5: 1), so that the CTAs' phases without FP64
-  // work (gather loads, barriers) overlap other CTAs' arithmetic.
+  // 128 registers; Baer-Nunziato N = 2: 4 at 128 registers, 128 bytes
+  // spilled, 8% faster than 3 unspilled; N = 3: 3 at 168 registers, where
+  // the FP64 mode's reference-order variant spills about 140 bytes and the
+  // FP32-mixed one none; N = 4: 2; N = 5: 1), so that the CTAs' phases
+  // without FP64 work (gather loads, barriers) overlap other CTAs' arithmetic.
   static constexpr int MIN_BLOCKS = sizeof(T) == 4 ? (Sys::ID == kSysBN ? (N == 3 ? 4 : N == 2 ? 5 : 1) : 6)
-                                                   : (Sys::ID == kSysBN ? (N <= 3 ? 3 : N == 4 ? 2 : 1) : 4);
+                                                   : (Sys::ID == kSysBN ? (N == 2 ? 4 : N <= 3 ? 3 : N == 4 ? 2 : 1) : 4);
   static constexpr int NE = (S + 1) * S;               // x edges (and y edges) of the subgrid
   static constexpr int NEF = (Sys::ID == kSysBN ? 4 : 2) * V * NE;  // edge fluxes (+ BN fluctuations)
   // compute-type (T) elements: sub0 [V][R*R]; the reconstructed states wLx
