@@ -77,13 +77,12 @@ struct SubCfg {
   // CTAs per SM the register allocation aims at.  FP32: one more than the
   // unconstrained allocation allows where that does not spill.  FP64 (the
   // FP64 pipe bounds it): as many as shared memory admits, up to 4 (Euler:
-  // 128 registers; Baer-Nunziato N = 2: 4 at 128 registers, 128 bytes
-  // spilled, 8% faster than 3 unspilled; N = 3: 3 at 168 registers, where
-  // the FP64 mode's reference-order variant spills about 140 bytes and the
-  // FP32-mixed one none; N = 4: 2; N = 5: 1), so that the CTAs' phases
-  // without FP64 work (gather loads, barriers) overlap other CTAs' arithmetic.
+  // 128 registers; Baer-Nunziato N = 2 and 3: 4 at 128 registers, about 130
+  // bytes spilled, 8% and 2% faster than 3 unspilled; N = 4: 2; N = 5: 1), so
+  // that the CTAs' phases without FP64 work (gather loads, barriers) overlap
+  // other CTAs' arithmetic.
   static constexpr int MIN_BLOCKS = sizeof(T) == 4 ? (Sys::ID == kSysBN ? (N == 3 ? 4 : N == 2 ? 5 : 1) : 6)
-                                                   : (Sys::ID == kSysBN ? (N == 2 ? 4 : N <= 3 ? 3 : N == 4 ? 2 : 1) : 4);
+                                                   : (Sys::ID == kSysBN ? (N <= 3 ? 4 : N == 4 ? 2 : 1) : 4);
   static constexpr int NE = (S + 1) * S;               // x edges (and y edges) of the subgrid
   static constexpr int NEF = (Sys::ID == kSysBN ? 4 : 2) * V * NE;  // edge fluxes (+ BN fluctuations)
   // compute-type (T) elements: sub0 [V][R*R]; the reconstructed states wLx
@@ -104,9 +103,13 @@ struct SubCfg {
   static constexpr int TEL = V * R * R + TSTATE + NEF + 2 * S * P + P * P;
   static constexpr int TBYTES = ((TEL * (int)sizeof(T) + 15) / 16) * 16;
   // FP64 elements: new polynomial UN [V][P2], DMP y pass LY [V][S][P], LB
-  // [V][P][P], reduction [2][V][warps], operators uh2lim, uh2lob (FP64)
+  // [V][P][P], reduction [2][V][warps] -- all used after the finite-volume
+  // update, so in the FP64 re-solve they take the edge fluxes' room, which
+  // that update was the last to read -- and the operators uh2lim, uh2lob (FP64)
   static constexpr int OPS_DBL = S * P + P * P;
-  static constexpr int DEL = V * P2 + V * S * P + V * P * P + 2 * V * (THREADS / 32) + OPS_DBL;
+  static constexpr int DMP_DBL = V * P2 + V * S * P + V * P * P + 2 * V * (THREADS / 32);
+  static constexpr bool DMP_IN_EF = sizeof(T) == 8 && DMP_DBL <= NEF;
+  static constexpr int DEL = (DMP_IN_EF ? 0 : DMP_DBL) + OPS_DBL;
   // misc: flags, CFL max, neighbour cells and their status
   static constexpr int MISC = 16 + 9 * 8 + 9 * 4 + 4 * V + 12;
   static constexpr int SMEM_BYTES = TBYTES + DEL * 8 + MISC;
@@ -209,11 +212,11 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
   T* LUY = wRx;                      // [V][P][S]: luhy(v, iii, s) at (v*P + s)*S + iii
   T* NB = wLx;                       // gather staging: [9][V][P2]
   T* LYN = NB + 9 * V * P2;          // [9][V][P][S]: sum_m uh(k, m) uh2lim(s, m) at ((n*V + v)*P + k)*S + s
-  double* UN = reinterpret_cast<double*>(smem_raw + C::TBYTES);  // [V][P2]
+  double* UN = C::DMP_IN_EF ? reinterpret_cast<double*>(EF) : reinterpret_cast<double*>(smem_raw + C::TBYTES);  // [V][P2]
   double* LY = UN + V * P2;          // DMP y pass [V][S][P]
   double* LB = LY + V * S * P;       // [V][P][P]
   double* red = LB + V * P * P;      // [2][V][NW]
-  double* opsm = red + 2 * V * NW;   // uh2lim, uh2lob (FP64)
+  double* opsm = C::DMP_IN_EF ? reinterpret_cast<double*>(smem_raw + C::TBYTES) : red + 2 * V * NW;  // uh2lim, uh2lob (FP64)
   unsigned char* misc = reinterpret_cast<unsigned char*>(opsm + C::OPS_DBL);
   int* flag = reinterpret_cast<int*>(misc);
   unsigned long long* cmaxp = reinterpret_cast<unsigned long long*>(misc + 8);
