@@ -341,7 +341,7 @@ int aderdg_create(const aderdg_config* cfg, aderdg_ctx** out) {
   if (!r) r = dalloc(c, &c->d_st, 1);
   if (!r) r = dalloc(c, &a.uh[0], st_elems);
   if (!r) r = dalloc(c, &a.uh[1], st_elems);
-  // duh and the face fluxes hold FP32 values in the FP32-mixed mode: half the doubles
+  // duh and the face fluxes hold FP32 values in the FP32 modes: half the doubles
   auto stor = [&](size_t n) { return c->fp32 ? (n + 1) / 2 : n; };
   if (!r) r = dalloc(c, &a.duh, stor(st_elems));
   unsigned char *qb = nullptr, *fb = nullptr;

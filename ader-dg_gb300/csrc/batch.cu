@@ -338,7 +338,7 @@ int aderdg_batch_create(int system, int N, int precision, int limiter, long capa
   if (!r) r = balloc(b, &b->d_st_scr, (size_t)max_instances);
   if (!r) r = balloc(b, &a.uh[0], U * P * P * V);
   if (!r) r = balloc(b, &a.uh[1], U * P * P * V);
-  // duh and the face fluxes hold FP32 values in the FP32-mixed mode: half the doubles
+  // duh and the face fluxes hold FP32 values in the FP32 modes: half the doubles
   auto stor = [&](size_t n) { return precision ? (n + 1) / 2 : n; };
   if (!r) r = balloc(b, &a.duh, stor(U * P * P * V));
   unsigned char *qb = nullptr, *fb = nullptr;

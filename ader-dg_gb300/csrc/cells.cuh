@@ -45,7 +45,7 @@ __device__ __forceinline__ double okey_inv(long long k) {
 // on one cell; the caller synchronises between the two passes.  The operators
 // come from shared memory: lim = uh2lim (s,k) at [s + S*k], lob = uh2lob (q,k)
 // at [q + P*k].  T = double: exact-order mul then add, or one fused
-// multiply-add per term (kFast); T = float: fused multiply-adds (FP32-mixed).
+// multiply-add per term (kFast); T = float: fused multiply-adds (the FP32 modes).
 template <int N, int V, class T>
 struct Proj {
   static constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1;
@@ -273,7 +273,7 @@ struct CellCfg {
   // in the same room
   static constexpr int CELL_DBL = V * P2 + V * S * P + V * P * P + 2 * V * P2;
   static_assert(8 * V * P2 + 4 * (3 * V * P2 + V * S * P + V * P * P) <= 8 * CELL_DBL, "FP32 cell layout");
-  static constexpr int OPS_DBL = S * P + P * P;  // uh2lim, uh2lob (FP64, then FP32 in the mixed mode)
+  static constexpr int OPS_DBL = S * P + P * P;  // uh2lim, uh2lob (FP64, then FP32 in the FP32 modes)
   static constexpr int SMEM_BYTES = CPB * CELL_DBL * 8 + OPS_DBL * 12 + CPB * 8 /*cell max*/ + CPB * 4 /*flags*/ +
                                     CPB * V * 4 /*|U| max*/ + CPB * V * 4 /*FP32 reference state*/ + 16;
   // blocks per SM the register allocation aims at, in 256-thread units:

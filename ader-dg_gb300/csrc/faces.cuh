@@ -64,7 +64,7 @@ __device__ __forceinline__ void dmr_state(const PhysC<T>& pc, const double* Vpd,
   for (int v = 0; v < 4; ++v) F[v] = Fb[d * 4 + v];
 }
 
-// Euler Rusanov pieces in the compute type T (FP32 in the mixed mode)
+// Euler Rusanov pieces in the compute type T (FP32 in the FP32 modes)
 template <class T>
 __device__ __forceinline__ T euler_max_eig_t(T gamma, const T* Q, int d) {
   const T u = (d == 0 ? Q[1] : Q[2]) / Q[0];

@@ -543,7 +543,7 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
     }
     __syncthreads();
     if constexpr (sizeof(T) == 4) {
-      // FP32-mixed DMP: deviations from the new polynomial's node-0 state
+      // FP32-wide DMP: deviations from the new polynomial's node-0 state
       for (int p = t; p < P2; p += NT)
 #pragma unroll
         for (int v = 0; v < V; ++v) {
@@ -554,8 +554,8 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
       __syncthreads();
     }
     // ---- DMP of the new polynomial (recompute = 2) and the next min/max.
-    // FP32-mixed: FP32 projections when their error bound stays within the
-    // DMP's absolute tolerance, else FP64 (as in the cell kernel).
+    // FP32-wide (T = float): FP32 projections when their error bound stays
+    // within the DMP's absolute tolerance, else FP64 (as in the cell kernel).
     float err[V];
     bool f32 = false;
     if constexpr (sizeof(T) == 4) {
@@ -594,8 +594,8 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
       Proj<N, V, double>::template xpass_minmax<Sys>(UN, LY, LB, opsm, opsm + S * P, ph, t, NT, mn, mx, posfail);
       warp_minmax_store<double, V, NW>(mn, mx, red, t);
     }
-    // CFL denominator of the new polynomial (FP32-mixed: FP32 eigenvalues
-    // where the FP32 pressure is settled, FP64 otherwise)
+    // CFL denominator of the new polynomial (FP32-wide: FP32 eigenvalues
+    // where the FP32 pressure is settled; FP64 in the other modes)
     for (int p = t; p < P2; p += NT) {
       double Q[V];
 #pragma unroll

@@ -20,7 +20,7 @@ namespace aderdg {
 // Physical constants in the compute type T, formed once from Phys with the
 // same FP64 expressions the reference writes inline (gamma - 1, gamma_s *
 // pi_s, ...): for T = double every function below rounds exactly like the
-// reference expression; T = float serves the FP32-mixed subcell re-solve.
+// reference expression; T = float serves the FP32-wide subcell re-solve.
 template <class T>
 struct PhysC {
   T gamma, gm1;                    // Euler

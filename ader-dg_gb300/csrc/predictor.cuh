@@ -340,7 +340,7 @@ __device__ __forceinline__ void predictor_outputs(const BatchArgs& a, const DevO
   const R* sY = cs + 2 * V * P2;
   if constexpr (kVolume) {
     // volume integral: duh = (w_j/dx) sum_k Kxi(i,k) Fhi_x(k,j) + (w_i/dy) sum_k Kxi(j,k) Fhi_y(i,k) [+ w_i w_j Shi]
-    // duh is stored in the compute precision R (FP32 in the mixed mode)
+    // duh is stored in the compute precision R (FP32 in the FP32 modes)
     R vx, vy;
     if constexpr (sizeof(R) == 4) {
       vx = op.w[j] * R(in.idxf);

@@ -205,7 +205,7 @@ enum aderdg_array {
   ADERDG_A_STATUS        /* int status(I,J) */
 };
 /* Element count of an array (doubles or ints), or a negative error.  In the
- * FP32-mixed mode DUH, QBND, FBND/GRADQBND and FU..GP are held in FP32 on the
+ * FP32 modes DUH, QBND, FBND/GRADQBND and FU..GP are held in FP32 on the
  * device; get/set convert them to and from double. */
 long aderdg_array_size(aderdg_ctx* ctx, int which);
 int aderdg_get_array(aderdg_ctx* ctx, int which, void* out);
