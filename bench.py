@@ -74,6 +74,7 @@ def parse():
     ap.add_argument("--rates", default="10,30,100,300,500", help="Poisson arrival rates swept, requests/s")
     ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32"])
     ap.add_argument("--side", type=int, default=0)
+    ap.add_argument("--N", type=int, default=0, help="single workload: degree (default: the workload's)")
     ap.add_argument("--hbm-budget-gb", type=float, default=160.0)
     ap.add_argument("--sync-every", type=int, default=4, help="served runs: steps per host round of a group")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -354,7 +355,7 @@ def run_reference(args):
                                 "on every host core" % (CPU_SET, CPU_SIDE_CAP), "requests": CPU_SET * cores}
     else:
         import aderdg
-        cfg, ic, params, tend = aderdg.workloads.make(args.workload, side=args.side or None)
+        cfg, ic, params, tend = aderdg.workloads.make(args.workload, side=args.side or None, N=args.N or None)
         specs = [dict(name=args.workload, N=cfg.N, side=cfg.imax, params=params, tend=tend)]
         sample = ("the workload on a %dx%d grid on each of %d cores; %d warm-up + %d timed steps; FP64"
                   % (CPU_SIDE_CAP, CPU_SIDE_CAP, cores, args.warmup, args.steps))
@@ -495,7 +496,8 @@ def run_served(aderdg, args, specs, prec, rate):
 def run_single(args, aderdg, dist, rank, ws, lr):
     """A plain named workload on one simulation (not the headline)."""
     prec = aderdg.FP32_MIXED if args.precision == "fp32" else aderdg.FP64
-    cfg, ic, params, tend = aderdg.workloads.make(args.workload, side=args.side or None, precision=prec)
+    cfg, ic, params, tend = aderdg.workloads.make(args.workload, side=args.side or None, N=args.N or None,
+                                                  precision=prec)
     uh, lh = aderdg.project_initial_condition(cfg, ic, params)
     s = aderdg.Solver(cfg)
     s.upload(uh)
