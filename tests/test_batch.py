@@ -173,3 +173,23 @@ def test_admissions_queue_without_waiting(gpu_lib):
         s.close()
         assert np.array_equal(b.download(slots[k]), alone)
     b.close()
+
+
+def test_ready_reports_completion_without_waiting(gpu_lib):
+    """aderdg_batch_ready: true once everything queued on the batch's stream
+    has completed (then sync does not wait), and never blocks."""
+    import time
+    cfg, ic, params, tend = aderdg.workloads.make("euler_rp2d", side=96, N=3)
+    b = aderdg.Batch(aderdg.SYS_EULER, 3, aderdg.FP64, 1, capacity_units=97 * 97, max_instances=1)
+    slot = _admit(b, cfg, ic, params, tend)
+    b.sync()
+    assert b.ready()
+    b.launch(40)
+    t0 = time.perf_counter()
+    first = b.ready()                       # returns at once, whatever the answer
+    assert time.perf_counter() - t0 < 0.05
+    b.sync()
+    assert b.ready()
+    assert b.query(slot)["steps"] == 40
+    print("ready right after queueing 40 steps: %s" % first)
+    b.close()
