@@ -69,8 +69,14 @@ class Server:
     """Admits requests into per-(system, N) batches under an HBM budget."""
 
     def __init__(self, hbm_budget_bytes, precision=FP64, max_instances=256, sync_every=4, workers=8,
-                 keep_results=False, device_setup=True, download_results=True, share="equal"):
+                 keep_results=False, device_setup=True, download_results=True, share="equal", backfill_window=16,
+                 backfill_s=1.0):
         self.budget = int(hbm_budget_bytes)
+        # admission: up to backfill_window waiting requests of a group are tried
+        # per round (1: strict arrival order), while its oldest waiting request
+        # has waited at most backfill_s seconds
+        self.backfill_window = max(1, int(backfill_window))
+        self.backfill_s = backfill_s
         # how the budget is split over the (system, N) groups: "equal" in
         # equal parts, "demand" in proportion to the device bytes their
         # requests need in total (each group then holds about the same
@@ -161,24 +167,34 @@ class Server:
             # kernels overlap the next admissions
             for g, q in waiting.items():
                 b = self.groups[g]
-                while q:
-                    r = q[0]
+                # in arrival order; a request that does not fit yet does not
+                # block the smaller ones behind it (backfill, within a window),
+                # unless it has waited longer than backfill_s: then the room
+                # that frees up is kept for it
+                k = 0
+                now = clock()
+                while k < len(q):
+                    r = q[k]
+                    slot = None
                     if self.device_setup and r.uh is None:
                         slot = b.admit_ic(r.cfg, r.ic, r.params, r.tend, r.max_steps)
-                        if slot is None:
-                            break
-                        self.h2d_bytes += 32 * 8
+                        if slot is not None:
+                            self.h2d_bytes += 32 * 8
                     else:
                         f = futures[r.rid]
-                        if not f.done():
+                        if f.done():
+                            uh, lh = f.result()
+                            slot = b.admit(r.cfg, uh, lh, r.tend, r.max_steps)
+                            if slot is not None:
+                                del futures[r.rid]
+                                self.h2d_bytes += uh.nbytes + (lh.nbytes if lh is not None else 0)
+                    if slot is None:
+                        if (k + 1 >= self.backfill_window or now - q[0].arrival > self.backfill_s
+                                or len(running[g]) >= self.max_instances):
                             break
-                        uh, lh = f.result()
-                        slot = b.admit(r.cfg, uh, lh, r.tend, r.max_steps)
-                        if slot is None:
-                            break
-                        del futures[r.rid]
-                        self.h2d_bytes += uh.nbytes + (lh.nbytes if lh is not None else 0)
-                    q.popleft()
+                        k += 1
+                        continue
+                    del q[k]
                     r.slot, r.admitted = slot, clock()
                     running[g][slot] = r
                 if running[g] and not inflight[g]:
