@@ -542,18 +542,23 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
       }
     }
     __syncthreads();
+    // ---- DMP of the new polynomial: recompute = 2 cells only (a recompute =
+    // 1 cell is limited whatever it gives, and its next min/max come from
+    // its subcell data), uniform per CTA.
+    const bool dmp = rec == 2;
     if constexpr (sizeof(T) == 4) {
       // FP32-wide DMP: deviations from the new polynomial's node-0 state
-      for (int p = t; p < P2; p += NT)
+      if (dmp) {
+        for (int p = t; p < P2; p += NT)
 #pragma unroll
-        for (int v = 0; v < V; ++v) {
-          const float d = (float)(UN[v * P2 + p] - UN[v * P2]);
-          UNf[v * P2 + p] = d;
-          atomicMax(&amax[v], __float_as_uint(fabsf(d)));
-        }
+          for (int v = 0; v < V; ++v) {
+            const float d = (float)(UN[v * P2 + p] - UN[v * P2]);
+            UNf[v * P2 + p] = d;
+            atomicMax(&amax[v], __float_as_uint(fabsf(d)));
+          }
+      }
       __syncthreads();
     }
-    // ---- DMP of the new polynomial (recompute = 2) and the next min/max.
     // FP32-wide (T = float): FP32 projections when their error bound stays
     // within the DMP's absolute tolerance, else FP64 (as in the cell kernel).
     float err[V];
@@ -567,13 +572,15 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
       }
     }
     if constexpr (sizeof(T) == 4) {
-      if (f32) Proj<N, V, float>::template ypass<true>(UNf, LYf, LBf, limT, lobT, t, NT);
+      if (dmp && f32) Proj<N, V, float>::template ypass<true>(UNf, LYf, LBf, limT, lobT, t, NT);
     }
-    if (!f32) Proj<N, V, double>::ypass(UN, LY, LB, opsm, opsm + S * P, t, NT);
+    if (dmp && !f32) Proj<N, V, double>::ypass(UN, LY, LB, opsm, opsm + S * P, t, NT);
     __syncthreads();
     double mn[V], mx[V];
     bool posfail = false;
-    if (f32) {
+    if (!dmp) {
+      // no projections: the CFL part below only
+    } else if (f32) {
       float fmn[V], fmx[V];
 #pragma unroll
       for (int v = 0; v < V; ++v) { fmn[v] = __int_as_float(0x7f800000); fmx[v] = -__int_as_float(0x7f800000); }
@@ -615,7 +622,7 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
     __syncthreads();
     double* mmo = a.mm[par ^ 1] + (size_t)c * 2 * V;
     double dmn = 0.0, dmx = 0.0;  // thread v < V: min/max of the new polynomial's variable v
-    if (t < V) {
+    if (dmp && t < V) {
       const int v = t;
       double cmn, cmx;
       if (f32) {
