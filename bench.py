@@ -138,7 +138,7 @@ def predictor_flops_per_cell(system, N, ad_fused=True):
     return P2 * (setup + it1 + mids * mid + last + vol) + faces
 
 
-def subcell_flops_per_cell(system, N):
+def subcell_flops_per_cell(system, N, dmp=True):
     """Floating-point operations of the subcell re-solve (k_subcell, FP64 in the
     FP32-mixed mode) per re-solved cell, from its loop structure: the 3x3
     neighbourhood's subcell data (y pass of the rows the reconstruction reads,
@@ -147,9 +147,10 @@ def subcell_flops_per_cell(system, N):
     directions, the half-step update), the Rusanov fluxes of the subgrid
     edges with their eigenvalues (Baer-Nunziato: plus the 3-point path
     integral), the finite-volume update, put_subcell_data, the DMP
-    projections of the new polynomial and the CFL eigenvalues of its nodes.
-    A fused multiply-add counts 2, a division or square root 1, as in
-    predictor_flops_per_cell."""
+    projections of the new polynomial (dmp: a recompute = 2 cell; a
+    recompute = 1 cell has none, Euler/limiter.f90:599-620) and the CFL
+    eigenvalues of its nodes. A fused multiply-add counts 2, a division or
+    square root 1, as in predictor_flops_per_cell."""
     P, S, V = N + 1, 2 * N + 1, NVAR[system]
     R, H, NE = S + 4, S + 2, (S + 1) * S
     dot = lambda n: 2 * n - 1  # noqa: E731
@@ -164,9 +165,9 @@ def subcell_flops_per_cell(system, N):
     edges = 2 * NE * (2 * (flux + eig) + 5 * V + roe)
     fv = S * S * (V * (16 if bn else 8) + ncp)
     put = V * (P * S + P * P) * dot(S)
-    dmp = V * ((P * S + P * P) * dot(P) + (S * S + P * P) * dot(P))
+    dmp_proj = V * ((P * S + P * P) * dot(P) + (S * S + P * P) * dot(P)) if dmp else 0
     cfl = P * P * (45 if bn else 21)
-    return gather + muscl + edges + fv + put + dmp + cfl
+    return gather + muscl + edges + fv + put + dmp_proj + cfl
 
 
 # ---------------------------------------------------------------- clocks
@@ -407,12 +408,14 @@ def _resident(aderdg, specs, prec, W, K):
 
 def _profile_groups(groups):
     """Per-launch device ms of one more (eager) step of every group, summed,
-    and each group's re-solved cells in that step."""
+    and each group's re-solved cells in that step: (listed, troubled), the
+    troubled ones being its recompute = 1 cells."""
     tot, listed = {}, {}
     for key, g in groups.items():
         for k, v in g.profile().items():
             tot[k] = tot.get(k, 0.0) + v
-        listed[key] = g.counters()["n_listed"]
+        c = g.counters()
+        listed[key] = (c["n_listed"], c["n_recompute"])
     return tot, listed
 
 
@@ -665,18 +668,22 @@ def run_mix(args, aderdg, dist, rank, ws, lr):
     ach = pred_flops / (pred_ms * 1e-3) / 1e9 if pred_ms > 0 else None
     mode_key = "fp32" if mixed else "fp64"
     traffic, limiter = _traffic(head["group_dofs"], "k_predictor_bytes_per_dof", mode_key)
-    listed = {k: n for k, n in head["listed"].items() if k[0] != aderdg.SYS_ADVDIFF}
+    listed = {k: n[0] for k, n in head["listed"].items() if k[0] != aderdg.SYS_ADVDIFF}
     sub_traffic, sub_limiter = _traffic(listed, "k_subcell_bytes_per_listed_cell", mode_key)
     dominant = max(kern_ms, key=lambda k: kern_ms[k])
     sub_ms = ph.get("subcell", 0.0)
-    sub_flops = sum(subcell_flops_per_cell(key[0], key[1]) * n for key, n in head["listed"].items())
+    sub_flops = sum(subcell_flops_per_cell(key[0], key[1], dmp=False) * n1
+                    + (subcell_flops_per_cell(key[0], key[1]) - subcell_flops_per_cell(key[0], key[1], dmp=False))
+                    * (n1 - n2) for key, (n1, n2) in head["listed"].items())
     sub_ach = sub_flops / (sub_ms * 1e-3) / 1e9 if sub_ms > 0 else None
     roof_sub = {"bound": "fp64", "kernel": "k_subcell (the subcell re-solve, FP64, all groups with the limiter)",
                 "achieved": sub_ach, "peak": fp64_peak, "unit": "GFLOP/s",
                 "frac": (sub_ach / fp64_peak) if sub_ach else None,
                 "peak_source": "FP64 FMA throughput measured on this GPU by aderdg_probe_peaks",
-                "flops_per_launch": sub_flops, "listed_cells": int(sum(head["listed"].values())),
-                "flop_model": "bench.py subcell_flops_per_cell x re-solved cells of the profiled step",
+                "flops_per_launch": sub_flops, "listed_cells": int(sum(n[0] for n in head["listed"].values())),
+                "troubled_cells": int(sum(n[1] for n in head["listed"].values())),
+                "flop_model": "bench.py subcell_flops_per_cell x re-solved cells of the profiled step, "
+                              "the DMP projections for its recompute = 2 cells only",
                 "launch_ms": sub_ms, "dominant_phase": dominant,
                 "phase_share": {k: v / sum(kern_ms.values()) for k, v in kern_ms.items()},
                 "phase_ms_one_step": ph, "traffic": sub_traffic,
@@ -691,7 +698,8 @@ def run_mix(args, aderdg, dist, rank, ws, lr):
             "launch_ms": pred_ms, "dominant_phase": dominant,
             "phase_share": {k: v / sum(kern_ms.values()) for k, v in kern_ms.items()},
             "phase_ms_one_step": ph, "traffic": traffic,
-            "groups": {"%d_%d" % k: {"dofs": head["group_dofs"][k], "listed_cells": head["listed"].get(k, 0)}
+            "groups": {"%d_%d" % k: {"dofs": head["group_dofs"][k], "listed_cells": head["listed"].get(k, (0, 0))[0],
+                                   "troubled_cells": head["listed"].get(k, (0, 0))[1]}
                        for k in head["group_dofs"]},
             "traffic_source": "profiles/traffic.json: DRAM bytes per DOF of k_predictor per (system, N) group from "
                               "one ncu capture of the batched mix, times each group's DOFs",
