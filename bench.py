@@ -84,6 +84,9 @@ def parse():
     ap.add_argument("--host-setup", action="store_true", help="serve with host-projected initial fields")
     ap.add_argument("--to-tend", action="store_true",
                     help="single workload: also run it from t=0 to its end time (time-to-solution, exact-solution error)")
+    ap.add_argument("--study", default="",
+                    help="single workload with an exact solution: grid sides (e.g. 32,64,128,256) each run from t=0 to "
+                         "its end time; error against the exact solution and the observed order per refinement")
     return ap.parse_args()
 
 
@@ -572,6 +575,32 @@ def run_to_tend(aderdg, cfg, ic, params, tend):
     return out
 
 
+def run_study(args, aderdg):
+    """Convergence study of a workload with an exact solution (the isentropic
+    vortex's configuration: N = 4, limiter on, grids 32 to 256, t = 10): each
+    grid from its initial field to the end time through the device-resident
+    loop; L1 / L2 / L-infinity error of the density (u for advection-diffusion)
+    cell averages against the exact solution, as Euler/analyze_soln.f90:10-56
+    measures it, and the order log2(e(h) / e(h/2)) between successive grids."""
+    prec = aderdg.FP32_MIXED if args.precision == "fp32" else aderdg.FP64
+    sides = [int(x) for x in args.study.split(",") if x]
+    rows = []
+    for side in sides:
+        cfg, ic, params, tend = aderdg.workloads.make(args.workload, side=side, N=args.N or None, precision=prec)
+        if ic not in (aderdg.IC_EULER_VORTEX, aderdg.IC_AD_SINE):
+            raise SystemExit("--study needs a workload with an exact solution (euler_vortex, ad_sine)")
+        r = run_to_tend(aderdg, cfg, ic, params, tend)
+        err = r["error_vs_exact"]
+        rows.append(dict(side=side, N=cfg.N, steps=r["steps"], tts_s=r["tts_s"],
+                         limited_cells_at_end=r["limited_cells_at_end"], l1=err["l1"], l2=err["l2"], linf=err["linf"]))
+    for a, b in zip(rows, rows[1:]):
+        b["order_l1"] = float(np.log2(a["l1"] / b["l1"])) if b["l1"] > 0 else None
+        b["order_linf"] = float(np.log2(a["linf"] / b["linf"])) if b["linf"] > 0 else None
+    return {"study": args.workload, "precision": args.precision, "limiter": int(cfg.limiter), "tend": tend,
+            "grids": rows, "what": "error of the final cell averages against the exact solution per grid; order "
+                                   "between successive grids"}
+
+
 def allsum(dist, x):
     if dist is None:
         return x
@@ -752,6 +781,10 @@ def run_ours(args):
         sys.exit(2)
     import aderdg
     aderdg.build()
+    if args.study:
+        if rank == 0:
+            print(json.dumps(run_study(args, aderdg)), flush=True)
+        return
     if args.workload != "mix":
         line = run_single(args, aderdg, dist, rank, ws, lr)
         if line:
