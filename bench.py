@@ -147,7 +147,8 @@ def subcell_flops_per_cell(system, N, dmp=True):
     neighbourhood's subcell data (y pass of the rows the reconstruction reads,
     x pass of the gathered strip; every neighbour counted unlimited), the
     MUSCL-Hancock reconstruction (slopes, the four half-step fluxes along their
-    directions, the half-step update), the Rusanov fluxes of the subgrid
+    directions, the half-step update; Euler: the interior subcells, its halo
+    subcells having zero slopes), the Rusanov fluxes of the subgrid
     edges with their eigenvalues (Baer-Nunziato: plus the 3-point path
     integral), the finite-volume update, put_subcell_data, the DMP
     projections of the new polynomial (dmp: a recompute = 2 cell; a
@@ -163,8 +164,10 @@ def subcell_flops_per_cell(system, N, dmp=True):
     ncp = 20 if bn else 0            # p_g, u_n and the NCP source
     roe = 3 * (2 * 9 + 13 + 6) + 9 if bn else 0
     gather = (3 * S + 12) * V * P * dot(P) + R * R * V * dot(P)
-    slope_states = H * H if bn else S * S
-    muscl = slope_states * 2 * V * 4 + H * H * (8 * V + 4 * flux + 4 * V + 8 * V + ncp + (V if bn else 0))
+    # Euler: slopes of the interior subcells only, so a halo state's four
+    # half-step fluxes cancel and its evolved states are its own value (no work)
+    evolved = H * H if bn else S * S
+    muscl = evolved * 2 * V * 4 + evolved * (8 * V + 4 * flux + 4 * V + 8 * V + ncp + (V if bn else 0))
     edges = 2 * NE * (2 * (flux + eig) + 5 * V + roe)
     fv = S * S * (V * (16 if bn else 8) + ncp)
     put = V * (P * S + P * P) * dot(S)
