@@ -145,7 +145,8 @@ def subcell_flops_per_cell(system, N, dmp=True):
     """Floating-point operations of the subcell re-solve (k_subcell, FP64 in the
     FP32-mixed mode) per re-solved cell, from its loop structure: the 3x3
     neighbourhood's subcell data (y pass of the rows the reconstruction reads,
-    x pass of the gathered strip; every neighbour counted unlimited), the
+    x pass of the strip it reads: two rings of neighbour subcells for
+    Baer-Nunziato, one for Euler; every neighbour counted unlimited), the
     MUSCL-Hancock reconstruction (slopes, the four half-step fluxes along their
     directions, the half-step update; Euler: the interior subcells, its halo
     subcells having zero slopes), the Rusanov fluxes of the subgrid
@@ -156,14 +157,18 @@ def subcell_flops_per_cell(system, N, dmp=True):
     eigenvalues of its nodes. A fused multiply-add counts 2, a division or
     square root 1, as in predictor_flops_per_cell."""
     P, S, V = N + 1, 2 * N + 1, NVAR[system]
-    R, H, NE = S + 4, S + 2, (S + 1) * S
+    H, NE = S + 2, (S + 1) * S
     dot = lambda n: 2 * n - 1  # noqa: E731
     bn = system == 2
     flux = 36 if bn else 15          # flux along one axis (reciprocal, velocities, pressure, components)
     eig = 16 if bn else 7            # sound speeds and maxval(abs(Lambda))
     ncp = 20 if bn else 0            # p_g, u_n and the NCP source
     roe = 3 * (2 * 9 + 13 + 6) + 9 if bn else 0
-    gather = (3 * S + 12) * V * P * dot(P) + R * R * V * dot(P)
+    # the rows and columns the reconstruction reads: Baer-Nunziato's halo
+    # slopes need two rings of neighbour subcells, Euler's interior slopes one
+    ring = 2 if bn else 1
+    G = S + 2 * ring
+    gather = (3 * S + 6 * ring) * V * P * dot(P) + G * G * V * dot(P)
     # Euler: slopes of the interior subcells only, so a halo state's four
     # half-step fluxes cancel and its evolved states are its own value (no work)
     evolved = H * H if bn else S * S
