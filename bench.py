@@ -143,41 +143,51 @@ def predictor_flops_per_cell(system, N, ad_fused=True):
 
 def subcell_flops_per_cell(system, N, dmp=True):
     """Floating-point operations of the subcell re-solve (k_subcell, FP64 in the
-    FP32-mixed mode) per re-solved cell, from its loop structure: the 3x3
-    neighbourhood's subcell data (y pass of the rows the reconstruction reads,
-    x pass of the strip it reads: two rings of neighbour subcells for
-    Baer-Nunziato, one for Euler; every neighbour counted unlimited), the
-    MUSCL-Hancock reconstruction (slopes, the four half-step fluxes along their
-    directions, the half-step update; Euler: the interior subcells, its halo
-    subcells having zero slopes), the Rusanov fluxes of the subgrid
-    edges with their eigenvalues (Baer-Nunziato: plus the 3-point path
-    integral), the finite-volume update, put_subcell_data, the DMP
-    projections of the new polynomial (dmp: a recompute = 2 cell; a
-    recompute = 1 cell has none, Euler/limiter.f90:599-620) and the CFL
-    eigenvalues of its nodes. A fused multiply-add counts 2, a division or
-    square root 1, as in predictor_flops_per_cell."""
+    FP32-mixed mode) per re-solved cell: what the new subcell data, the new
+    polynomial, its DMP verdict (dmp: a recompute = 2 cell; a recompute = 1
+    cell has none, Euler/limiter.f90:599-620) and its CFL denominators need.
+    A fused multiply-add counts 2, a division or square root 1, as in
+    predictor_flops_per_cell.
+
+    Euler: equal to the instrumented count of tests/test_subcell_flop_model.py
+    -- the neighbourhood's subcell data the interior slopes read (the y pass
+    of 3S + 2 neighbour rows, the x pass of the S^2 + 4S subcells), MUSCL-
+    Hancock on the S^2 interior subcells (the halo subcells have zero slopes:
+    their half-step flux differences vanish and their face states are their
+    values), the Rusanov flux of every subgrid edge along its normal, the
+    finite-volume update, put_subcell_data, the DMP (subcell and Gauss-Lobatto
+    projections, thresholds, the pressure of every subcell) and the CFL
+    denominator of every node.
+
+    Baer-Nunziato: from the loop structure, not instrumented -- two rings of
+    neighbour subcells (its halo slopes), MUSCL-Hancock with the NCP source on
+    all (S+2)^2 subcells, the edge fluxes with the 3-point path integral, the
+    FV update with the fluctuations and the NCP source, put_subcell_data, the
+    DMP projections and the CFL eigenvalues."""
     P, S, V = N + 1, 2 * N + 1, NVAR[system]
     H, NE = S + 2, (S + 1) * S
     dot = lambda n: 2 * n - 1  # noqa: E731
-    bn = system == 2
-    flux = 36 if bn else 15          # flux along one axis (reciprocal, velocities, pressure, components)
-    eig = 16 if bn else 7            # sound speeds and maxval(abs(Lambda))
-    ncp = 20 if bn else 0            # p_g, u_n and the NCP source
-    roe = 3 * (2 * 9 + 13 + 6) + 9 if bn else 0
-    # the rows and columns the reconstruction reads: Baer-Nunziato's halo
-    # slopes need two rings of neighbour subcells, Euler's interior slopes one
-    ring = 2 if bn else 1
-    G = S + 2 * ring
-    gather = (3 * S + 6 * ring) * V * P * dot(P) + G * G * V * dot(P)
-    # Euler: slopes of the interior subcells only, so a halo state's four
-    # half-step fluxes cancel and its evolved states are its own value (no work)
-    evolved = H * H if bn else S * S
-    muscl = evolved * 2 * V * 4 + evolved * (8 * V + 4 * flux + 4 * V + 8 * V + ncp + (V if bn else 0))
+    if system != 2:
+        flux, eig = 14, 4                      # flux along one axis with one reciprocal; |u_n| + c
+        setup = 5                              # dx/S, dy/S, dt/(dx/S), dt/(dy/S), dt/2
+        gather = (3 * S + 2) * V * P * dot(P) + (S * S + 4 * S) * V * dot(P)
+        muscl = S * S * (20 * V + 4 * flux)    # slopes 4V, face states 6V, Qt 5V, half step 5V
+        edges = 2 * NE * (2 * (flux + eig) + 1 + 5 * V)
+        fv = S * S * 6 * V
+        put = V * (P * S + P * P) * dot(S)
+        dmp_work = (V * ((P * S + P * P) + (S * S + P * P)) * dot(P) + 7 * S * S + 4 * V) if dmp else 0
+        cfl = P * P * 19
+        return setup + gather + muscl + edges + fv + put + dmp_work + cfl
+    flux, eig, ncp = 36, 16, 20                # flux along one axis; sound speeds; p_g, u_n and the NCP source
+    roe = 3 * (2 * 9 + 13 + 6) + 9
+    G = S + 4
+    gather = (3 * S + 12) * V * P * dot(P) + G * G * V * dot(P)
+    muscl = H * H * 2 * V * 4 + H * H * (8 * V + 4 * flux + 4 * V + 8 * V + ncp + V)
     edges = 2 * NE * (2 * (flux + eig) + 5 * V + roe)
-    fv = S * S * (V * (16 if bn else 8) + ncp)
+    fv = S * S * (V * 16 + ncp)
     put = V * (P * S + P * P) * dot(S)
     dmp_proj = V * ((P * S + P * P) * dot(P) + (S * S + P * P) * dot(P)) if dmp else 0
-    cfl = P * P * (45 if bn else 21)
+    cfl = P * P * 45
     return gather + muscl + edges + fv + put + dmp_proj + cfl
 
 
