@@ -293,18 +293,25 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
     }
     if (t < V) amax[t] = 0u;
     __syncthreads();
-    for (int p = t; p < 9 * P2 * V; p += NT) {
-      const int n = p / (P2 * V), r = p - n * (P2 * V);
+    // Euler's interior slopes read one ring of neighbour subcells, beside the
+    // cell's edges only (neighbours n = 1, 3, 5, 7); Baer-Nunziato's halo
+    // slopes read two rings, corners included (all nine)
+    constexpr int NNB = BN ? 9 : 5;
+    for (int p = t; p < NNB * P2 * V; p += NT) {
+      const int m = p / (P2 * V), r = p - m * (P2 * V);
+      const int n = BN ? m : (m == 0 ? 1 : m == 4 ? 7 : m + 2);
       const int node = r / V, v = r - node * V;
       if (nbs[n] == 0) NB[(n * V + v) * P2 + node] = (T)a.uh[par][(size_t)nbc[n] * P2 * V + r];
     }
     __syncthreads();
     // the items actually read, enumerated densely (no idle lanes): all S
-    // rows of the neighbours beside the cell (n = 3, 4, 5), and the two rows
-    // nearest to the cell of those below (n = 0, 1, 2: subcell rows S-2, S-1)
-    // and above (n = 6, 7, 8: rows 0, 1); LYN keeps the full [9][V][P][S] index
-    constexpr int NMID = 3 * V * P * S, NROW = 2 * V * P;
-    for (int q = t; q < NMID + 6 * NROW; q += NT) {
+    // rows of the neighbours beside the cell (n = 3, 4, 5), and the rows
+    // nearest to the cell of those below and above -- Baer-Nunziato: two of
+    // n = 0, 1, 2 (subcell rows S-2, S-1) and of n = 6, 7, 8 (rows 0, 1);
+    // Euler: one of n = 1 (row S-1) and of n = 7 (row 0); LYN keeps the full
+    // [9][V][P][S] index
+    constexpr int NMID = 3 * V * P * S, NROW = (BN ? 2 : 1) * V * P, NOUT = BN ? 6 : 2;
+    for (int q = t; q < NMID + NOUT * NROW; q += NT) {
       int n, v, kk, sb;
       if (q < NMID) {
         n = 3 + q / (V * P * S);
@@ -312,12 +319,18 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
         v = r / (P * S);
         kk = (r / S) % P;
         sb = r % S;
-      } else {
+      } else if constexpr (BN) {
         const int q2 = q - NMID, n6 = q2 / NROW, r2 = q2 % NROW;
         n = n6 < 3 ? n6 : n6 + 3;
         v = r2 / (2 * P);
         kk = (r2 >> 1) % P;
         sb = (n < 3 ? S - 2 : 0) + (r2 & 1);
+      } else {
+        const int q2 = q - NMID, r2 = q2 % NROW;
+        n = q2 < NROW ? 1 : 7;
+        v = r2 / P;
+        kk = r2 % P;
+        sb = n == 1 ? S - 1 : 0;
       }
       if (nbs[n] != 0) continue;
       const T* u = NB + (n * V + v) * P2;
@@ -327,8 +340,23 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
       LYN[((n * V + v) * P + kk) * S + sb] = ly;
     }
     __syncthreads();
-    for (int p = t; p < R * R; p += NT) {
-      const int ii = p % R - 1, jj = p / R - 1;
+    // Baer-Nunziato: subcells -1 .. S+2 in both directions; Euler: the S x S
+    // interior and the four strips beside it (columns 1..S of rows 0..S+1,
+    // then columns 0 and S+1 of rows 1..S)
+    constexpr int NX = BN ? R * R : S * S + 4 * S;
+    for (int p = t; p < NX; p += NT) {
+      int ii, jj;
+      if constexpr (BN) {
+        ii = p % R - 1;
+        jj = p / R - 1;
+      } else if (p < S * (S + 2)) {
+        ii = 1 + p % S;
+        jj = p / S;
+      } else {
+        const int p2 = p - S * (S + 2);
+        ii = p2 < S ? 0 : S + 1;
+        jj = 1 + p2 % S;
+      }
       const int bi = ii < 1 ? -1 : (ii > S ? 1 : 0), bj = jj < 1 ? -1 : (jj > S ? 1 : 0);
       const int sa = ii - 1 - bi * S, sb = jj - 1 - bj * S;
       const int n = (bi + 1) + 3 * (bj + 1);
@@ -392,6 +420,8 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
       }
       const bool interior = p < S * S;
       if (!BN && !interior) {
+        // the corners are neither gathered nor read by an edge
+        if ((ii == 0 || ii == H - 1) && (jj == 0 || jj == H - 1)) continue;
 #pragma unroll
         for (int v = 0; v < V; ++v) {
           const T q = SU(v, ii, jj);
