@@ -149,7 +149,8 @@ def subcell_flops_per_cell(system, N, dmp=True):
     A fused multiply-add counts 2, a division or square root 1, as in
     predictor_flops_per_cell.
 
-    Euler: equal to the instrumented count of tests/test_subcell_flop_model.py
+    Both systems equal the instrumented count of tests/test_subcell_flop_model.py.
+    Euler
     -- the neighbourhood's subcell data the interior slopes read (the y pass
     of 3S + 2 neighbour rows, the x pass of the S^2 + 4S subcells), MUSCL-
     Hancock on the S^2 interior subcells (the halo subcells have zero slopes:
@@ -159,11 +160,14 @@ def subcell_flops_per_cell(system, N, dmp=True):
     projections, thresholds, the pressure of every subcell) and the CFL
     denominator of every node.
 
-    Baer-Nunziato: from the loop structure, not instrumented -- two rings of
-    neighbour subcells (its halo slopes), MUSCL-Hancock with the NCP source on
-    all (S+2)^2 subcells, the edge fluxes with the 3-point path integral, the
-    FV update with the fluctuations and the NCP source, put_subcell_data, the
-    DMP projections and the CFL eigenvalues."""
+    Baer-Nunziato: likewise equal to the instrumented count -- the neighbour
+    subcells the slopes of the (S+2)^2 - 4 evolved subcells read (two rings:
+    3S + 8 rows in the y pass, (S+2)^2 + 4S subcells in the x pass),
+    MUSCL-Hancock with the NCP source on those subcells, per edge the Rusanov
+    flux and the path-conservative fluctuation (3-point path integral), the
+    finite-volume update with the fluctuations and the NCP source at the half
+    step, put_subcell_data, the DMP (with the admissibility of every subcell)
+    and the CFL denominators."""
     P, S, V = N + 1, 2 * N + 1, NVAR[system]
     H, NE = S + 2, (S + 1) * S
     dot = lambda n: 2 * n - 1  # noqa: E731
@@ -178,17 +182,27 @@ def subcell_flops_per_cell(system, N, dmp=True):
         dmp_work = (V * ((P * S + P * P) + (S * S + P * P)) * dot(P) + 7 * S * S + 4 * V) if dmp else 0
         cfl = P * P * 19
         return setup + gather + muscl + edges + fv + put + dmp_work + cfl
-    flux, eig, ncp = 36, 16, 20                # flux along one axis; sound speeds; p_g, u_n and the NCP source
-    roe = 3 * (2 * 9 + 13 + 6) + 9
-    G = S + 4
-    gather = (3 * S + 12) * V * P * dot(P) + G * G * V * dot(P)
-    muscl = H * H * 2 * V * 4 + H * H * (8 * V + 4 * flux + 4 * V + 8 * V + ncp + V)
-    edges = 2 * NE * (2 * (flux + eig) + 5 * V + roe)
-    fv = S * S * (V * 16 + ncp)
+    # Baer-Nunziato: flux along one axis from one reciprocal of Q0 Q4 (35), the
+    # sound speeds and maxval(abs(Lambda)) (12), the NCP source from p_g and u_n
+    # (22: only the volume-fraction gradient enters), the Roe fluctuation (111:
+    # PDEMatrixB has one non-zero column, so three path points of p_g, u_n
+    # and p_g u_n times the jump of alpha)
+    flux, eig, ncp, roe = 35, 12, 22, 111
+    setup = 7                                  # dx/S, dy/S, dt/(dx/S), dt/(dy/S), dt/2 and their halves
+    gather = (3 * S + 8) * V * P * dot(P) + (H * H + 4 * S) * V * dot(P)
+    # the (S+2)^2 - 4 evolved subcells (the corners feed no edge): slopes 4V,
+    # alpha gradient 2, source, face states 6V, 4 fluxes, Qt 5V + 1 (the
+    # structural zeros of the source and of the ninth flux component), half step 5V
+    muscl = (H * H - 4) * (4 * V + 2 + ncp + 6 * V + 4 * flux + 5 * V + 1 + 5 * V)
+    # per edge: the jump, two fluxes and speeds, the Rusanov flux, the fluctuation
+    edges = 2 * NE * (V + 2 * (flux + eig) + 4 * (V - 1) + 2 + roe)
+    # per subcell: the half-step state, its source, flux differences 6V, the
+    # five non-zero fluctuation components per direction, the seven of the source
+    fv = S * S * (2 * V + ncp + 6 * V + 2 * 15 + 14)
     put = V * (P * S + P * P) * dot(S)
-    dmp_proj = V * ((P * S + P * P) * dot(P) + (S * S + P * P) * dot(P)) if dmp else 0
-    cfl = P * P * 45
-    return gather + muscl + edges + fv + put + dmp_proj + cfl
+    dmp_work = (V * ((P * S + P * P) + (S * S + P * P)) * dot(P) + 4 * V + 27 * S * S) if dmp else 0
+    cfl = P * P * 44
+    return setup + gather + muscl + edges + fv + put + dmp_work + cfl
 
 
 # ---------------------------------------------------------------- clocks
