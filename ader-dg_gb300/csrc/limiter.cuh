@@ -295,7 +295,8 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
     __syncthreads();
     // Euler's interior slopes read one ring of neighbour subcells, beside the
     // cell's edges only (neighbours n = 1, 3, 5, 7); Baer-Nunziato's halo
-    // slopes read two rings, corners included (all nine)
+    // slopes read two rings beside the edges and the first ring's corners
+    // (all nine neighbours)
     constexpr int NNB = BN ? 9 : 5;
     for (int p = t; p < NNB * P2 * V; p += NT) {
       const int m = p / (P2 * V), r = p - m * (P2 * V);
@@ -307,10 +308,11 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
     // the items actually read, enumerated densely (no idle lanes): all S
     // rows of the neighbours beside the cell (n = 3, 4, 5), and the rows
     // nearest to the cell of those below and above -- Baer-Nunziato: two of
-    // n = 0, 1, 2 (subcell rows S-2, S-1) and of n = 6, 7, 8 (rows 0, 1);
-    // Euler: one of n = 1 (row S-1) and of n = 7 (row 0); LYN keeps the full
+    // n = 1 (subcell rows S-2, S-1) and of n = 7 (rows 0, 1), one of the
+    // corner neighbours n = 0, 2 (row S-1) and n = 6, 8 (row 0); Euler: one
+    // of n = 1 (row S-1) and of n = 7 (row 0); LYN keeps the full
     // [9][V][P][S] index
-    constexpr int NMID = 3 * V * P * S, NROW = (BN ? 2 : 1) * V * P, NOUT = BN ? 6 : 2;
+    constexpr int NMID = 3 * V * P * S, NROW = V * P, NOUT = BN ? 8 : 2;
     for (int q = t; q < NMID + NOUT * NROW; q += NT) {
       int n, v, kk, sb;
       if (q < NMID) {
@@ -320,11 +322,12 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
         kk = (r / S) % P;
         sb = r % S;
       } else if constexpr (BN) {
-        const int q2 = q - NMID, n6 = q2 / NROW, r2 = q2 % NROW;
-        n = n6 < 3 ? n6 : n6 + 3;
-        v = r2 / (2 * P);
-        kk = (r2 >> 1) % P;
-        sb = (n < 3 ? S - 2 : 0) + (r2 & 1);
+        // rows 0..7: (n, sb) = (1, S-2) (1, S-1) (7, 0) (7, 1) (0, S-1) (2, S-1) (6, 0) (8, 0)
+        const int q2 = q - NMID, row = q2 / NROW, r2 = q2 % NROW;
+        n = row < 2 ? 1 : row < 4 ? 7 : row == 4 ? 0 : row == 5 ? 2 : row == 6 ? 6 : 8;
+        v = r2 / P;
+        kk = r2 % P;
+        sb = row < 2 ? S - 2 + row : row < 4 ? row - 2 : row < 6 ? S - 1 : 0;
       } else {
         const int q2 = q - NMID, r2 = q2 % NROW;
         n = q2 < NROW ? 1 : 7;
@@ -340,15 +343,23 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
       LYN[((n * V + v) * P + kk) * S + sb] = ly;
     }
     __syncthreads();
-    // Baer-Nunziato: subcells -1 .. S+2 in both directions; Euler: the S x S
-    // interior and the four strips beside it (columns 1..S of rows 0..S+1,
-    // then columns 0 and S+1 of rows 1..S)
-    constexpr int NX = BN ? R * R : S * S + 4 * S;
+    // Baer-Nunziato: subcells 0 .. S+1 in both directions, then the four
+    // strips of the second ring beside the edges (columns -1 and S+2 of rows
+    // 1..S, rows -1 and S+2 of columns 1..S); Euler: the S x S interior and
+    // the four strips beside it (columns 1..S of rows 0..S+1, then columns 0
+    // and S+1 of rows 1..S)
+    constexpr int NX = BN ? H * H + 4 * S : S * S + 4 * S;
     for (int p = t; p < NX; p += NT) {
       int ii, jj;
       if constexpr (BN) {
-        ii = p % R - 1;
-        jj = p / R - 1;
+        if (p < H * H) {
+          ii = p % H;
+          jj = p / H;
+        } else {
+          const int p2 = p - H * H, side = p2 / S, o = 1 + p2 % S;
+          ii = side == 0 ? -1 : side == 1 ? S + 2 : o;
+          jj = side < 2 ? o : (side == 2 ? -1 : S + 2);
+        }
       } else if (p < S * (S + 2)) {
         ii = 1 + p % S;
         jj = p / S;
@@ -419,9 +430,9 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
         else { ii = H - 1; jj = 1 + (r - 2 * H - S); }
       }
       const bool interior = p < S * S;
+      // the corners of the ring feed no edge (Euler does not gather them)
+      if (!interior && (ii == 0 || ii == H - 1) && (jj == 0 || jj == H - 1)) continue;
       if (!BN && !interior) {
-        // the corners are neither gathered nor read by an edge
-        if ((ii == 0 || ii == H - 1) && (jj == 0 || jj == H - 1)) continue;
 #pragma unroll
         for (int v = 0; v < V; ++v) {
           const T q = SU(v, ii, jj);
