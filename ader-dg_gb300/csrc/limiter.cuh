@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(256) k_mark(BatchArgs a) {
 template <class Sys, int N, class T>
 struct SubCfg {
   static constexpr int P = N + 1, P2 = P * P, S = 2 * N + 1, V = Sys::V;
-  static constexpr int R = S + 4;  // gathered region: subcells -1 .. S+2 (1-based)
+  static constexpr int R = S + 4;  // room of the gathered subcells -1 .. S+2 (1-based; Euler reads 0 .. S+1)
   static constexpr int H = S + 2;  // reconstructed region: 0 .. S+1
   static constexpr int THREADS = 128;
   // CTAs per SM the register allocation aims at.  FP32: one more than the
