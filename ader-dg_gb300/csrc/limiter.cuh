@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(SubCfg<Sys, N, T>::THREADS, SubCfg<Sys, N, T>:
   unsigned long long* cmaxp = reinterpret_cast<unsigned long long*>(misc + 8);
   long long* nbc = reinterpret_cast<long long*>(misc + 16);  // 3x3 neighbour cells, n = (bi+1) + 3 (bj+1)
   int* nbs = reinterpret_cast<int*>(misc + 16 + 9 * 8);     // their status (0: project olduh)
-  unsigned* amax = reinterpret_cast<unsigned*>(nbs + 9);     // FP32-mixed: max |UN| per variable
+  unsigned* amax = reinterpret_cast<unsigned*>(nbs + 9);     // FP32-wide: max |UN - UN(node 0)| per variable
   float* UNf = reinterpret_cast<float*>(wLy);                // FP32 DMP (after the re-solve)
   float* LYf = UNf + V * P2;
   float* LBf = LYf + V * S * P;
