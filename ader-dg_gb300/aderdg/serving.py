@@ -24,10 +24,10 @@ import time
 
 import numpy as np
 
+from . import workloads
 from .core import FP64, SYS_ADVDIFF, Batch, PinnedArray, project_initial_condition
 
 ENONFINITE = -5  # aderdg_status: the simulation's time step became non-finite
-from . import workloads
 
 
 class Request:
@@ -62,7 +62,7 @@ def poisson_arrivals(n, rate, seed):
     if not np.isfinite(rate) or rate <= 0:
         return np.zeros(n)
     rng = np.random.default_rng(seed + 1000)
-    return np.cumsum(rng.exponential(1.0 / rate, size=n)) - 0.0
+    return np.cumsum(rng.exponential(1.0 / rate, size=n))
 
 
 class Server:
