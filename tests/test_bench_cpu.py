@@ -46,3 +46,52 @@ def test_study_orders(monkeypatch):
     assert "order_l1" not in out["grids"][0]
     for g in out["grids"][1:]:
         assert abs(g["order_l1"] - 5.0) < 1e-12 and abs(g["order_linf"] - 5.0) < 1e-12
+
+
+def test_clock_summary_flags_throttling():
+    """The clocks record of a timed region: median SM clock, the maximum, and
+    every throttle reason seen active (the fields of nvidia-smi's query)."""
+    sys.path.insert(0, REPO)
+    import bench
+    c = bench.ClockSampler()
+    assert c.summary()["reasons"] == ["nvidia-smi unavailable"]
+    row = "0, {sm}, 2070, 900.0, 0x0, {hw}, Not Active, Not Active, {cap}"
+    rows = ((2070, "Not Active", "Not Active"), (1980, "Not Active", "Active"), (2070, "Active", "Not Active"))
+    for sm, hw, cap in rows:
+        c.samples.append([x.strip() for x in row.format(sm=sm, hw=hw, cap=cap).split(",")])
+    s = c.summary()
+    assert s["sm_mhz"] == 2070.0 and s["sm_max_mhz"] == 2070.0 and s["samples"] == 3
+    assert s["reasons"] == ["hw_slowdown", "sw_power_cap"]
+    c.samples = [[x.strip() for x in row.format(sm="[N/A]", hw="Not Active", cap="Not Active").split(",")]]
+    assert c.summary()["sm_mhz"] is None
+
+
+def test_error_summary():
+    """error_vs_fp64: per-request relative errors and troubled-cell counts."""
+    sys.path.insert(0, REPO)
+    import bench
+    errs = [dict(rel_l1=1e-7 * k, rel_linf=1e-6 * k, limited=10 + (k == 3), limited_fp64=10, mask_diff=int(k == 3))
+            for k in range(1, 5)]
+    s = bench._err_stats(errs)
+    assert s["requests"] == 4 and s["max_l1"] == 4e-7 and s["max_linf"] == 4e-6
+    assert abs(s["median_l1"] - 2.5e-7) < 1e-20
+    assert s["limited_cells_fp64"] == 40 and s["mask_disagreements"] == 1
+    assert abs(s["max_count_diff_pct"] - 10.0) < 1e-12 and abs(s["total_count_diff_pct"] - 2.5) < 1e-12
+
+
+def test_traffic_from_the_committed_table():
+    """roofline.traffic: the committed per-(system, N) bytes per unit times the
+    units; None when a group has no capture."""
+    sys.path.insert(0, REPO)
+    import bench
+    with open(os.path.join(REPO, "profiles", "traffic.json")) as fh:
+        tr = json.load(fh)
+    per = tr["k_subcell_bytes_per_listed_cell"]["fp32"]
+    units = {(1, 3): 100, (2, 3): 7}
+    tot, lim = bench._traffic(units, "k_subcell_bytes_per_listed_cell", "fp32")
+    assert abs(tot - (100 * per["1_3"] + 7 * per["2_3"])) < 1e-6 and "FP64 pipe" in lim
+    assert bench._traffic({(2, 9): 1}, "k_subcell_bytes_per_listed_cell", "fp32")[0] is None
+    for key in ("k_predictor_bytes_per_dof", "k_subcell_bytes_per_listed_cell"):
+        for s in (1, 2):
+            for n in (2, 3, 4, 5):
+                assert tr[key]["fp32"]["%d_%d" % (s, n)] > 0, (key, s, n)

@@ -291,8 +291,9 @@ def _smooth_bn(cfg, N, I, J):
                 rs, us, vs, p_s = 1.0 + 0.1 * math.cos(0.7 * x), 0.2 * math.sin(0.5 * y), 0.1 * math.cos(0.6 * x), 1.0
                 rg, ug, vg, p_g = 0.5 + 0.05 * math.sin(0.8 * y), 0.1 * math.cos(0.4 * x), 0.2, 1.0 + 0.1 * math.sin(x)
                 q0, q4 = a * rs, (1.0 - a) * rg
-                uh[j, i, node] = [q0, q0 * us, q0 * vs, q0 * (0.5 * (us * us + vs * vs) + (p_s + gs * ps) / (rs * (gs - 1.0))),
-                                  q4, q4 * ug, q4 * vg, q4 * (0.5 * (ug * ug + vg * vg) + (p_g + gg * pg) / (rg * (gg - 1.0))), a]
+                es = 0.5 * (us * us + vs * vs) + (p_s + gs * ps) / (rs * (gs - 1.0))
+                eg = 0.5 * (ug * ug + vg * vg) + (p_g + gg * pg) / (rg * (gg - 1.0))
+                uh[j, i, node] = [q0, q0 * us, q0 * vs, q0 * es, q4, q4 * ug, q4 * vg, q4 * eg, a]
     return uh.ravel()
 
 
