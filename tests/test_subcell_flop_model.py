@@ -1,9 +1,9 @@
-"""The Euler subcell re-solve's flop model against an instrumented count.
+"""The subcell re-solve's flop model against an instrumented count.
 
 `bench.subcell_flops_per_cell` gives the roofline's algorithmic flops of the
 subcell re-solve kernel (k_subcell), the dominant kernel of the FP32-mixed
-step.  Here the re-solve of one Euler cell is restated in Python on the
-counting scalar of test_flop_model (every +, -, *, /, sqrt on data is one
+step.  Here the re-solve of one cell is restated in Python on the counting
+scalar of test_flop_model (every +, -, *, /, sqrt on data is one
 flop, a fused multiply-add 2, an accumulation of n terms from zero 2n - 1;
 compares, min/max, |x| and sign tests are free), computing exactly what the
 result needs:
@@ -23,11 +23,17 @@ result needs:
 - the CFL denominator of every node of the new polynomial
   (Euler/calc_time_step.f90:9-52).
 
+Baer-Nunziato (resolve_cell_bn) adds the slopes, the NCP source and the half
+step on the halo subcells (two rings of neighbour subcells; the ring's
+corners feed no edge), the path-conservative fluctuation of every edge and
+the NCP source at the half step in the finite-volume update.
+
 The restatement's results are checked against the oracle's limiter step on a
-5 x 5 isentropic vortex whose centre cell is forced troubled
-(recompute = 1; its edge neighbours become recompute = 2): the new subcell
-data, the new polynomial and the DMP verdict of a recompute = 2 neighbour.
-The model must equal the count exactly.
+5 x 5 grid (the isentropic vortex; a smooth two-phase state for
+Baer-Nunziato) whose centre cell is forced troubled (recompute = 1; its edge
+neighbours become recompute = 2): the new subcell data, the new polynomial
+and the DMP verdict of a recompute = 2 neighbour.  The model must equal the
+count exactly.
 """
 import math
 
