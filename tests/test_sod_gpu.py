@@ -1,5 +1,6 @@
 """Sod's shock tube on the GPU path, Euler and both phases of Baer-Nunziato,
-against the exact Riemann solution.
+against the exact Riemann solution; and a Baer-Nunziato material interface
+that must stay in pressure-velocity equilibrium.
 
 The flows and the exact solver are those of the oracle's known-answer tests
 (test_oracle_kat.py): a one-dimensional strip (periodic in y, transmissive in
@@ -84,3 +85,27 @@ def test_bn_sod_both_phases(gpu_lib, prec):
     tol = 1e-6 if prec == aderdg.FP64 else 0.05
     assert abs(err - ref) <= tol * ref, (err, ref)
     assert limited > 0
+
+
+@pytest.mark.parametrize("prec", [aderdg.FP64, aderdg.FP32_MIXED])
+def test_bn_interface_equilibrium(gpu_lib, prec):
+    """A material interface in pressure-velocity equilibrium stays in it on the
+    GPU path (test_oracle_kat.bn_interface_state): FP64 to rounding like the
+    oracle, FP32-mixed to the FP32 contractions' rounding (measured on the
+    GB300: 3.7e-14 and 2.1e-6)."""
+    from test_oracle_kat import bn_equilibrium_deviation, bn_interface_state
+    n = 100
+    cfg = aderdg.Config(system=aderdg.SYS_BN, N=N, imax=n, jmax=J, xl=(0.0, 0.0), xr=(1.0, J / n),
+                        bc=(3, 3, 3, 3), limiter=1, precision=prec, gamma_s=1.4, gamma_g=1.4, pi_s=0.0, pi_g=0.0)
+    uh, lh = bn_interface_state(n, N)
+    s = aderdg.Solver(cfg)
+    s.upload(uh)
+    s.init_limiter(lh)
+    t, _ = s.run(0.0, 0.1, 1000000)
+    assert t == 0.1
+    out, _ = s.download()
+    s.close()
+    du, dp = bn_equilibrium_deviation(out)
+    print("BN interface, precision %d: |u - 1| %.2e, |p - 1| %.2e" % (prec, du, dp))
+    tol = 1e-12 if prec == aderdg.FP64 else 1e-5
+    assert du < tol and dp < tol, (du, dp)
